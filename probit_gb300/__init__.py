@@ -1,0 +1,25 @@
+"""probit_gb300: GB300-native (sm_103a) Laplace approximate inference for GPs.
+
+A drop-in for the Laplace path of the reference package (bb515/probit):
+``LaplaceGP`` with ``weight``, ``precision``, ``approximate_posterior``,
+``objective``, ``value_and_grad`` and ``predict``, computed by hand-written
+CUDA kernels behind the C-ABI declared in ``include/probit_gb300.h``.
+"""
+
+from .approximators import LaplaceGP
+from .kernels import EQ, Matern12
+from .utilities import (
+    check_cutpoints,
+    grad_log_probit_likelihood,
+    hessian_log_probit_likelihood,
+    log_gaussian_likelihood,
+    log_probit_likelihood,
+    log_probit_likelihood_stable,
+)
+
+__all__ = [
+    "LaplaceGP", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
+    "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
+    "check_cutpoints",
+]
+__version__ = "0.1.0"

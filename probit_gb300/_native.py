@@ -1,0 +1,134 @@
+"""ctypes binding of ``libprobit_gb300.so`` (the C-ABI of include/probit_gb300.h).
+
+The library is the only compute path: if it is missing or cannot be loaded,
+every entry point raises ``NativeLibraryError``; there is no CPU fallback.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+import threading
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libprobit_gb300.so"
+HEADER = _PKG.parent / "include" / "probit_gb300.h"
+
+PGB_OK = 0
+PGB_EINVAL = -1
+PGB_ENOMEM = -2
+PGB_ECUDA = -3
+PGB_ENOTPD = -4
+PGB_ENAN = -5
+PGB_ETIMEOUT = -6
+PGB_EUNSUPPORTED = -7
+PGB_ESTATE = -8
+
+KERNEL_EQ = 0
+KERNEL_MATERN12 = 1
+KERNEL_EQ_PERIODIC = 2
+
+LIK_GAUSSIAN = 0
+LIK_PROBIT = 1
+LIK_PROBIT_STABLE = 2
+
+MAX_D = 16
+
+
+class NativeLibraryError(RuntimeError):
+    """The CUDA library is missing or failed to load."""
+
+
+class PgbError(RuntimeError):
+    """A C-ABI call returned a negative status."""
+
+    def __init__(self, code: int, where: str):
+        self.code = code
+        super().__init__(f"{where}: {strerror(code)} ({code})")
+
+
+class Desc(C.Structure):
+    _fields_ = [
+        ("n", C.c_int32),
+        ("d", C.c_int32),
+        ("kernel", C.c_int32),
+        ("n_lengthscales", C.c_int32),
+        ("period", C.c_float),
+        ("likelihood", C.c_int32),
+        ("j", C.c_int32),
+        ("tolerance", C.c_float),
+        ("maxiter", C.c_int32),
+        ("flags", C.c_int32),
+    ]
+
+
+class Status(C.Structure):
+    _fields_ = [
+        ("code", C.c_int32),
+        ("iterations", C.c_int32),
+        ("notpd_col", C.c_int32),
+        ("converged", C.c_int32),
+    ]
+
+
+_VP = C.c_void_p
+_SIGS = {
+    "pgb_version": (C.c_char_p, []),
+    "pgb_strerror": (C.c_char_p, [C.c_int]),
+    "pgb_theta_size": (C.c_int, [C.POINTER(Desc)]),
+    "pgb_gp_create": (C.c_int, [C.POINTER(Desc), C.POINTER(_VP)]),
+    "pgb_gp_destroy": (C.c_int, [_VP]),
+    "pgb_gp_status": (C.c_int, [_VP, C.POINTER(Status), _VP]),
+    "pgb_gram": (C.c_int, [C.POINTER(Desc), _VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int64, _VP]),
+    "pgb_log_likelihood": (C.c_int, [C.POINTER(Desc), _VP, _VP, _VP, C.c_int32, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_weight": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_precision": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_approximate_posterior": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_factor": (C.c_int, [_VP, _VP]),
+    "pgb_predict": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, _VP, C.c_int32, _VP]),
+}
+
+_lib = None
+_lock = threading.Lock()
+
+
+def exported_symbols() -> list[str]:
+    """Names of the functions the C-ABI binding declares."""
+    return list(_SIGS)
+
+
+def load(path: str | os.PathLike | None = None) -> C.CDLL:
+    """Load the library once (raises ``NativeLibraryError`` if it is absent)."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        p = Path(path) if path else LIB_PATH
+        if not p.exists():
+            raise NativeLibraryError(
+                f"{p} not found: build it with `python -m probit_gb300.build` (nvcc, sm_103a)")
+        try:
+            lib = C.CDLL(str(p))
+        except OSError as e:  # pragma: no cover - depends on the host
+            raise NativeLibraryError(f"cannot load {p}: {e}") from e
+        for name, (res, args) in _SIGS.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+        return lib
+
+
+def strerror(code: int) -> str:
+    try:
+        return load().pgb_strerror(int(code)).decode()
+    except NativeLibraryError:
+        return f"error {code}"
+
+
+def check(code: int, where: str) -> None:
+    if code != PGB_OK:
+        raise PgbError(code, where)

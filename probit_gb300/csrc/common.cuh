@@ -1,0 +1,196 @@
+// Shared device helpers for the probit_gb300 CUDA library (sm_103a).
+//
+// Hyperparameter block layout (float32, device memory), the same layout the
+// C-ABI documents in include/probit_gb300.h:
+//   theta = [ l_0 .. l_{nl-1}, s, sigma_n, b_0 .. b_J ]
+// nl = 1 (isotropic) or D (ARD); s = signal variance; sigma_n = noise std;
+// b = ordinal cutpoints (probit only; b_0 = -inf, b_J = +inf).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <math.h>
+
+#include "../../include/probit_gb300.h"
+
+namespace pgb {
+
+constexpr int T = 128;           // tile edge of every blocked matrix
+constexpr int MAX_D = 16;        // input dimensions handled by the kernels
+constexpr int MAX_THETA = 64;    // entries of one hyperparameter block
+
+// Device status word layout (int32[8]) shared by every kernel of one GP.
+enum StatusSlot {
+  ST_CODE = 0,        // first error code (PGB_E*), 0 = ok
+  ST_ITERS = 1,       // Newton iterations done
+  ST_NOTPD_COL = 2,   // first column whose pivot was not positive (or -1)
+  ST_ABORT = 3,       // set by any kernel that gave up waiting
+  ST_CONVERGED = 4,   // 1 once the fixed point test passed
+  ST_SPARE0 = 5,
+  ST_SPARE1 = 6,
+  ST_SPARE2 = 7,
+};
+
+// ---------------------------------------------------------------- memory order
+__device__ __forceinline__ int ld_acquire(const int* p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ void st_release(int* p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed(const int* p) {
+  int v;
+  asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ __forceinline__ uint64_t global_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait for *flag >= target.  Gives up after `limit_ns` of wall time
+// or as soon as another block has raised the abort word; a give-up raises the
+// abort word itself (with PGB_ETIMEOUT as the status code when none is set)
+// so every other waiter of this launch returns promptly.  Returns true when
+// the flag was seen.
+constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;   // 4 s
+__device__ __forceinline__ bool wait_flag_geq(const int* flag, int target, int* status) {
+  if (ld_acquire(flag) >= target) return true;
+  const uint64_t t0 = global_ns();
+  unsigned ns = 32;
+  while (true) {
+    if (ld_acquire(flag) >= target) return true;
+    if (ld_relaxed(status + ST_ABORT)) return false;
+    if (global_ns() - t0 > WAIT_LIMIT_NS) {
+      atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
+      atomicExch(status + ST_ABORT, 1);
+      return false;
+    }
+    __nanosleep(ns);
+    if (ns < 1024) ns <<= 1;
+  }
+}
+
+__device__ __forceinline__ void raise_status(int* status, int code) {
+  atomicCAS(status + ST_CODE, 0, code);
+}
+
+// ---------------------------------------------------------------- kernels
+// Kernel functions restated from mlkernels' EQ / Matern12 / EQ.periodic(p)
+// with ``stretch``: the inputs are divided by the lengthscale before the
+// distance (features are prepared by prep_features).  For the periodic
+// kernel the stored features are the raw inputs and the distance is
+// q_d = (2 sin(pi (x_d - z_d) / p) / l_d)^2.
+struct KernelParams {
+  int kind;        // PGB_KERNEL_*
+  int D;           // input dims
+  int Dp;          // feature row stride (floats)
+  int nl;          // number of lengthscales (1 or D)
+  float s;         // signal variance
+  float pi_over_p; // pi / period (periodic only)
+  float inv_l[MAX_D];   // 1/l_d (periodic: used after the sine)
+  float l[MAX_D];
+};
+
+__device__ __forceinline__ float sq_dist_dim(const KernelParams& kp, float xi, float xj, int d) {
+  if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
+    const float t = (xi - xj) * kp.pi_over_p;
+    const float v = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
+    return v * v;
+  }
+  const float v = xi - xj;
+  return v * v;
+}
+
+// k(r) * s from the summed scaled squared distance.
+__device__ __forceinline__ float kernel_from_d2(const KernelParams& kp, float d2) {
+  if (kp.kind == PGB_KERNEL_MATERN12) return kp.s * expf(-sqrtf(d2));
+  return kp.s * expf(-0.5f * d2);
+}
+
+__device__ __forceinline__ float kernel_eval(const KernelParams& kp, const float* xi, const float* xj) {
+  float d2 = 0.0f;
+  for (int d = 0; d < kp.D; ++d) d2 += sq_dist_dim(kp, xi[d], xj[d], d);
+  return kernel_from_d2(kp, d2);
+}
+
+// ---------------------------------------------------------------- reductions
+__device__ __forceinline__ float warp_sum(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double warp_sum_d(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block-wide sum of one float per thread into a double (deterministic order).
+template <int NT>
+__device__ __forceinline__ double block_sum_d(float v, double* smem_red) {
+  double w = warp_sum_d((double)v);
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) smem_red[warp] = w;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < NT / 32; ++i) r += smem_red[i];
+    smem_red[0] = r;
+  }
+  __syncthreads();
+  r = smem_red[0];
+  __syncthreads();
+  return r;
+}
+
+__host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+}  // namespace pgb
+
+namespace pgb {
+
+// Static shape of one GP problem (kernel arguments by value).
+struct Shape {
+  int n;          // training points
+  int D;          // input dims
+  int Dp;         // feature row stride (floats, multiple of 4)
+  int kind;       // PGB_KERNEL_*
+  int nl;         // lengthscales (1 or D)
+  int lik;        // PGB_LIK_*
+  int J;          // ordinal classes
+  float pi_over_p;  // pi / period
+};
+
+// Build the kernel parameters from the device hyperparameter block.
+__device__ __forceinline__ KernelParams make_kp(const Shape& sh, const float* __restrict__ theta) {
+  KernelParams kp;
+  kp.kind = sh.kind;
+  kp.D = sh.D;
+  kp.Dp = sh.Dp;
+  kp.nl = sh.nl;
+  kp.pi_over_p = sh.pi_over_p;
+#pragma unroll 1
+  for (int d = 0; d < sh.nl; ++d) {
+    kp.l[d] = __ldg(theta + d);
+    kp.inv_l[d] = 1.0f / kp.l[d];
+  }
+  kp.s = __ldg(theta + sh.nl);
+  return kp;
+}
+
+__device__ __forceinline__ float theta_sigma(const Shape& sh, const float* theta) {
+  return __ldg(theta + sh.nl + 1);
+}
+__device__ __forceinline__ const float* theta_cutpoints(const Shape& sh, const float* theta) {
+  return theta + sh.nl + 2;
+}
+__host__ __device__ inline int theta_len(int nl, int lik, int J) {
+  return nl + 2 + (lik == PGB_LIK_GAUSSIAN ? 0 : J + 1);
+}
+
+}  // namespace pgb

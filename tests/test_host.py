@@ -1,0 +1,88 @@
+"""Host-side logic of the drop-in API (no GPU needed)."""
+
+import math
+
+import numpy as np
+import pytest
+
+import probit_gb300 as pg
+from probit_gb300 import _native as N
+from probit_gb300.approximators import LaplaceGP, tree_leaves, tree_map
+from probit_gb300.kernels import EQ, Matern12, resolve
+from probit_gb300.utilities import check_cutpoints, CutpointValueError, likelihood_mode
+
+
+def test_kernel_composition_like_mlkernels():
+    s = resolve(2.0 * EQ().stretch(0.5).periodic(0.25))
+    assert (s.kind, s.lengthscale, s.variance, s.period) == ("eq_periodic", 0.5, 2.0, 0.25)
+    s = resolve(Matern12().stretch(np.array([1.0, 2.0])) * 3.0)
+    assert s.kind == "matern12" and s.variance == 3.0 and list(s.lengthscale) == [1.0, 2.0]
+    assert resolve(EQ()).lengthscale == 1.0
+    with pytest.raises(NotImplementedError):
+        EQ().periodic(1.0).stretch(2.0)
+    with pytest.raises(NotImplementedError):
+        Matern12().periodic(1.0)
+    with pytest.raises(NotImplementedError):
+        EQ() + EQ()
+    with pytest.raises(NotImplementedError):
+        resolve(object())
+
+
+def test_kernel_scaling_keeps_torch_graph():
+    import torch
+
+    ell = torch.tensor(0.7, dtype=torch.float64, requires_grad=True)
+    s = torch.tensor(1.3, dtype=torch.float64, requires_grad=True)
+    spec = resolve(s * EQ().stretch(ell))
+    (spec.lengthscale * 2 + spec.variance).backward()
+    assert ell.grad.item() == 2.0 and s.grad.item() == 1.0
+
+
+def test_likelihood_mode_identity():
+    assert likelihood_mode(pg.log_gaussian_likelihood) == N.LIK_GAUSSIAN
+    assert likelihood_mode(pg.log_probit_likelihood) == N.LIK_PROBIT
+    assert likelihood_mode(pg.log_probit_likelihood_stable, pg.grad_log_probit_likelihood,
+                           pg.hessian_log_probit_likelihood) == N.LIK_PROBIT_STABLE
+    with pytest.raises(NotImplementedError):
+        likelihood_mode(lambda f, y, p: f)
+    with pytest.raises(NotImplementedError):
+        likelihood_mode(pg.log_probit_likelihood, pg.grad_log_probit_likelihood)
+
+
+def test_reference_functions_recognised_by_name():
+    def log_probit_likelihood(f, y, p):
+        return f
+
+    log_probit_likelihood.__module__ = "probit.utilities"
+    assert likelihood_mode(log_probit_likelihood) == N.LIK_PROBIT
+
+
+def test_check_cutpoints_forms():
+    assert np.array_equal(check_cutpoints([-0.5, 0.5], 3), [-math.inf, -0.5, 0.5, math.inf])
+    assert np.array_equal(check_cutpoints([-math.inf, -0.5, 0.5], 3), [-math.inf, -0.5, 0.5, math.inf])
+    assert np.array_equal(check_cutpoints([-0.5, 0.5, math.inf], 3), [-math.inf, -0.5, 0.5, math.inf])
+    with pytest.raises(CutpointValueError):
+        check_cutpoints([0.5, -0.5], 3)
+    with pytest.raises(ValueError):
+        check_cutpoints([1.0, 2.0, 3.0, 4.0, 5.0], 3)
+
+
+def test_pytree_helpers():
+    t = ((1.0, np.array([1.0, 2.0])), (0.3, [4.0, {"a": 5.0}]))
+    assert len(tree_leaves(t)) == 5
+    d = tree_map(lambda x: np.asarray(x) * 2, t)
+    assert float(d[1][1][1]["a"]) == 10.0
+
+
+def test_laplacegp_theta_layout_and_key():
+    X = np.zeros((5, 2), np.float32)
+    y = np.zeros(5, np.int32)
+    gp = LaplaceGP((X, y), lambda p: p[1] * Matern12().stretch(p[0]), pg.log_probit_likelihood)
+    theta, key = gp._theta(((np.array([0.5, 0.7]), 1.5), (0.6, [-np.inf, 0.0, np.inf])))
+    assert theta.tolist() == [0.5, 0.7, 1.5, 0.6, -np.inf, 0.0, np.inf]
+    assert key == (N.KERNEL_MATERN12, 2, 1.0, 2)
+    with pytest.raises(ValueError):
+        gp._theta(((np.array([0.5, 0.7, 0.1]), 1.5), (0.6, [-np.inf, 0.0, np.inf])))
+    with pytest.raises(ValueError):
+        LaplaceGP((np.zeros(5), y), lambda p: EQ(), pg.log_probit_likelihood)
+    assert repr(gp) == "LaplaceGP"
