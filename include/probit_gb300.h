@@ -104,6 +104,19 @@ int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream);
 int pgb_gram(const pgb_desc* desc, const float* theta, const float* X1, int32_t n1,
              const float* X2, int32_t n2, float* K, int64_t ldk, void* stream);
 
+/* pgb_gram without any device allocation, for callers that must not
+ * allocate while they run (XLA FFI custom calls under JAX's preallocating
+ * allocator, work recorded by a framework's stream capture, services that
+ * reserve memory at start-up).  This entry point has no counterpart in the
+ * reference.  Its scratch is a fixed 4 MiB array inside the library, held by
+ * every GPU that loads it: (n1 + n2) * ceil4(d) must not exceed 1,048,576
+ * floats, else PGB_EUNSUPPORTED.  All calls share that array, so calls whose
+ * work overlaps on the GPU race; order them on one stream.  The first call on
+ * a device resolves the array's address and may load device code: make it
+ * before any stream capture. */
+int pgb_gram_noalloc(const pgb_desc* desc, const float* theta, const float* X1, int32_t n1,
+                     const float* X2, int32_t n2, float* K, int64_t ldk, void* stream);
+
 /* Per-point log p(y|f) and its first three derivatives in f (any output may
  * be NULL).  Replaces the jit(vmap(...)) likelihood wrappers of
  * Approximator.__init__ (approximators.py:92-104) over log_probit_likelihood /
