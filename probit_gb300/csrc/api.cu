@@ -61,21 +61,24 @@ struct pgb_gp {
   // features and factor
   float* Xf = nullptr;
   float* L = nullptr;
+  float* Linv = nullptr;   // inverses of the diagonal tiles of L (nt x T x T)
   float* Rv = nullptr;     // RHS_VEC row tile (T x ld)
   float* Rz = nullptr;     // RHS_IDENT rows (n_pad x ld): L^-T
   float* Binv = nullptr;   // n_pad x ld
   // vectors (n_pad)
-  // b holds the Newton residual r = d1 - a
+  // b holds the Newton residual r = d1 - a, t the right-hand side r / sqrt W
   float *a = nullptr, *f = nullptr, *d1 = nullptr, *W = nullptr, *sw = nullptr, *b = nullptr, *t = nullptr,
         *x = nullptr, *logp = nullptr, *d3 = nullptr, *dsig = nullptr, *svec = nullptr, *rv = nullptr,
         *zbar = nullptr, *tz = nullptr, *y2 = nullptr, *Ky2 = nullptr, *u = nullptr, *c = nullptr,
         *rowdot = nullptr;
+  float* sw_prev = nullptr; // sqrt W of the resident factor (bitwise reuse test)
+  int* reuse = nullptr;    // [0] factor valid, [1] W differs, [2] reuse decision
   float* scal = nullptr;   // [0] err, [1] value
   float* grad = nullptr;
   int* status = nullptr;
   int* ready = nullptr;    // (2 nt) x nt
-  int* counters = nullptr; // [0] dag, [1] trsv
-  int* tflags = nullptr;   // nt
+  int* counters = nullptr; // [0] dag, [1] trsv (trans), [2] predict dag, [3] trsv (lower)
+  int* tflags = nullptr;   // 2 nt: trans solve, lower solve
   double* part = nullptr;
   double* tpart = nullptr;
   double* lpart = nullptr;
@@ -99,6 +102,7 @@ struct pgb_gp {
   cudaGraphExec_t gexec[OP_COUNT] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t cap_s = nullptr, cap_s2 = nullptr;
   int grad_ready = 0;      // Rz / Binv allocated
+  int eager = 0;           // PGB_EAGER=1: launch kernels directly, host-driven Newton loop
   int factor_valid = 0;    // L is the factor of B at the resident W (same theta)
 };
 
@@ -201,19 +205,25 @@ void enq_newton_step(pgb_gp* gp, cudaStream_t s, cudaGraphConditionalHandle h, i
   const Shape& sh = gp->sh;
   // f = K a
   launch_gram_matvec(sh, gp->theta, gp->Xf, gp->n, gp->Xf, gp->n, nullptr, 0, gp->a, nullptr, gp->f, s);
-  // d1, W, sqrt W, r = d1 - a
-  launch_newton_lik(sh, gp->theta, gp->f, gp->y_in, gp->a, gp->n_pad, gp->d1, gp->W, gp->sw, gp->b, s);
-  // t = W^1/2 K r
-  launch_gram_matvec(sh, gp->theta, gp->Xf, gp->n, gp->Xf, gp->n, nullptr, 0, gp->b, gp->sw, gp->t, s);
-  // L L^T = B and w = L^-1 t in one factorisation
+  // d1, W, sqrt W, r = d1 - a, t = r / sqrt W
+  launch_newton_lik(sh, gp->theta, gp->f, gp->y_in, gp->a, gp->n_pad, gp->d1, gp->W, gp->sw, gp->b, gp->t, s);
+  // bitwise-unchanged W keeps the resident factor
+  launch_reuse_check(gp->n, gp->sw, gp->sw_prev, gp->reuse, s);
+  // new W: L L^T = B and w = L^-1 t in one factorisation (skipped on reuse)
   enq_dag(gp, JOB_VEC, s);
+  launch_reuse_mark_valid(gp->reuse, gp->status, s);
+  // reused W: w = L^-1 t by the forward wavefront solve (skipped otherwise)
+  cudaMemsetAsync(gp->tflags + gp->nt, 0, sizeof(int) * gp->nt, s);
+  cudaMemsetAsync(gp->counters + 3, 0, sizeof(int), s);
+  launch_trsv(gp->n, gp->nt, gp->ld, gp->L, gp->Linv, gp->t, gp->Rv, 0, gp->tflags + gp->nt, gp->counters + 3, gp->status,
+              std::min(gp->nt, gp->num_sms), gp->reuse + 2, 1, s);
   // x = L^-T w
   cudaMemsetAsync(gp->tflags, 0, sizeof(int) * gp->nt, s);
   cudaMemsetAsync(gp->counters + 1, 0, sizeof(int), s);
-  launch_trsv(gp->n, gp->nt, gp->ld, gp->L, gp->Rv, gp->x, 1, gp->tflags, gp->counters + 1, gp->status,
-              std::min(gp->nt, gp->num_sms), s);
-  // a += r - W^1/2 x, stopping rule
-  launch_newton_update(gp->n, gp->b, gp->sw, gp->x, gp->a, gp->part, s);
+  launch_trsv(gp->n, gp->nt, gp->ld, gp->L, gp->Linv, gp->Rv, gp->x, 1, gp->tflags, gp->counters + 1, gp->status,
+              std::min(gp->nt, gp->num_sms), nullptr, 0, s);
+  // a += W^1/2 x, stopping rule
+  launch_newton_update(gp->n, gp->sw, gp->x, gp->a, gp->part, s);
   launch_newton_finalize(gp->part, ceil_div(gp->n, 256), gp->desc.tolerance, gp->desc.maxiter, gp->status,
                          gp->scal, h, use_cond, s);
 }
@@ -226,17 +236,18 @@ void enq_precision(pgb_gp* gp, cudaStream_t s) {
 void enq_grad(pgb_gp* gp, cudaStream_t s) {
   const Shape& sh = gp->sh;
   const int n = gp->n, np = gp->n_pad;
-  launch_syrk_zzt(gp->Rz, gp->ld, gp->nt, gp->tiles_lower, gp->ntiles_lower, gp->Binv, gp->ld, s);
+  cudaMemsetAsync(gp->counters + 4, 0, sizeof(int), s);
+  launch_syrk_zzt(gp->Rz, gp->ld, gp->nt, gp->tiles_lower, gp->ntiles_lower, gp->Binv, gp->ld, gp->counters + 4,
+                  gp->status, std::max(1, std::min(gp->num_sms, gp->ntiles_lower)), s);
   // rowdot_i = sum_j B^-1_ij K_ij sw_j  ->  diag(Sigma)_i = rowdot_i / sw_i
   launch_gram_matvec(sh, gp->theta, gp->Xf, n, gp->Xf, n, gp->Binv, gp->ld, gp->sw, nullptr, gp->rowdot, s);
   launch_grad_vec1(n, np, gp->rowdot, gp->sw, gp->d3, gp->a, gp->d1, gp->dsig, gp->svec, gp->rv, s);
   // zbar = K (a - d1 - s)
   launch_gram_matvec(sh, gp->theta, gp->Xf, n, gp->Xf, n, nullptr, 0, gp->rv, nullptr, gp->zbar, s);
-  // u = zbar - K W^1/2 B^-1 W^1/2 zbar
+  // u = (I + K W)^-1 zbar = W^-1/2 B^-1 W^1/2 zbar
   launch_scale_vec(n, np, gp->sw, gp->zbar, gp->tz, s);
-  launch_dense_matvec(gp->Binv, gp->ld, n, n, gp->tz, gp->sw, gp->y2, s);
-  launch_gram_matvec(sh, gp->theta, gp->Xf, n, gp->Xf, n, nullptr, 0, gp->y2, nullptr, gp->Ky2, s);
-  launch_grad_vec3(n, np, gp->zbar, gp->Ky2, gp->a, gp->d1, gp->svec, gp->W, gp->u, gp->c, s);
+  launch_dense_matvec(gp->Binv, gp->ld, n, n, gp->tz, nullptr, gp->y2, s);
+  launch_grad_vec3(n, np, gp->y2, gp->sw, gp->a, gp->d1, gp->svec, gp->W, gp->u, gp->c, s);
   launch_grad_trace(sh, gp->theta, gp->Xf, gp->Binv, gp->ld, gp->sw, gp->c, gp->a, gp->tiles_lower,
                     gp->ntiles_lower, gp->tpart, s);
   launch_grad_lik_final(sh, gp->theta, gp->f, gp->y_in, gp->dsig, gp->u, gp->tpart, gp->ntiles_lower, gp->lpart,
@@ -255,6 +266,45 @@ int ensure_grad_buffers(pgb_gp* gp) {
   return PGB_OK;
 }
 
+void enq_prologue(pgb_gp* gp, cudaStream_t s) {
+  enq_reset_status(gp, s);
+  enq_prep(gp, s);
+  cudaMemsetAsync(gp->a, 0, sizeof(float) * gp->n_pad, s);
+  cudaMemsetAsync(gp->reuse, 0, sizeof(int) * 4, s);   // new theta: no resident factor
+}
+
+void enq_epilogue(pgb_gp* gp, int op, cudaStream_t s) {
+  if (op >= OP_POSTERIOR) {
+    enq_precision(gp, s);
+    launch_reuse_check(gp->n, gp->sw, gp->sw_prev, gp->reuse, s);
+    enq_dag(gp, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
+    launch_reuse_mark_valid(gp->reuse, gp->status, s);
+    if (op >= OP_OBJECTIVE) launch_evidence(gp->n, gp->logp, gp->f, gp->a, gp->L, gp->ld, gp->part, gp->scal + 1, s);
+    if (op == OP_VG) enq_grad(gp, s);
+  }
+}
+
+// The same work without graphs: kernels launched directly, the Newton loop
+// driven from the host (one status read per step).  For profilers that do
+// not follow kernels inside conditional graph nodes.
+int run_eager(pgb_gp* gp, int op, cudaStream_t s) {
+  if (op == OP_VG) {
+    int r = ensure_grad_buffers(gp);
+    if (r != PGB_OK) return r;
+  }
+  enq_prologue(gp, s);
+  for (int it = 0; it < gp->desc.maxiter; ++it) {
+    enq_newton_step(gp, s, 0, 0);
+    int again = 0;
+    CU_TRY(cudaMemcpyAsync(&again, gp->status + ST_SPARE0, sizeof(int), cudaMemcpyDeviceToHost, s));
+    CU_TRY(cudaStreamSynchronize(s));
+    if (!again) break;
+  }
+  enq_epilogue(gp, op, s);
+  CU_TRY(cudaGetLastError());
+  return PGB_OK;
+}
+
 // Capture the graph of one operation.
 int build_graph(pgb_gp* gp, int op) {
   if (gp->gexec[op]) return PGB_OK;
@@ -265,9 +315,7 @@ int build_graph(pgb_gp* gp, int op) {
   cudaStream_t s = gp->cap_s, s2 = gp->cap_s2;
   cudaGraph_t g = nullptr;
   CU_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-  enq_reset_status(gp, s);
-  enq_prep(gp, s);
-  cudaMemsetAsync(gp->a, 0, sizeof(float) * gp->n_pad, s);
+  enq_prologue(gp, s);
   // WHILE node for the Newton loop
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg = nullptr;
@@ -289,12 +337,7 @@ int build_graph(pgb_gp* gp, int op) {
   enq_newton_step(gp, s2, h, 1);
   cudaGraph_t body_out = nullptr;
   CU_TRY(cudaStreamEndCapture(s2, &body_out));
-  if (op >= OP_POSTERIOR) {
-    enq_precision(gp, s);
-    enq_dag(gp, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
-    if (op >= OP_OBJECTIVE) launch_evidence(gp->n, gp->logp, gp->f, gp->a, gp->L, gp->ld, gp->part, gp->scal + 1, s);
-    if (op == OP_VG) enq_grad(gp, s);
-  }
+  enq_epilogue(gp, op, s);
   CU_TRY(cudaStreamEndCapture(s, &g));
   CU_TRY(cudaGraphInstantiate(&gp->gexec[op], g, 0));
   cudaGraphDestroy(g);
@@ -311,6 +354,14 @@ int ingest(pgb_gp* gp, const float* X, const void* y, const float* theta, cudaSt
 
 int run_op(pgb_gp* gp, int op, const float* X, const void* y, const float* theta, cudaStream_t s) {
   if (!y) return PGB_EINVAL;
+  if (gp->eager) {
+    int r = ingest(gp, X, y, theta, s);
+    if (r != PGB_OK) return r;
+    r = run_eager(gp, op, s);
+    if (r != PGB_OK) return r;
+    gp->factor_valid = op >= OP_POSTERIOR;
+    return PGB_OK;
+  }
   int r = build_graph(gp, op);
   if (r != PGB_OK) return r;
   r = ingest(gp, X, y, theta, s);
@@ -382,17 +433,20 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
   A(gp->theta, (size_t)MAX_THETA);
   A(gp->Xf, np * gp->sh.Dp);
   A(gp->L, mat);
+  A(gp->Linv, (size_t)gp->nt * T * T);
   A(gp->Rv, (size_t)T * gp->ld);
   float** vecs[] = {&gp->a, &gp->f, &gp->d1, &gp->W, &gp->sw, &gp->b, &gp->t, &gp->x, &gp->logp, &gp->d3,
                     &gp->dsig, &gp->svec, &gp->rv, &gp->zbar, &gp->tz, &gp->y2, &gp->Ky2, &gp->u, &gp->c,
                     &gp->rowdot};
   for (float** v : vecs) A(*v, np);
+  A(gp->sw_prev, np);
+  A(gp->reuse, 4);
   A(gp->scal, 8);
   A(gp->grad, (size_t)MAX_THETA);
   A(gp->status, kStatusWords);
   A(gp->ready, (size_t)2 * gp->nt * gp->nt);
-  A(gp->counters, 4);
-  A(gp->tflags, gp->nt);
+  A(gp->counters, 8);
+  A(gp->tflags, 2 * (size_t)gp->nt);
   A(gp->part, (size_t)ceil_div((int)np, 256) + 8);
   // lower tile pairs
   std::vector<int2> tl;
@@ -408,6 +462,7 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
   CU_TRY(cudaMemset(gp->a, 0, np * sizeof(float)));
   CU_TRY(cudaMemset(gp->Rv, 0, (size_t)T * gp->ld * sizeof(float)));
   CU_TRY(cudaMemset(gp->status, 0, kStatusWords * sizeof(int)));
+  CU_TRY(cudaMemset(gp->reuse, 0, 4 * sizeof(int)));
   // jobs
   for (int k = 0; k < JOB_COUNT; ++k) {
     DagJob& j = gp->hjobs[k];
@@ -416,19 +471,25 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
     j.nt = gp->nt;
     j.ld = gp->ld;
     j.L = gp->L;
+    j.Linv = gp->Linv;
     j.Xf = gp->Xf;
     j.sw = gp->sw;
     j.theta = gp->theta;
     j.sh = gp->sh;
     j.ready = gp->ready;
     j.status = gp->status;
+    j.reuse = gp->reuse + 2;
+    j.reuse_mode = 0;
   }
   gp->hjobs[JOB_VEC].rhs_kind = RHS_VEC;
   gp->hjobs[JOB_VEC].nrt = 1;
   gp->hjobs[JOB_VEC].nrhs = 1;
   gp->hjobs[JOB_VEC].R = gp->Rv;
   gp->hjobs[JOB_VEC].rhs_vec = gp->t;
+  gp->hjobs[JOB_VEC].reuse_mode = 2;
   gp->hjobs[JOB_NONE].rhs_kind = RHS_NONE;
+  gp->hjobs[JOB_NONE].reuse_mode = 1;
+  gp->hjobs[JOB_IDENT].reuse_mode = 1;
   gp->hjobs[JOB_IDENT].rhs_kind = RHS_IDENT;
   gp->hjobs[JOB_IDENT].nrt = gp->nt;
   gp->hjobs[JOB_IDENT].nrhs = gp->n_pad;
@@ -444,6 +505,10 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
       return rr;
     }
   }
+  {
+    const char* e = std::getenv("PGB_EAGER");
+    gp->eager = (e && e[0] == '1') ? 1 : 0;
+  }
   CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s, cudaStreamNonBlocking));
   CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s2, cudaStreamNonBlocking));
   *out = gp;
@@ -454,7 +519,7 @@ int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
   for (int k = 0; k < OP_COUNT; ++k)
     if (gp->gexec[k]) cudaGraphExecDestroy(gp->gexec[k]);
-  void* ptrs[] = {gp->X_in, gp->y_in, gp->theta, gp->Xf, gp->L, gp->Rv, gp->Rz, gp->Binv, gp->a, gp->f, gp->d1,
+  void* ptrs[] = {gp->Linv, gp->sw_prev, gp->reuse, gp->X_in, gp->y_in, gp->theta, gp->Xf, gp->L, gp->Rv, gp->Rz, gp->Binv, gp->a, gp->f, gp->d1,
                   gp->W, gp->sw, gp->b, gp->t, gp->x, gp->logp, gp->d3, gp->dsig, gp->svec, gp->rv, gp->zbar,
                   gp->tz, gp->y2, gp->Ky2, gp->u, gp->c, gp->rowdot, gp->scal, gp->grad, gp->status, gp->ready,
                   gp->counters, gp->tflags, gp->part, gp->tpart, gp->lpart, gp->tiles_lower, gp->jobs, gp->Rc,
@@ -570,6 +635,7 @@ int pgb_factor(pgb_gp* gp, void* stream) {
   if (!gp) return PGB_EINVAL;
   if (!gp->factor_valid) return PGB_ESTATE;
   cudaStream_t s = (cudaStream_t)stream;
+  CU_TRY(cudaMemsetAsync(gp->reuse + 2, 0, sizeof(int), s));   // always a full factorisation
   enq_dag(gp, JOB_NONE, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
@@ -620,6 +686,7 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
     enq_reset_status(gp, s);
     enq_prep(gp, s);
     launch_sqrt_w(gp->n, gp->n_pad, W, gp->sw, s);
+    CU_TRY(cudaMemsetAsync(gp->reuse, 0, sizeof(int) * 4, s));   // factor of the caller's W, not reusable
     enq_dag(gp, JOB_NONE, s);
     gp->factor_valid = 0;
   } else {
@@ -650,6 +717,20 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
   }
   CU_TRY(cudaGetLastError());
   return PGB_OK;
+}
+
+// Internal diagnostic entry (not part of the public C-ABI): device pointer of
+// one of a handle's intermediate buffers, for the test suite.
+void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
+  if (!gp || !name) return nullptr;
+  struct Item { const char* n; void* p; };
+  const Item items[] = {{"a", gp->a}, {"f", gp->f}, {"d1", gp->d1}, {"W", gp->W}, {"sw", gp->sw}, {"d3", gp->d3},
+                        {"dsig", gp->dsig}, {"svec", gp->svec}, {"zbar", gp->zbar}, {"u", gp->u}, {"c", gp->c},
+                        {"rowdot", gp->rowdot}, {"L", gp->L}, {"Linv", gp->Linv}, {"Rz", gp->Rz}, {"Binv", gp->Binv},
+                        {"logp", gp->logp}, {"grad", gp->grad}, {"scal", gp->scal}, {"reuse", gp->reuse}};
+  for (const Item& it : items)
+    if (std::strcmp(it.n, name) == 0) return it.p;
+  return nullptr;
 }
 
 }  // extern "C"

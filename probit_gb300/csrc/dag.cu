@@ -21,13 +21,22 @@
 //   RHS_IDENT : the identity             -> L^-T (upper)      (gradient)
 //   RHS_CROSS : rows K(x*_m, X) W^1/2    -> (L^-1 W^1/2 K_*)^T (predict)
 #include "kernels.cuh"
-#include "tile_gemm.cuh"
+#include "umma.cuh"
 
 namespace pgb {
 
 constexpr int DAG_THREADS = 256;
 constexpr int SC_LD = T + 1;
-constexpr size_t DAG_SMEM = sizeof(float) * (2 * KC * SROW + 2 * T * SC_LD);
+// tensor-core pipeline: NST stages of (A_hi, A_lo, B_hi, B_lo) 128 x 32 fp32
+// chunks (16 KB each), unioned with the epilogue tiles sC, sL.
+constexpr int NST = 3;
+constexpr int CHUNK_BYTES = T * 128;             // 128 rows x 32 fp32
+constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;     // A_hi, A_lo, B_hi, B_lo
+constexpr int UNION_BYTES = NST * STAGE_BYTES;   // >= 2 * T * SC_LD * 4
+constexpr size_t DAG_SMEM = UNION_BYTES + 1024 + 64;
+static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
+constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
+constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 
 // Initial value of tile (i, j) before the left-looking updates.
 template <int DM>
@@ -104,78 +113,139 @@ __device__ void fill_init(const DagJob& jb, const KernelParams& kp, int i, int j
   }
 }
 
-// In-place Cholesky of the lower triangle of the 128 x 128 tile in sC.
-// 32-wide panels: warp 0 factors the diagonal block, all threads solve the
-// rows below and update the trailing lower triangle.
+constexpr unsigned FULL = 0xffffffffu;
+
+// 32 x 32 Cholesky in one warp's registers: lane l owns row l (d[m] = A[l][m],
+// m <= l).  Column c: pivot from lane c by shuffle, scale, rank-1 update of
+// the later columns with the pivot column broadcast lane by lane.
+__device__ __forceinline__ void warp_potrf32(float (&d)[32], int lane, int col0, int* status) {
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    const float piv = __shfl_sync(FULL, d[c], c);
+    if (lane == 0 && !(piv > 0.0f)) {
+      atomicMin(status + ST_NOTPD_COL, col0 + c);
+      atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
+    }
+    const float lc = sqrtf(piv);
+    if (lane == c) d[c] = lc;
+    if (lane > c) d[c] = d[c] / lc;
+#pragma unroll
+    for (int m = c + 1; m < 32; ++m) {
+      const float lmc = __shfl_sync(FULL, d[c], m);
+      if (lane >= m) d[m] = fmaf(-d[c], lmc, d[m]);
+    }
+  }
+}
+
+// In-place Cholesky of the lower triangle of the 128 x 128 tile in sC:
+// 32-wide panels; warp 0 factors the diagonal block in registers, one thread
+// per row solves the panel below (row in registers, L row broadcast from
+// shared memory), 4 x 4 register blocks update the trailing lower triangle.
 __device__ void potrf_tile(float* sC, int col0, int* status) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = 0; jb < T; jb += 32) {
     if (warp == 0) {
-      for (int c = 0; c < 32; ++c) {
-        const int cc = jb + c;
-        const float piv = sC[cc * SC_LD + cc];
-        const float lc = sqrtf(piv);
-        if (lane == 0 && !(piv > 0.0f)) {
-          atomicMin(status + ST_NOTPD_COL, col0 + cc);
-          atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
-        }
-        __syncwarp();
-        if (lane > c) sC[(jb + lane) * SC_LD + cc] /= lc;
-        __syncwarp();
-        if (lane == c) sC[cc * SC_LD + cc] = lc;
-        if (lane > c) {
-          const float lv = sC[(jb + lane) * SC_LD + cc];
-          for (int m = c + 1; m <= lane; ++m) sC[(jb + lane) * SC_LD + jb + m] -= lv * sC[(jb + m) * SC_LD + cc];
-        }
-        __syncwarp();
-      }
+      float d[32];
+#pragma unroll
+      for (int m = 0; m < 32; ++m) d[m] = sC[(jb + lane) * SC_LD + jb + m];
+      warp_potrf32(d, lane, col0 + jb, status);
+#pragma unroll
+      for (int m = 0; m < 32; ++m)
+        if (m <= lane) sC[(jb + lane) * SC_LD + jb + m] = d[m];
     }
     __syncthreads();
     const int rem = T - jb - 32;
     if (rem > 0) {
       if (tid < rem) {
         const int r = jb + 32 + tid;
+        float x[32];
+#pragma unroll
+        for (int m = 0; m < 32; ++m) x[m] = sC[r * SC_LD + jb + m];
+#pragma unroll
         for (int c = 0; c < 32; ++c) {
-          float x = sC[r * SC_LD + jb + c];
-          for (int m = 0; m < c; ++m) x -= sC[r * SC_LD + jb + m] * sC[(jb + c) * SC_LD + jb + m];
-          sC[r * SC_LD + jb + c] = x / sC[(jb + c) * SC_LD + jb + c];
+          float acc = x[c];
+#pragma unroll
+          for (int m = 0; m < c; ++m) acc = fmaf(-x[m], sC[(jb + c) * SC_LD + jb + m], acc);
+          x[c] = acc / sC[(jb + c) * SC_LD + jb + c];
         }
+#pragma unroll
+        for (int m = 0; m < 32; ++m) sC[r * SC_LD + jb + m] = x[m];
       }
       __syncthreads();
-      for (int e = tid; e < rem * rem; e += DAG_THREADS) {
-        const int r = jb + 32 + e / rem, c = jb + 32 + e % rem;
-        if (c <= r) {
-          float s = sC[r * SC_LD + c];
+      const int nb = rem / 4;
+      for (int blk = tid; blk < nb * nb; blk += DAG_THREADS) {
+        const int br = blk / nb, bc = blk % nb;
+        if (bc > br) continue;
+        const int r0 = jb + 32 + br * 4, c0 = jb + 32 + bc * 4;
+        float acc[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
 #pragma unroll 8
-          for (int m = 0; m < 32; ++m) s -= sC[r * SC_LD + jb + m] * sC[c * SC_LD + jb + m];
-          sC[r * SC_LD + c] = s;
+        for (int m = 0; m < 32; ++m) {
+          float a[4], b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            a[q] = sC[(r0 + q) * SC_LD + jb + m];
+            b[q] = sC[(c0 + q) * SC_LD + jb + m];
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
         }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
       }
       __syncthreads();
     }
   }
 }
 
-// X L^T = C for the rows of sC (in place), L lower in sL.
-__device__ void trsm_rows(float* sC, const float* sL) {
-  const int tid = threadIdx.x;
-  for (int cb = 0; cb < T; cb += 32) {
-    if (tid < T) {
-      const int r = tid;
-      for (int c = cb; c < cb + 32; ++c) {
-        float x = sC[r * SC_LD + c];
-        for (int m = cb; m < c; ++m) x -= sC[r * SC_LD + m] * sL[c * SC_LD + m];
-        sC[r * SC_LD + c] = x / sL[c * SC_LD + c];
-      }
+// sL (lower) = inverse of the lower-triangular 128 x 128 L in sC.
+// Diagonal 32 x 32 blocks: warp b solves L_bb y = e_l for column l in lane
+// l's registers.  Off-diagonal blocks by distance:
+//   Linv_rc = -Linv_rr * sum_{c <= m < r} L_rm Linv_mc,
+// the partial sum P_rc kept in the (unused) upper block (c, r) of sL.
+__device__ void trinv_tile(const float* sC, float* sL) {
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (warp < 4) {
+    const int b0 = warp * 32;
+    float y[32];
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      float acc = (r == lane) ? 1.0f : 0.0f;
+#pragma unroll
+      for (int m = 0; m < r; ++m) acc = fmaf(-sC[(b0 + r) * SC_LD + b0 + m], y[m], acc);
+      y[r] = acc / sC[(b0 + r) * SC_LD + b0 + r];
+    }
+#pragma unroll
+    for (int r = 0; r < 32; ++r) sL[(b0 + r) * SC_LD + b0 + lane] = y[r];
+  }
+  __syncthreads();
+  for (int dl = 1; dl < 4; ++dl) {
+    const int nblk = 4 - dl;
+    // P_rc = sum_{m=c}^{r-1} L_rm Linv_mc  (block indices), stored at block (c, r)
+    for (int e = tid; e < nblk * 1024; e += DAG_THREADS) {
+      const int bi = e >> 10, rr = (e >> 5) & 31, cc = e & 31;
+      const int bc = bi, br = bi + dl;
+      float acc = 0.0f;
+      for (int m = bc * 32; m < br * 32; ++m)
+        acc = fmaf(sC[(br * 32 + rr) * SC_LD + m], sL[m * SC_LD + bc * 32 + cc], acc);
+      sL[(bc * 32 + cc) * SC_LD + br * 32 + rr] = acc;   // transposed into the upper block
     }
     __syncthreads();
-    const int rem = T - cb - 32;
-    for (int e = tid; e < T * rem; e += DAG_THREADS) {
-      const int r = e / rem, c = cb + 32 + e % rem;
-      float s = sC[r * SC_LD + c];
-#pragma unroll 8
-      for (int m = cb; m < cb + 32; ++m) s -= sC[r * SC_LD + m] * sL[c * SC_LD + m];
-      sC[r * SC_LD + c] = s;
+    // Linv_rc = -Linv_rr P_rc
+    for (int e = tid; e < nblk * 1024; e += DAG_THREADS) {
+      const int bi = e >> 10, rr = (e >> 5) & 31, cc = e & 31;
+      const int bc = bi, br = bi + dl;
+      float acc = 0.0f;
+      for (int m = 0; m <= rr; ++m)
+        acc = fmaf(sL[(br * 32 + rr) * SC_LD + br * 32 + m], sL[(bc * 32 + cc) * SC_LD + br * 32 + m], acc);
+      sL[(br * 32 + rr) * SC_LD + bc * 32 + cc] = -acc;
     }
     __syncthreads();
   }
@@ -194,11 +264,160 @@ __device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_
   return ok;
 }
 
+// Per-block tensor-core state, uniform across the block.
+struct TcCtx {
+  uint32_t tmem;       // accumulator: 128 lanes x 128 fp32 columns
+  uint32_t g;          // chunks issued so far by this block (stage = g % NST)
+  uint32_t ntask;      // accumulator commits waited so far
+  uint8_t* stages;     // 1024-aligned stage buffers (unioned with sC, sL)
+  uint64_t* mbar;      // [NST] stage-free barriers, [NST] accumulator barrier
+};
+
+// Load one 128 x 32 chunk of A (tile rows i) and B (tile rows j) into registers:
+// thread t holds units e = t + 256 q (q < 4) of each, e -> (row e >> 3, unit e & 7).
+__device__ __forceinline__ void load_chunk(const float* __restrict__ A, long long lda, const float* __restrict__ B,
+                                           long long ldb, int kc, float4 (&ra)[4], float4 (&rb)[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = threadIdx.x + DAG_THREADS * q;
+    const int row = e >> 3, u = e & 7;
+    ra[q] = __ldcg(reinterpret_cast<const float4*>(A + (size_t)row * lda + kc + 4 * u));
+    rb[q] = __ldcg(reinterpret_cast<const float4*>(B + (size_t)row * ldb + kc + 4 * u));
+  }
+}
+
+__device__ __forceinline__ void store_split(uint8_t* hi, uint8_t* lo, int row, int u, float4 v) {
+  float4 h, l;
+  split_tf32(v.x, h.x, l.x);
+  split_tf32(v.y, h.y, l.y);
+  split_tf32(v.z, h.z, l.z);
+  split_tf32(v.w, h.w, l.w);
+  const uint32_t off = sw128_offset(row, u);
+  *reinterpret_cast<float4*>(hi + off) = h;
+  *reinterpret_cast<float4*>(lo + off) = l;
+}
+
+__device__ __forceinline__ void store_chunk(uint8_t* stage, const float4 (&ra)[4], const float4 (&rb)[4]) {
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = threadIdx.x + DAG_THREADS * q;
+    const int row = e >> 3, u = e & 7;
+    store_split(stage, stage + CHUNK_BYTES, row, u, ra[q]);
+    store_split(stage + 2 * CHUNK_BYTES, stage + 3 * CHUNK_BYTES, row, u, rb[q]);
+  }
+}
+
+// Thread 0: the 12 MMAs of one 32-wide k-chunk (4 k-steps x 3 products).
+__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, bool first) {
+  const uint32_t a_hi = smem_u32(stage), a_lo = a_hi + CHUNK_BYTES;
+  const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+#pragma unroll
+  for (int ks = 0; ks < 4; ++ks) {
+    const uint32_t o = ks * 32;
+    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
+    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, 1u);
+    umma_tf32(tc.tmem, sdesc_sw128(a_lo + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+  }
+}
+
+// Wait (bounded) until every MMA this block issued has completed.
+__device__ bool tc_drain(TcCtx& tc, int* status) {
+  __syncthreads();
+  if (threadIdx.x == 0) umma_commit(tc.mbar + NST);
+  const bool ok = mbar_wait_bounded(tc.mbar + NST, tc.ntask & 1u, MMA_WAIT_NS);
+  tc.ntask++;
+  if (!ok && threadIdx.x == 0) {
+    atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
+    atomicExch(status + ST_ABORT, 1);
+  }
+  tc_fence_after();
+  __syncthreads();
+  return ok;
+}
+
+// acc (TMEM) = sum_{k0 <= k < k1} A_k B_k^T in 3xTF32, where A_k / B_k are
+// the 128 x 128 tiles at Abase + k*T / Bbase + k*T (row strides lda / ldb).  Thread 0
+// calls wait_tile(k) before tile k is loaded; a false return (a wait gave up)
+// drains the MMAs in flight and returns false.
+template <class WaitTile>
+__device__ bool tc_accumulate(const float* Abase, long long lda, const float* Bbase, long long ldb, int k0, int k1,
+                              TcCtx& tc, int* s_ok, int* status, WaitTile wait_tile) {
+  const int nchunks = (k1 - k0) * (T / 32);
+  float4 ra[4], rb[4];
+  if (threadIdx.x == 0) {
+    s_ok[0] = wait_tile(k0);
+    __threadfence();
+  }
+  __syncthreads();
+  if (!s_ok[0]) return false;
+  load_chunk(Abase + (size_t)k0 * T, lda, Bbase + (size_t)k0 * T, ldb, 0, ra, rb);
+  for (int c = 0; c < nchunks; ++c) {
+    const uint32_t g = tc.g;
+    uint8_t* stage = tc.stages + (g % NST) * STAGE_BYTES;
+    if (g >= NST) {
+      if (!mbar_wait_bounded(tc.mbar + (g % NST), ((g / NST) - 1u) & 1u, MMA_WAIT_NS)) {
+        if (threadIdx.x == 0) {
+          atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
+          atomicExch(status + ST_ABORT, 1);
+        }
+        tc_drain(tc, status);
+        return false;
+      }
+    }
+    store_chunk(stage, ra, rb);
+    fence_proxy_async_smem();
+    const int cn = c + 1;
+    const int slot = cn & 1;
+    if (threadIdx.x == 0) {
+      bool ok = true;
+      if (cn < nchunks && (cn % (T / 32)) == 0) {
+        ok = wait_tile(k0 + cn / (T / 32));
+        __threadfence();
+      }
+      s_ok[slot] = ok;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      tc_fence_after();
+      issue_chunk(tc, stage, c == 0);
+      umma_commit(tc.mbar + (g % NST));
+    }
+    tc.g = g + 1;
+    if (!s_ok[slot]) {
+      tc_drain(tc, status);
+      return false;
+    }
+    if (cn < nchunks) {
+      const int kt = k0 + cn / (T / 32);
+      const int kc = (cn % (T / 32)) * 32;
+      load_chunk(Abase + (size_t)kt * T, lda, Bbase + (size_t)kt * T, ldb, kc, ra, rb);
+    }
+  }
+  return tc_drain(tc, status);
+}
+
+// Subtract (sign = -1) or store (sign = +1) the TMEM accumulator into the
+// 128 x 128 shared tile sC (row stride SC_LD); all 8 warps take part.
+__device__ __forceinline__ void tmem_to_tile(const TcCtx& tc, float* sC, float sign) {
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int row = (w & 3) * 32 + lane;
+  const int col0 = (w >> 2) * 64;
+#pragma unroll
+  for (int h = 0; h < 2; ++h) {
+    float v[32];
+    tmem_ld_32x32(tc.tmem + ((uint32_t)((w & 3) * 32) << 16) + (uint32_t)(col0 + 32 * h), v);
+#pragma unroll
+    for (int q = 0; q < 32; ++q) {
+      float* p = sC + row * SC_LD + col0 + 32 * h + q;
+      *p = sign < 0.0f ? *p - v[q] : v[q];
+    }
+  }
+  tc_fence_before();
+}
+
 template <int DM>
-__device__ void dag_task(const DagJob& jb, int i, int j, float* smem, int* s_ok) {
-  float* sA = smem;
-  float* sB = sA + KC * SROW;
-  float* sC = sB + KC * SROW;
+__device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
+  float* sC = reinterpret_cast<float*>(tc.stages);
   float* sL = sC + T * SC_LD;
   const int nt = jb.nt;
   const long long ld = jb.ld;
@@ -207,40 +426,53 @@ __device__ void dag_task(const DagJob& jb, int i, int j, float* smem, int* s_ok)
   float* rowbase = is_rhs ? jb.R + (size_t)ri * T * ld : jb.L + (size_t)i * T * ld;
   const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
   const KernelParams kp = make_kp(jb.sh, jb.theta);
-
-  float acc[8][8];
-  acc_zero(acc);
-  for (int k = k0; k < j; ++k) {
-    if (!block_wait(jb.ready + (size_t)i * nt + k, jb.status, s_ok)) return;
-    if (!block_wait(jb.ready + (size_t)j * nt + k, jb.status, s_ok)) return;
-    acc_gemm_tile(acc, rowbase + (size_t)k * T, ld, jb.L + (size_t)j * T * ld + (size_t)k * T, ld, sA, sB);
+  if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
+    // the resident L tile is already the factor: publish it and move on
+    __syncthreads();
+    if (threadIdx.x == 0) st_release(jb.ready + (size_t)i * nt + j, 1);
+    return;
   }
+
+  const bool have_acc = j > k0;
+  if (have_acc) {
+    const int* ready = jb.ready;
+    int* status = jb.status;
+    auto wait_tile = [=](int k) {
+      return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
+             wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
+    };
+    if (!tc_accumulate(rowbase, ld, jb.L + (size_t)j * T * ld, ld, k0, j, tc, s_ok, jb.status, wait_tile)) return;
+  }
+  // the stage buffers are free (all MMAs completed): build C in sC
   fill_init<DM>(jb, kp, i, j, sC);
   __syncthreads();
-  {
-    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-    for (int a = 0; a < 8; ++a)
-#pragma unroll
-      for (int b = 0; b < 8; ++b) sC[acc_row(ty, a) * SC_LD + acc_row(tx, b)] -= acc[a][b];
-  }
+  if (have_acc) tmem_to_tile(tc, sC, -1.0f);
   __syncthreads();
   float* dst = rowbase + (size_t)j * T;
+  float* Linv_j = jb.Linv + (size_t)j * T * T;
   if (!is_rhs && i == j) {
+    // L_jj = chol(C) and its inverse, both published with the tile flag
     potrf_tile(sC, j * T, jb.status);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
     }
-  } else {
-    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok)) return;
-    const float* Ljj = jb.L + (size_t)j * T * ld + (size_t)j * T;
+    trinv_tile(sC, sL);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      sL[r * SC_LD + c] = c <= r ? __ldcg(Ljj + (size_t)r * ld + c) : 0.0f;
+      Linv_j[(size_t)r * T + c] = c <= r ? sL[r * SC_LD + c] : 0.0f;
     }
+  } else {
+    // X = C L_jj^-T = C Linv_jj^T on the tensor cores (C staged through dst)
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+    }
+    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2)) return;
+    auto always = [](int) { return true; };
+    if (!tc_accumulate(dst, ld, Linv_j, T, 0, 1, tc, s_ok, jb.status, always)) return;
+    tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
-    trsm_rows(sC, sL);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
@@ -269,9 +501,32 @@ template <int DM>
 __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob* __restrict__ jobs,
                                                                     const int4* __restrict__ tasks, int ntasks,
                                                                     int* __restrict__ counter) {
-  extern __shared__ __align__(16) float smem[];
+  extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
-  __shared__ int s_ok;
+  __shared__ int s_ok[4];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
+  TcCtx tc;
+  {
+    const uint32_t base = smem_u32(dsmem);
+    const uint32_t aligned = (base + 1023u) & ~1023u;
+    tc.stages = dsmem + (aligned - base);
+  }
+  tc.mbar = s_mbar;
+  tc.g = 0;
+  tc.ntask = 0;
+  if (threadIdx.x < 32) {
+    tmem_alloc(&s_tmem, 128);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  tc.tmem = s_tmem;
   while (true) {
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -285,11 +540,63 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     if (t >= ntasks) break;
     const int4 tk = tasks[t];
     const DagJob jb = jobs[tk.x];
-    dag_task<DM>(jb, tk.y, tk.z, smem, &s_ok);
+    if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
+    dag_task<DM>(jb, tk.y, tk.z, tc, s_ok);
   }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
 }
 
+// Check kernel: C (128 x 128) = A B^T with A, B 128 x K row-major (K a
+// multiple of 128), through the same 3xTF32 pipeline as the factorisation.
+__global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const float* __restrict__ A,
+                                                                       const float* __restrict__ B, int K,
+                                                                       float* __restrict__ C, int* __restrict__ status) {
+  extern __shared__ uint8_t dsmem[];
+  __shared__ int s_ok[4];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
+  TcCtx tc;
+  {
+    const uint32_t base = smem_u32(dsmem);
+    const uint32_t aligned = (base + 1023u) & ~1023u;
+    tc.stages = dsmem + (aligned - base);
+  }
+  tc.mbar = s_mbar;
+  tc.g = 0;
+  tc.ntask = 0;
+  if (threadIdx.x < 32) {
+    tmem_alloc(&s_tmem, 128);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  tc.tmem = s_tmem;
+  float* sC = reinterpret_cast<float*>(tc.stages);
+  auto always = [](int) { return true; };
+  if (tc_accumulate(A, K, B, K, 0, K / T, tc, s_ok, status, always)) {
+    tmem_to_tile(tc, sC, 1.0f);
+    __syncthreads();
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) C[e] = sC[(e >> 7) * SC_LD + (e & (T - 1))];
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+}
+
+__global__ void syrk_zzt_kernel(const float* __restrict__ Z, long long ldz, int nt, const int2* __restrict__ tiles,
+                                int ntiles, float* __restrict__ Binv, long long ldb, int* __restrict__ counter,
+                                int* __restrict__ status);
+
 void dag_set_attributes() {
+  cudaFuncSetAttribute(tc_tile_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
+  cudaFuncSetAttribute(syrk_zzt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
@@ -307,36 +614,81 @@ void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, in
 
 // ---------------------------------------------------------------- B^-1 = Z Z^T
 // Z = L^-T (upper, stored in the RHS rows of an RHS_IDENT factorisation).
-// Tile (I, J), I >= J: sum over k >= I of Z_Ik Z_Jk^T; written to (I, J) and
-// transposed to (J, I) so B^-1 is stored full.
-__global__ void __launch_bounds__(256, 1) syrk_zzt_kernel(const float* __restrict__ Z, long long ldz, int nt,
-                                                          const int2* __restrict__ tiles, float* __restrict__ Binv,
-                                                          long long ldb) {
-  extern __shared__ __align__(16) float smem[];
-  float* sA = smem;
-  float* sB = sA + KC * SROW;
-  const int2 tl = tiles[blockIdx.x];
-  const int I = tl.x, J = tl.y;
-  float acc[8][8];
-  acc_zero(acc);
-  for (int k = I; k < nt; ++k)
-    acc_gemm_tile(acc, Z + (size_t)I * T * ldz + (size_t)k * T, ldz, Z + (size_t)J * T * ldz + (size_t)k * T, ldz, sA,
-                  sB);
-  const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-#pragma unroll
-  for (int a = 0; a < 8; ++a)
-#pragma unroll
-    for (int b = 0; b < 8; ++b) {
-      const int r = acc_row(ty, a), c = acc_row(tx, b);
-      Binv[(size_t)(I * T + r) * ldb + J * T + c] = acc[a][b];
-      if (I != J) Binv[(size_t)(J * T + c) * ldb + I * T + r] = acc[a][b];
+// Tile (I, J), I >= J: sum over k >= I of Z_Ik Z_Jk^T on the tensor cores;
+// written to (I, J) and, transposed through shared memory, to (J, I), so
+// B^-1 is stored full.  Persistent blocks take tiles in list order (longest
+// k-range first) through an atomic counter.
+__global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const float* __restrict__ Z, long long ldz, int nt,
+                                                                  const int2* __restrict__ tiles, int ntiles,
+                                                                  float* __restrict__ Binv, long long ldb,
+                                                                  int* __restrict__ counter, int* __restrict__ status) {
+  extern __shared__ uint8_t dsmem[];
+  __shared__ int s_task;
+  __shared__ int s_ok[4];
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
+  TcCtx tc;
+  {
+    const uint32_t base = smem_u32(dsmem);
+    const uint32_t aligned = (base + 1023u) & ~1023u;
+    tc.stages = dsmem + (aligned - base);
+  }
+  tc.mbar = s_mbar;
+  tc.g = 0;
+  tc.ntask = 0;
+  if (threadIdx.x < 32) {
+    tmem_alloc(&s_tmem, 128);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  tc.tmem = s_tmem;
+  float* sC = reinterpret_cast<float*>(tc.stages);
+  while (true) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = atomicAdd(counter, 1);
+      if (t < ntiles && ld_relaxed(status + ST_ABORT)) t = ntiles;
+      s_task = t;
     }
+    __syncthreads();
+    const int t = s_task;
+    if (t >= ntiles) break;
+    const int2 tl = tiles[t];
+    const int I = tl.x, J = tl.y;
+    auto always = [](int) { return true; };
+    if (!tc_accumulate(Z + (size_t)I * T * ldz, ldz, Z + (size_t)J * T * ldz, ldz, I, nt, tc, s_ok, status, always))
+      break;
+    tmem_to_tile(tc, sC, 1.0f);
+    __syncthreads();
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      Binv[(size_t)(I * T + r) * ldb + J * T + c] = sC[r * SC_LD + c];
+      if (I != J) Binv[(size_t)(J * T + r) * ldb + I * T + c] = sC[c * SC_LD + r];
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
 }
 
 void launch_syrk_zzt(const float* Z, long long ldz, int nt, const int2* tiles, int ntiles, float* Binv, long long ldb,
-                     cudaStream_t st) {
-  const size_t smem = sizeof(float) * 2 * KC * SROW;
-  syrk_zzt_kernel<<<ntiles, 256, smem, st>>>(Z, ldz, nt, tiles, Binv, ldb);
+                     int* counter, int* status, int grid, cudaStream_t st) {
+  syrk_zzt_kernel<<<grid, DAG_THREADS, DAG_SMEM, st>>>(Z, ldz, nt, tiles, ntiles, Binv, ldb, counter, status);
 }
 
 }  // namespace pgb
+
+// Internal check entry (not part of the public C-ABI): one 128 x 128 tile
+// product through the tensor-core pipeline.
+extern "C" int pgbx_tc_tile_check(const float* A, const float* B, int K, float* C, int* status, void* stream) {
+  if (!A || !B || !C || !status || K <= 0 || K % pgb::T) return PGB_EINVAL;
+  pgb::dag_set_attributes();
+  pgb::tc_tile_check_kernel<<<1, pgb::DAG_THREADS, pgb::DAG_SMEM, (cudaStream_t)stream>>>(A, B, K, C, status);
+  return cudaGetLastError() == cudaSuccess ? PGB_OK : PGB_ECUDA;
+}

@@ -14,6 +14,7 @@ struct DagJob {
   int nt;            // tiles per dimension (ceil(n / T))
   long long ld;      // floats per row of L and R
   float* L;          // nt*T rows: lower tiles of the factor
+  float* Linv;       // nt tiles of T x T: inverses of the diagonal tiles of L
   int rhs_kind;      // RhsKind
   int nrt;           // RHS tile rows
   int nrhs;          // RHS rows in use
@@ -27,6 +28,12 @@ struct DagJob {
   Shape sh;
   int* ready;            // (nt + nrt) x nt tile flags, zeroed before the launch
   int* status;
+  // factor reuse: when *reuse is 1 the resident L is already the factor of
+  // this B (bitwise equal W, same theta).  reuse_mode 1: skip the L tiles and
+  // solve only the RHS rows; 2: skip the whole launch (the caller solves the
+  // RHS with the triangular solve instead).
+  const int* reuse;
+  int reuse_mode;
 };
 
 // gram.cu
@@ -47,9 +54,8 @@ void launch_grad_trace(const Shape& sh, const float* theta, const float* Xf, con
 void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const void* y, int n, float* logp,
                      float* d1, float* d2, float* d3, cudaStream_t st);
 void launch_newton_lik(const Shape& sh, const float* theta, const float* f, const void* y, const float* a,
-                       int n_pad, float* d1, float* W, float* sw, float* r, cudaStream_t st);
-void launch_newton_update(int n, const float* r, const float* sw, const float* x, float* a, double* part,
-                          cudaStream_t st);
+                       int n_pad, float* d1, float* W, float* sw, float* r, float* rhs, cudaStream_t st);
+void launch_newton_update(int n, const float* sw, const float* x, float* a, double* part, cudaStream_t st);
 void launch_newton_finalize(const double* part, int nparts, float tol, int maxiter, int* status, float* err_out,
                             cudaGraphConditionalHandle cond, int use_cond, cudaStream_t st);
 void launch_lik_full(const Shape& sh, const float* theta, const float* f, const void* y, int n_pad, float* logp,
@@ -59,7 +65,7 @@ void launch_evidence(int n, const float* logp, const float* f, const float* a, c
 void launch_grad_vec1(int n, int n_pad, const float* rowdot, const float* sw, const float* d3, const float* a,
                       const float* d1, float* dsig, float* svec, float* r, cudaStream_t st);
 void launch_scale_vec(int n, int n_pad, const float* sw, const float* in, float* out, cudaStream_t st);
-void launch_grad_vec3(int n, int n_pad, const float* zbar, const float* Ky2, const float* a, const float* d1,
+void launch_grad_vec3(int n, int n_pad, const float* y1, const float* sw, const float* a, const float* d1,
                       const float* svec, const float* W, float* u, float* c, cudaStream_t st);
 void launch_grad_lik_final(const Shape& sh, const float* theta, const float* f, const void* y, const float* dsig,
                            const float* u, const double* tpart, int ntp, double* lpart, float* grad,
@@ -67,17 +73,21 @@ void launch_grad_lik_final(const Shape& sh, const float* theta, const float* f, 
 void launch_predict_var(const Shape& sh, const float* theta, const float* rowsq, int nt, int m, float* var,
                         cudaStream_t st);
 void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st);
+// factor reuse: flags[0] = factor valid, flags[1] = W differs, flags[2] = reuse
+void launch_reuse_check(int n, const float* sw, float* sw_prev, int* flags, cudaStream_t st);
+void launch_reuse_mark_valid(int* flags, const int* status, cudaStream_t st);
 
 // dag.cu
 void dag_set_attributes();
 void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int Dp, int grid,
                        cudaStream_t st);
 void launch_syrk_zzt(const float* Z, long long ldz, int nt, const int2* tiles, int ntiles, float* Binv, long long ldb,
-                     cudaStream_t st);
+                     int* counter, int* status, int grid, cudaStream_t st);
 
 // trsv.cu
 void trsv_set_attributes();
-void launch_trsv(int n, int nt, long long ld, const float* L, const float* b, float* x, int trans, int* flags,
-                 int* counter, int* status, int grid, cudaStream_t st);
+// run_if: when non-null the launch does nothing unless *run_if == run_when
+void launch_trsv(int n, int nt, long long ld, const float* L, const float* Linv, const float* b, float* x, int trans,
+                 int* flags, int* counter, int* status, int grid, const int* run_if, int run_when, cudaStream_t st);
 
 }  // namespace pgb

@@ -2,8 +2,9 @@
 //   lower: L x = b        trans: L^T x = b
 // Wavefront over 128-row blocks: blocks are claimed in solve order through an
 // atomic counter, each block accumulates the contributions of already-solved
-// blocks as their flags are released, then solves its diagonal tile.  A block
-// only waits on blocks claimed before it, so the launch cannot deadlock.
+// blocks as their flags are released, then applies the inverse of its
+// diagonal tile (kept by the factorisation).  A block only waits on blocks
+// claimed before it, so the launch cannot deadlock.
 // Replaces the triangular part of the reference's LU solve
 // (implicit/solvers.py:24) in the B form L L^T = B.
 #include "kernels.cuh"
@@ -11,13 +12,14 @@
 namespace pgb {
 
 constexpr int TS_THREADS = 256;
-constexpr int TL_LD = T + 1;
 
 __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long long ld, const float* __restrict__ L,
+                                                             const float* __restrict__ Linv,
                                                              const float* __restrict__ b, float* __restrict__ x,
                                                              int trans, int* __restrict__ flags,
-                                                             int* __restrict__ counter, int* __restrict__ status) {
-  extern __shared__ __align__(16) float sL[];   // T x TL_LD
+                                                             int* __restrict__ counter, int* __restrict__ status,
+                                                             const int* __restrict__ run_if, int run_when) {
+  if (run_if && *run_if != run_when) return;
   __shared__ float sacc[T];
   __shared__ float sx[T];
   __shared__ float spart[2][T];
@@ -75,31 +77,25 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
       __syncthreads();
     }
     if (!ok) continue;
-    // diagonal tile
-    const float* Lii = L + (size_t)i * T * ld + (size_t)i * T;
-    for (int e = tid; e < T * T; e += TS_THREADS) {
-      const int r = e >> 7, c = e & (T - 1);
-      sL[r * TL_LD + c] = c <= r ? __ldcg(Lii + (size_t)r * ld + c) : 0.0f;
-    }
+    // diagonal tile: x_i = Linv_ii acc (lower) or Linv_ii^T acc (trans)
+    const float* Li = Linv + (size_t)i * T * T;
+    if (tid < T) sx[tid] = sacc[tid];
     __syncthreads();
-    if (warp == 0) {
-      if (!trans) {
-        for (int c = 0; c < T; ++c) {
-          const float xc = sacc[c] / sL[c * TL_LD + c];
-          __syncwarp();
-          for (int m = c + 1 + lane; m < T; m += 32) sacc[m] -= sL[m * TL_LD + c] * xc;
-          if (lane == 0) sacc[c] = xc;
-          __syncwarp();
-        }
-      } else {
-        for (int c = T - 1; c >= 0; --c) {
-          const float xc = sacc[c] / sL[c * TL_LD + c];
-          __syncwarp();
-          for (int m = lane; m < c; m += 32) sacc[m] -= sL[c * TL_LD + m] * xc;
-          if (lane == 0) sacc[c] = xc;
-          __syncwarp();
-        }
+    if (!trans) {
+      for (int rr = 0; rr < 16; ++rr) {
+        const int r = warp * 16 + rr;
+        const float4 lv = __ldcg(reinterpret_cast<const float4*>(Li + (size_t)r * T + lane * 4));
+        float s = lv.x * sx[lane * 4] + lv.y * sx[lane * 4 + 1] + lv.z * sx[lane * 4 + 2] + lv.w * sx[lane * 4 + 3];
+        s = warp_sum(s);
+        if (lane == 0) sacc[r] = s;
       }
+    } else {
+      const int c = tid & (T - 1), half = tid >> 7;
+      float s = 0.0f;
+      for (int r = half * 64; r < half * 64 + 64; ++r) s = fmaf(__ldcg(Li + (size_t)r * T + c), sx[r], s);
+      spart[half][c] = s;
+      __syncthreads();
+      if (tid < T) sacc[tid] = spart[0][tid] + spart[1][tid];
     }
     __syncthreads();
     if (tid < T) x[(size_t)i * T + tid] = sacc[tid];
@@ -111,14 +107,11 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
   }
 }
 
-void trsv_set_attributes() {
-  cudaFuncSetAttribute(trsv_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(sizeof(float) * T * TL_LD));
-}
+void trsv_set_attributes() {}
 
-void launch_trsv(int n, int nt, long long ld, const float* L, const float* b, float* x, int trans, int* flags,
-                 int* counter, int* status, int grid, cudaStream_t st) {
-  const size_t smem = sizeof(float) * T * TL_LD;
-  trsv_kernel<<<grid, TS_THREADS, smem, st>>>(n, nt, ld, L, b, x, trans, flags, counter, status);
+void launch_trsv(int n, int nt, long long ld, const float* L, const float* Linv, const float* b, float* x, int trans,
+                 int* flags, int* counter, int* status, int grid, const int* run_if, int run_when, cudaStream_t st) {
+  trsv_kernel<<<grid, TS_THREADS, 0, st>>>(n, nt, ld, L, Linv, b, x, trans, flags, counter, status, run_if, run_when);
 }
 
 }  // namespace pgb

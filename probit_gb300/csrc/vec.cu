@@ -41,20 +41,24 @@ void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const 
 // ---------------------------------------------------------------- Newton step
 // The reference's update is a correction, z <- z - J^-1 (F(z) - z) with
 // J = diag(d2) K - I (implicit/solvers.py:18-25).  With W = -d2 and
-// B = I + W^1/2 K W^1/2, -J^-1 = (I + W K)^-1 = I - W^1/2 B^-1 W^1/2 K, so
-//   r = d1 - a,   delta = r - W^1/2 B^-1 W^1/2 K r,   a <- a + delta.
-// Keeping the correction form (rather than recomputing a from b = W f + d1)
-// keeps the float32 rounding floor of ||a_k - a_{k-1}|| as low as the
-// reference's.  From f = K a this kernel writes d1, W, sqrt W and r.
-// Padding entries (i >= n, up to n_pad) are zeroed.
+// B = I + W^1/2 K W^1/2, -J^-1 = (I + W K)^-1 = W^1/2 B^-1 W^-1/2, so
+//   r = d1 - a,   delta = W^1/2 B^-1 (W^-1/2 r),   a <- a + delta.
+// This form has no subtraction of nearly equal vectors (the GPML form
+// r - W^1/2 B^-1 W^1/2 K r cancels where K W is large), so its float32 error
+// is that of the reference's LU solve.  W^1/2 is floored at 1e-18 so a W
+// that underflows to 0 keeps every quantity finite.
+// From f = K a this kernel writes d1, W, W^1/2, r and the right-hand side
+// y = r / W^1/2.  Padding entries (i >= n, up to n_pad) are zeroed.
+constexpr float kSwFloor = 1e-18f;
+
 __global__ void newton_lik_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ f,
                                   const void* __restrict__ y, const float* __restrict__ a, int n_pad,
                                   float* __restrict__ d1, float* __restrict__ W, float* __restrict__ sw,
-                                  float* __restrict__ r) {
+                                  float* __restrict__ r, float* __restrict__ rhs) {
   const int i = blockIdx.x * VT + threadIdx.x;
   if (i >= n_pad) return;
   if (i >= sh.n) {
-    d1[i] = 0.0f; W[i] = 0.0f; sw[i] = 0.0f; r[i] = 0.0f;
+    d1[i] = 0.0f; W[i] = 0.0f; sw[i] = 0.0f; r[i] = 0.0f; rhs[i] = 0.0f;
     return;
   }
   int yi;
@@ -62,27 +66,30 @@ __global__ void newton_lik_kernel(Shape sh, const float* __restrict__ theta, con
   LikOut o;
   lik_point<false>(sh.lik, f[i], yv, yi, theta_sigma(sh, theta), theta_cutpoints(sh, theta), o);
   const float w = -o.d2;
+  const float s = fmaxf(sqrtf(w), kSwFloor);
+  const float ri = o.d1 - a[i];
   d1[i] = o.d1;
   W[i] = w;
-  sw[i] = sqrtf(w);
-  r[i] = o.d1 - a[i];
+  sw[i] = s;
+  r[i] = ri;
+  rhs[i] = ri / s;
 }
 
 void launch_newton_lik(const Shape& sh, const float* theta, const float* f, const void* y, const float* a,
-                       int n_pad, float* d1, float* W, float* sw, float* r, cudaStream_t st) {
-  newton_lik_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, theta, f, y, a, n_pad, d1, W, sw, r);
+                       int n_pad, float* d1, float* W, float* sw, float* r, float* rhs, cudaStream_t st) {
+  newton_lik_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, theta, f, y, a, n_pad, d1, W, sw, r, rhs);
 }
 
-// a_new = a + (r - sw * x); block partial of ||a_new - a||^2 (as jaxopt
-// measures it, on the rounded new iterate); a <- a_new
-__global__ void newton_update_kernel(int n, const float* __restrict__ r, const float* __restrict__ sw,
-                                     const float* __restrict__ x, float* __restrict__ a, double* __restrict__ part) {
+// a_new = a + sw * x; block partial of ||a_new - a||^2 (as jaxopt measures
+// it, on the rounded new iterate); a <- a_new
+__global__ void newton_update_kernel(int n, const float* __restrict__ sw, const float* __restrict__ x,
+                                     float* __restrict__ a, double* __restrict__ part) {
   __shared__ double sred[VT / 32];
   const int i = blockIdx.x * VT + threadIdx.x;
   float e = 0.0f;
   if (i < n) {
     const float ai = a[i];
-    const float an = ai + (r[i] - sw[i] * x[i]);
+    const float an = ai + sw[i] * x[i];
     const float dlt = an - ai;
     e = dlt * dlt;
     a[i] = an;
@@ -109,13 +116,13 @@ __global__ void newton_finalize_kernel(const double* __restrict__ part, int npar
     if (conv) status[ST_CONVERGED] = 1;
     if (err != err) atomicCAS(status + ST_CODE, 0, PGB_ENAN);
     const bool again = (err > tol) && (it < maxiter) && (status[ST_ABORT] == 0);
+    status[ST_SPARE0] = again ? 1 : 0;   // read by the host-driven (eager) loop
     if (use_cond) cudaGraphSetConditional(cond, again ? 1u : 0u);
   }
 }
 
-void launch_newton_update(int n, const float* r, const float* sw, const float* x, float* a, double* part,
-                          cudaStream_t st) {
-  newton_update_kernel<<<ceil_div(n, VT), VT, 0, st>>>(n, r, sw, x, a, part);
+void launch_newton_update(int n, const float* sw, const float* x, float* a, double* part, cudaStream_t st) {
+  newton_update_kernel<<<ceil_div(n, VT), VT, 0, st>>>(n, sw, x, a, part);
 }
 
 void launch_newton_finalize(const double* part, int nparts, float tol, int maxiter, int* status, float* err_out,
@@ -143,7 +150,7 @@ __global__ void lik_full_kernel(Shape sh, const float* __restrict__ theta, const
   d1[i] = o.d1;
   d3[i] = o.d3;
   W[i] = -o.d2;
-  sw[i] = sqrtf(-o.d2);
+  sw[i] = fmaxf(sqrtf(-o.d2), kSwFloor);
 }
 
 void launch_lik_full(const Shape& sh, const float* theta, const float* f, const void* y, int n_pad, float* logp,
@@ -218,8 +225,9 @@ void launch_scale_vec(int n, int n_pad, const float* sw, const float* in, float*
   scale_vec_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, sw, in, out);
 }
 
-// u = zbar - K y2 ; c = a/2 - d1 - s - W u
-__global__ void grad_vec3_kernel(int n, int n_pad, const float* __restrict__ zbar, const float* __restrict__ Ky2,
+// u = (I + K W)^-1 zbar = W^-1/2 B^-1 (W^1/2 zbar) = y1 / sw (no cancellation);
+// c = a/2 - d1 - s - W u
+__global__ void grad_vec3_kernel(int n, int n_pad, const float* __restrict__ y1, const float* __restrict__ sw,
                                  const float* __restrict__ a, const float* __restrict__ d1,
                                  const float* __restrict__ svec, const float* __restrict__ W, float* __restrict__ u,
                                  float* __restrict__ c) {
@@ -229,14 +237,14 @@ __global__ void grad_vec3_kernel(int n, int n_pad, const float* __restrict__ zba
     u[i] = 0.0f; c[i] = 0.0f;
     return;
   }
-  const float ui = zbar[i] - Ky2[i];
+  const float ui = y1[i] / sw[i];
   u[i] = ui;
   c[i] = 0.5f * a[i] - d1[i] - svec[i] - W[i] * ui;
 }
 
-void launch_grad_vec3(int n, int n_pad, const float* zbar, const float* Ky2, const float* a, const float* d1,
+void launch_grad_vec3(int n, int n_pad, const float* y1, const float* sw, const float* a, const float* d1,
                       const float* svec, const float* W, float* u, float* c, cudaStream_t st) {
-  grad_vec3_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, zbar, Ky2, a, d1, svec, W, u, c);
+  grad_vec3_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, y1, sw, a, d1, svec, W, u, c);
 }
 
 // Likelihood-parameter gradient, per block: slot 0 = sigma_n, slots
@@ -345,6 +353,40 @@ __global__ void sqrt_w_kernel(int n, int n_pad, const float* __restrict__ W, flo
 
 void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st) {
   sqrt_w_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, W, sw);
+}
+
+// ---------------------------------------------------------------- factor reuse
+// flags[1] |= any(sw != sw_prev) (bitwise; NaN always differs); sw_prev <- sw.
+__global__ void reuse_check_kernel(int n, const float* __restrict__ sw, float* __restrict__ sw_prev,
+                                   int* __restrict__ flags) {
+  const int i = blockIdx.x * VT + threadIdx.x;
+  bool diff = false;
+  if (i < n) {
+    const float a = sw[i];
+    diff = __float_as_uint(a) != __float_as_uint(sw_prev[i]) || a != a;
+    sw_prev[i] = a;
+  }
+  if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(flags + 1, 1);
+}
+
+// flags[2] = valid && !differs; differs <- 0
+__global__ void reuse_decide_kernel(int* flags) {
+  flags[2] = (flags[0] != 0 && flags[1] == 0) ? 1 : 0;
+  flags[1] = 0;
+}
+
+void launch_reuse_check(int n, const float* sw, float* sw_prev, int* flags, cudaStream_t st) {
+  reuse_check_kernel<<<ceil_div(n, VT), VT, 0, st>>>(n, sw, sw_prev, flags);
+  reuse_decide_kernel<<<1, 1, 0, st>>>(flags);
+}
+
+// After a factorisation that computed L: the resident L matches sw_prev.
+__global__ void reuse_mark_valid_kernel(int* flags, const int* status) {
+  flags[0] = status[ST_CODE] == 0 ? 1 : 0;
+}
+
+void launch_reuse_mark_valid(int* flags, const int* status, cudaStream_t st) {
+  reuse_mark_valid_kernel<<<1, 1, 0, st>>>(flags, status);
 }
 
 }  // namespace pgb

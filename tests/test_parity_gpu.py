@@ -172,3 +172,18 @@ def test_not_positive_definite_gives_nan_and_status(cuda_device):
     # the handle stays usable afterwards
     v2 = gp.objective()(p.params())
     assert abs(v2 - float(g["value_f64"])) <= 1e-4 * abs(float(g["value_f64"]))
+
+
+@pytest.mark.gpu
+def test_eager_mode_matches_graph_mode(cuda_device, monkeypatch):
+    """PGB_EAGER=1 launches the same kernels without graphs: identical results."""
+    name = "ordinal_matern12_n200"
+    g = np.load(GOLD / f"{name}.npz")
+    p, theta, tol = make(name)
+    out = []
+    for eager in ("0", "1"):
+        monkeypatch.setenv("PGB_EAGER", eager)
+        gp = pg.LaplaceGP((g["X"], g["y"]), p.prior(), pg.log_probit_likelihood, tolerance=tol)
+        v, gr = gp.value_and_grad()(p.params())
+        out.append((v, flat(gr), gp.last_status()[1]))
+    assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
