@@ -103,6 +103,7 @@ struct pgb_gp {
   cudaStream_t cap_s = nullptr, cap_s2 = nullptr;
   int grad_ready = 0;      // Rz / Binv allocated
   int eager = 0;           // PGB_EAGER=1: launch kernels directly, host-driven Newton loop
+  unsigned long long* trace = nullptr;   // PGB_TRACE=1: per-task timestamps of the DAG
   int factor_valid = 0;    // L is the factor of B at the resident W (same theta)
 };
 
@@ -149,7 +150,7 @@ Shape make_shape(const pgb_desc* d) {
   s.nl = d->n_lengthscales;
   s.lik = d->likelihood;
   s.J = d->likelihood == PGB_LIK_GAUSSIAN ? 0 : d->j;
-  s.pi_over_p = d->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(M_PI / (double)d->period) : 0.0f;
+  s.inv_p = d->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(1.0 / (double)d->period) : 0.0f;
   return s;
 }
 
@@ -293,11 +294,20 @@ int run_eager(pgb_gp* gp, int op, cudaStream_t s) {
     if (r != PGB_OK) return r;
   }
   enq_prologue(gp, s);
+  const char* tr = std::getenv("PGB_TRACE");
+  const bool trace = tr && tr[0] == '1';
   for (int it = 0; it < gp->desc.maxiter; ++it) {
     enq_newton_step(gp, s, 0, 0);
     int again = 0;
+    float err = 0.0f;
+    int reuse[4] = {0, 0, 0, 0};
     CU_TRY(cudaMemcpyAsync(&again, gp->status + ST_SPARE0, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (trace) {
+      CU_TRY(cudaMemcpyAsync(&err, gp->scal, sizeof(float), cudaMemcpyDeviceToHost, s));
+      CU_TRY(cudaMemcpyAsync(reuse, gp->reuse, sizeof(reuse), cudaMemcpyDeviceToHost, s));
+    }
     CU_TRY(cudaStreamSynchronize(s));
+    if (trace) std::fprintf(stderr, "probit_gb300: newton %d ||delta||=%.6g reuse=%d\n", it + 1, err, reuse[2]);
     if (!again) break;
   }
   enq_epilogue(gp, op, s);
@@ -508,6 +518,18 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
   {
     const char* e = std::getenv("PGB_EAGER");
     gp->eager = (e && e[0] == '1') ? 1 : 0;
+    const char* t = std::getenv("PGB_TRACE");
+    if (t && t[0] == '1') {
+      size_t mx = 0;
+      for (int k = 0; k < JOB_COUNT; ++k) mx = std::max(mx, (size_t)gp->ntasks[k]);
+      if (dev_alloc(&gp->trace, mx * 8 + (size_t)gp->nt * 16) == PGB_OK) {
+        for (int k = 0; k < JOB_COUNT; ++k) {
+          gp->hjobs[k].trace = gp->trace;
+          gp->hjobs[k].ptrace = gp->trace + mx * 8;
+        }
+        CU_TRY(cudaMemcpy(gp->jobs, gp->hjobs, sizeof(gp->hjobs), cudaMemcpyHostToDevice));
+      }
+    }
   }
   CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s, cudaStreamNonBlocking));
   CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s2, cudaStreamNonBlocking));
@@ -519,7 +541,7 @@ int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
   for (int k = 0; k < OP_COUNT; ++k)
     if (gp->gexec[k]) cudaGraphExecDestroy(gp->gexec[k]);
-  void* ptrs[] = {gp->Linv, gp->sw_prev, gp->reuse, gp->X_in, gp->y_in, gp->theta, gp->Xf, gp->L, gp->Rv, gp->Rz, gp->Binv, gp->a, gp->f, gp->d1,
+  void* ptrs[] = {gp->trace, gp->Linv, gp->sw_prev, gp->reuse, gp->X_in, gp->y_in, gp->theta, gp->Xf, gp->L, gp->Rv, gp->Rz, gp->Binv, gp->a, gp->f, gp->d1,
                   gp->W, gp->sw, gp->b, gp->t, gp->x, gp->logp, gp->d3, gp->dsig, gp->svec, gp->rv, gp->zbar,
                   gp->tz, gp->y2, gp->Ky2, gp->u, gp->c, gp->rowdot, gp->scal, gp->grad, gp->status, gp->ready,
                   gp->counters, gp->tflags, gp->part, gp->tpart, gp->lpart, gp->tiles_lower, gp->jobs, gp->Rc,
@@ -727,7 +749,9 @@ void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
   const Item items[] = {{"a", gp->a}, {"f", gp->f}, {"d1", gp->d1}, {"W", gp->W}, {"sw", gp->sw}, {"d3", gp->d3},
                         {"dsig", gp->dsig}, {"svec", gp->svec}, {"zbar", gp->zbar}, {"u", gp->u}, {"c", gp->c},
                         {"rowdot", gp->rowdot}, {"L", gp->L}, {"Linv", gp->Linv}, {"Rz", gp->Rz}, {"Binv", gp->Binv},
-                        {"logp", gp->logp}, {"grad", gp->grad}, {"scal", gp->scal}, {"reuse", gp->reuse}};
+                        {"logp", gp->logp}, {"grad", gp->grad}, {"scal", gp->scal}, {"reuse", gp->reuse},
+                        {"trace", gp->trace}, {"tasks_none", gp->tasks[JOB_NONE]},
+                        {"ptrace", gp->hjobs[JOB_NONE].ptrace}};
   for (const Item& it : items)
     if (std::strcmp(it.n, name) == 0) return it.p;
   return nullptr;

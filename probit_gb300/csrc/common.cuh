@@ -70,7 +70,7 @@ __device__ __forceinline__ bool wait_flag_geq(const int* flag, int target, int* 
       return false;
     }
     __nanosleep(ns);
-    if (ns < 1024) ns <<= 1;
+    if (ns < 256) ns <<= 1;
   }
 }
 
@@ -83,22 +83,21 @@ __device__ __forceinline__ void raise_status(int* status, int code) {
 // with ``stretch``: the inputs are divided by the lengthscale before the
 // distance (features are prepared by prep_features).  For the periodic
 // kernel the stored features are the raw inputs and the distance is
-// q_d = (2 sin(pi (x_d - z_d) / p) / l_d)^2.
+// q_d = (2 sin(pi (x_d - z_d) / p) / l_d)^2, with sin(pi u) evaluated by sinpif.
 struct KernelParams {
   int kind;        // PGB_KERNEL_*
   int D;           // input dims
   int Dp;          // feature row stride (floats)
   int nl;          // number of lengthscales (1 or D)
   float s;         // signal variance
-  float pi_over_p; // pi / period (periodic only)
+  float inv_p;     // 1 / period (periodic only)
   float inv_l[MAX_D];   // 1/l_d (periodic: used after the sine)
   float l[MAX_D];
 };
 
 __device__ __forceinline__ float sq_dist_dim(const KernelParams& kp, float xi, float xj, int d) {
   if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-    const float t = (xi - xj) * kp.pi_over_p;
-    const float v = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
+    const float v = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
     return v * v;
   }
   const float v = xi - xj;
@@ -163,7 +162,7 @@ struct Shape {
   int nl;         // lengthscales (1 or D)
   int lik;        // PGB_LIK_*
   int J;          // ordinal classes
-  float pi_over_p;  // pi / period
+  float inv_p;      // 1 / period
 };
 
 // Build the kernel parameters from the device hyperparameter block.
@@ -173,7 +172,7 @@ __device__ __forceinline__ KernelParams make_kp(const Shape& sh, const float* __
   kp.D = sh.D;
   kp.Dp = sh.Dp;
   kp.nl = sh.nl;
-  kp.pi_over_p = sh.pi_over_p;
+  kp.inv_p = sh.inv_p;
 #pragma unroll 1
   for (int d = 0; d < sh.nl; ++d) {
     kp.l[d] = __ldg(theta + d);

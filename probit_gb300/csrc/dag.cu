@@ -33,117 +33,180 @@ constexpr int NST = 3;
 constexpr int CHUNK_BYTES = T * 128;             // 128 rows x 32 fp32
 constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;     // A_hi, A_lo, B_hi, B_lo
 constexpr int UNION_BYTES = NST * STAGE_BYTES;   // >= 2 * T * SC_LD * 4
-constexpr size_t DAG_SMEM = UNION_BYTES + 1024 + 64;
+constexpr size_t DAG_SMEM = UNION_BYTES + (2 * T * 17 + 2 * T) * 4 + 1024 + 64;
 static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
 constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
 constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 
-// Initial value of tile (i, j) before the left-looking updates.
+// Initial value C_init of tile (i, j) before the left-looking updates.  The
+// row and column features (and W^1/2) of the tile are staged in shared
+// memory first; each thread then evaluates the entries it owns in the TMEM
+// accumulator layout (row = TMEM lane, 64 columns) and stores -C_init there,
+// so the MMAs accumulate sum_k L_ik L_jk^T - C_init and the tile costs no
+// work after its last dependency arrives.
+constexpr int SX_STRIDE = 17;   // DM + 1 (<= 16 + 1), breaks bank conflicts
+constexpr int SX_FLOATS = 2 * T * SX_STRIDE + 2 * T;
+
 template <int DM>
-__device__ void fill_init(const DagJob& jb, const KernelParams& kp, int i, int j, float* sC) {
+__device__ void stage_features(const DagJob& jb, const KernelParams& kp, int i, int j, float* sX) {
   const int n = jb.n;
   const bool is_rhs = i >= jb.nt;
   const int ri = i - jb.nt;
-  for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
-    const int r = e >> 7, c = e & (T - 1);
-    const int gj = j * T + c;
-    float v = 0.0f;
-    if (!is_rhs) {
-      const int gi = i * T + r;
-      if (i == j && c > r) {
-        v = 0.0f;
-      } else if (gi < n && gj < n) {
-        float xi[DM], xj[DM];
-#pragma unroll
-        for (int d = 0; d < DM; ++d) {
-          xi[d] = d < kp.Dp ? __ldg(jb.Xf + (size_t)gi * kp.Dp + d) : 0.0f;
-          xj[d] = d < kp.Dp ? __ldg(jb.Xf + (size_t)gj * kp.Dp + d) : 0.0f;
-        }
-        float d2 = 0.0f;
-#pragma unroll
-        for (int d = 0; d < DM; ++d) {
-          if (d < kp.D) {
-            float q;
-            if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-              const float t = (xi[d] - xj[d]) * kp.pi_over_p;
-              q = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
-            } else {
-              q = xi[d] - xj[d];
-            }
-            d2 += q * q;
-          }
-        }
-        v = __ldcg(jb.sw + gi) * kernel_from_d2(kp, d2) * __ldcg(jb.sw + gj);
-        if (gi == gj) v += 1.0f;
-      } else {
-        v = (gi == gj) ? 1.0f : 0.0f;
-      }
-    } else if (jb.rhs_kind == RHS_VEC) {
-      const int gi = ri * T + r;
-      v = (gi == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
-    } else if (jb.rhs_kind == RHS_IDENT) {
-      v = (ri == j && r == c) ? 1.0f : 0.0f;
-    } else {  // RHS_CROSS
-      const int gi = ri * T + r;
-      if (gi < jb.nrhs && gj < n) {
-        float xi[DM], xj[DM];
-#pragma unroll
-        for (int d = 0; d < DM; ++d) {
-          xi[d] = d < kp.Dp ? __ldg(jb.Xq + (size_t)gi * kp.Dp + d) : 0.0f;
-          xj[d] = d < kp.Dp ? __ldg(jb.Xf + (size_t)gj * kp.Dp + d) : 0.0f;
-        }
-        float d2 = 0.0f;
-#pragma unroll
-        for (int d = 0; d < DM; ++d) {
-          if (d < kp.D) {
-            float q;
-            if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-              const float t = (xi[d] - xj[d]) * kp.pi_over_p;
-              q = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
-            } else {
-              q = xi[d] - xj[d];
-            }
-            d2 += q * q;
-          }
-        }
-        v = kernel_from_d2(kp, d2) * __ldcg(jb.sw + gj);
+  float* sXr = sX;
+  float* sXc = sX + T * SX_STRIDE;
+  float* sWr = sXc + T * SX_STRIDE;
+  float* sWc = sWr + T;
+  for (int e = threadIdx.x; e < T * DM; e += DAG_THREADS) {
+    const int r = e / DM, d = e % DM;
+    const int gj = j * T + r;
+    sXc[r * SX_STRIDE + d] = (gj < n && d < kp.Dp) ? __ldg(jb.Xf + (size_t)gj * kp.Dp + d) : 0.0f;
+    float xr = 0.0f;
+    if (d < kp.Dp) {
+      if (!is_rhs) {
+        const int gi = i * T + r;
+        if (gi < n) xr = __ldg(jb.Xf + (size_t)gi * kp.Dp + d);
+      } else if (jb.rhs_kind == RHS_CROSS) {
+        const int gi = ri * T + r;
+        if (gi < jb.nrhs) xr = __ldg(jb.Xq + (size_t)gi * kp.Dp + d);
       }
     }
-    sC[r * SC_LD + c] = v;
+    sXr[r * SX_STRIDE + d] = xr;
   }
+  for (int r = threadIdx.x; r < T; r += DAG_THREADS) {
+    const int gj = j * T + r, gi = i * T + r;
+    sWc[r] = gj < n ? __ldcg(jb.sw + gj) : 0.0f;
+    sWr[r] = (!is_rhs && gi < n) ? __ldcg(jb.sw + gi) : 0.0f;
+  }
+}
+
+template <int DM>
+__device__ __forceinline__ float cinit_entry(const DagJob& jb, const KernelParams& kp, int i, int j, int r, int c,
+                                             const float* sX) {
+  const float* sXr = sX;
+  const float* sXc = sX + T * SX_STRIDE;
+  const float* sWr = sXc + T * SX_STRIDE;
+  const float* sWc = sWr + T;
+  const int n = jb.n;
+  const bool is_rhs = i >= jb.nt;
+  const int ri = i - jb.nt;
+  const int gj = j * T + c;
+  if (!is_rhs) {
+    const int gi = i * T + r;
+    if (i == j && c > r) return 0.0f;
+    if (gi < n && gj < n) {
+      float d2 = 0.0f;
+#pragma unroll
+      for (int d = 0; d < DM; ++d) {
+        if (d < kp.D) {
+          float q;
+          const float xi = sXr[r * SX_STRIDE + d], xj = sXc[c * SX_STRIDE + d];
+          if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
+            q = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
+          else
+            q = xi - xj;
+          d2 += q * q;
+        }
+      }
+      float v = sWr[r] * kernel_from_d2(kp, d2) * sWc[c];
+      if (gi == gj) v += 1.0f;
+      return v;
+    }
+    return (gi == gj) ? 1.0f : 0.0f;
+  }
+  if (jb.rhs_kind == RHS_VEC) {
+    const int gi = ri * T + r;
+    return (gi == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
+  }
+  if (jb.rhs_kind == RHS_IDENT) return (ri == j && r == c) ? 1.0f : 0.0f;
+  const int gi = ri * T + r;   // RHS_CROSS
+  if (gi < jb.nrhs && gj < n) {
+    float d2 = 0.0f;
+#pragma unroll
+    for (int d = 0; d < DM; ++d) {
+      if (d < kp.D) {
+        float q;
+        const float xi = sXr[r * SX_STRIDE + d], xj = sXc[c * SX_STRIDE + d];
+        if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
+          q = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
+        else
+          q = xi - xj;
+        d2 += q * q;
+      }
+    }
+    return kernel_from_d2(kp, d2) * sWc[c];
+  }
+  return 0.0f;
 }
 
 constexpr unsigned FULL = 0xffffffffu;
 
 // 32 x 32 Cholesky in one warp's registers: lane l owns row l (d[m] = A[l][m],
-// m <= l).  Column c: pivot from lane c by shuffle, scale, rank-1 update of
-// the later columns with the pivot column broadcast lane by lane.
-__device__ __forceinline__ void warp_potrf32(float (&d)[32], int lane, int col0, int* status) {
-#pragma unroll
-  for (int c = 0; c < 32; ++c) {
-    const float piv = __shfl_sync(FULL, d[c], c);
-    if (lane == 0 && !(piv > 0.0f)) {
-      atomicMin(status + ST_NOTPD_COL, col0 + c);
-      atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
-    }
+// m <= l).  Column C: pivot from lane C by shuffle, scale, rank-1 update of
+// the later columns with the pivot column broadcast lane by lane.  The column
+// loop is unrolled by template recursion so every index is a compile-time
+// constant and the row stays in registers.
+template <int C>
+__device__ __forceinline__ void potrf32_col(float (&d)[32], int lane, int& bad) {
+  if constexpr (C < 32) {
+    const float piv = __shfl_sync(FULL, d[C], C);
+    if (!(piv > 0.0f) && bad < 0) bad = C;
     const float lc = sqrtf(piv);
-    if (lane == c) d[c] = lc;
-    if (lane > c) d[c] = d[c] / lc;
+    const float dc = (lane == C) ? lc : ((lane > C) ? d[C] / lc : d[C]);
+    d[C] = dc;
 #pragma unroll
-    for (int m = c + 1; m < 32; ++m) {
-      const float lmc = __shfl_sync(FULL, d[c], m);
-      if (lane >= m) d[m] = fmaf(-d[c], lmc, d[m]);
+    for (int m = C + 1; m < 32; ++m) {
+      const float lmc = __shfl_sync(FULL, dc, m);
+      if (lane >= m) d[m] = fmaf(-dc, lmc, d[m]);
     }
+    potrf32_col<C + 1>(d, lane, bad);
+  }
+}
+
+__device__ __forceinline__ void warp_potrf32(float (&d)[32], int lane, int col0, int* status) {
+  int bad = -1;
+  potrf32_col<0>(d, lane, bad);
+  if (lane == 0 && bad >= 0) {
+    atomicMin(status + ST_NOTPD_COL, col0 + bad);
+    atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
+  }
+}
+
+// Row substitution x[c] = (x[c] - sum_{m<c} x[m] L[c][m]) / L[c][c] for a
+// 32-wide block, L rows read from shared memory (row stride SC_LD), unrolled
+// by template recursion.
+template <int C>
+__device__ __forceinline__ void subst32_col(float (&x)[32], const float* Lb, const float* rdiag) {
+  if constexpr (C < 32) {
+    float acc = x[C];
+#pragma unroll
+    for (int m = 0; m < C; ++m) acc = fmaf(-x[m], Lb[C * SC_LD + m], acc);
+    x[C] = acc * rdiag[C];
+    subst32_col<C + 1>(x, Lb, rdiag);
+  }
+}
+
+// Column `lane` of the inverse of a 32 x 32 lower-triangular block:
+// y[r] = (delta_{r,lane} - sum_{m<r} L[r][m] y[m]) / L[r][r].
+template <int R>
+__device__ __forceinline__ void inv32_row(float (&y)[32], const float* Lb, int lane) {
+  if constexpr (R < 32) {
+    float acc = (R == lane) ? 1.0f : 0.0f;
+#pragma unroll
+    for (int m = 0; m < R; ++m) acc = fmaf(-Lb[R * SC_LD + m], y[m], acc);
+    y[R] = acc * __frcp_rn(Lb[R * SC_LD + R]);
+    inv32_row<R + 1>(y, Lb, lane);
   }
 }
 
 // In-place Cholesky of the lower triangle of the 128 x 128 tile in sC:
 // 32-wide panels; warp 0 factors the diagonal block in registers, one thread
-// per row solves the panel below (row in registers, L row broadcast from
-// shared memory), 4 x 4 register blocks update the trailing lower triangle.
-__device__ void potrf_tile(float* sC, int col0, int* status) {
+// per row solves the panel below (row in registers, L rows broadcast from
+// shared memory, reciprocal pivots in srd), 4 x 4 register blocks update the
+// trailing lower triangle.
+__device__ void potrf_tile(float* sC, float* srd, int col0, int* status, unsigned long long* pt = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = 0; jb < T; jb += 32) {
+    if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
     if (warp == 0) {
       float d[32];
 #pragma unroll
@@ -152,8 +215,10 @@ __device__ void potrf_tile(float* sC, int col0, int* status) {
 #pragma unroll
       for (int m = 0; m < 32; ++m)
         if (m <= lane) sC[(jb + lane) * SC_LD + jb + m] = d[m];
+      srd[lane] = __frcp_rn(d[lane]);
     }
     __syncthreads();
+    if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
     const int rem = T - jb - 32;
     if (rem > 0) {
       if (tid < rem) {
@@ -161,17 +226,12 @@ __device__ void potrf_tile(float* sC, int col0, int* status) {
         float x[32];
 #pragma unroll
         for (int m = 0; m < 32; ++m) x[m] = sC[r * SC_LD + jb + m];
-#pragma unroll
-        for (int c = 0; c < 32; ++c) {
-          float acc = x[c];
-#pragma unroll
-          for (int m = 0; m < c; ++m) acc = fmaf(-x[m], sC[(jb + c) * SC_LD + jb + m], acc);
-          x[c] = acc / sC[(jb + c) * SC_LD + jb + c];
-        }
+        subst32_col<0>(x, sC + jb * SC_LD + jb, srd);
 #pragma unroll
         for (int m = 0; m < 32; ++m) sC[r * SC_LD + jb + m] = x[m];
       }
       __syncthreads();
+      if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
       const int nb = rem / 4;
       for (int blk = tid; blk < nb * nb; blk += DAG_THREADS) {
         const int br = blk / nb, bc = blk % nb;
@@ -215,13 +275,7 @@ __device__ void trinv_tile(const float* sC, float* sL) {
   if (warp < 4) {
     const int b0 = warp * 32;
     float y[32];
-#pragma unroll
-    for (int r = 0; r < 32; ++r) {
-      float acc = (r == lane) ? 1.0f : 0.0f;
-#pragma unroll
-      for (int m = 0; m < r; ++m) acc = fmaf(-sC[(b0 + r) * SC_LD + b0 + m], y[m], acc);
-      y[r] = acc / sC[(b0 + r) * SC_LD + b0 + r];
-    }
+    inv32_row<0>(y, sC + b0 * SC_LD + b0, lane);
 #pragma unroll
     for (int r = 0; r < 32; ++r) sL[(b0 + r) * SC_LD + b0 + lane] = y[r];
   }
@@ -251,10 +305,62 @@ __device__ void trinv_tile(const float* sC, float* sL) {
   }
 }
 
+// X L^T = C in place for the 128 rows of sC (L lower in sL), by 32-column
+// blocks: one thread per row solves a block with the row in registers, then
+// 4 x 4 register blocks update the remaining columns.  Used on the critical
+// path (the sub-diagonal tile), where waiting for L^-1 would cost more.
+__device__ void trsm_subst(float* sC, const float* sL, float* srd) {
+  const int tid = threadIdx.x;
+  if (tid < T) srd[tid] = __frcp_rn(sL[tid * SC_LD + tid]);
+  __syncthreads();
+  for (int cb = 0; cb < T; cb += 32) {
+    if (tid < T) {
+      const int r = tid;
+      float x[32];
+#pragma unroll
+      for (int m = 0; m < 32; ++m) x[m] = sC[r * SC_LD + cb + m];
+      subst32_col<0>(x, sL + cb * SC_LD + cb, srd + cb);
+#pragma unroll
+      for (int m = 0; m < 32; ++m) sC[r * SC_LD + cb + m] = x[m];
+    }
+    __syncthreads();
+    const int rem = T - cb - 32;
+    if (rem > 0) {
+      const int nbc = rem / 4;   // 4-column groups
+      for (int blk = tid; blk < (T / 4) * nbc; blk += DAG_THREADS) {
+        const int r0 = (blk / nbc) * 4, c0 = cb + 32 + (blk % nbc) * 4;
+        float acc[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
+#pragma unroll 8
+        for (int m = 0; m < 32; ++m) {
+          float a[4], b[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            a[q] = sC[(r0 + q) * SC_LD + cb + m];
+            b[q] = sL[(c0 + q) * SC_LD + cb + m];
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
+      }
+      __syncthreads();
+    }
+  }
+}
+
 // Thread 0 waits, everyone learns the outcome.
-__device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_ok) {
+__device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_ok, int target = 1) {
   if (threadIdx.x == 0) {
-    const bool ok = wait_flag_geq(flag, 1, status);
+    const bool ok = wait_flag_geq(flag, target, status);
     __threadfence();
     *s_ok = ok ? 1 : 0;
   }
@@ -341,7 +447,7 @@ __device__ bool tc_drain(TcCtx& tc, int* status) {
 // drains the MMAs in flight and returns false.
 template <class WaitTile>
 __device__ bool tc_accumulate(const float* Abase, long long lda, const float* Bbase, long long ldb, int k0, int k1,
-                              TcCtx& tc, int* s_ok, int* status, WaitTile wait_tile) {
+                              TcCtx& tc, int* s_ok, int* status, WaitTile wait_tile, bool preloaded = false) {
   const int nchunks = (k1 - k0) * (T / 32);
   float4 ra[4], rb[4];
   if (threadIdx.x == 0) {
@@ -379,7 +485,7 @@ __device__ bool tc_accumulate(const float* Abase, long long lda, const float* Bb
     __syncthreads();
     if (threadIdx.x == 0) {
       tc_fence_after();
-      issue_chunk(tc, stage, c == 0);
+      issue_chunk(tc, stage, c == 0 && !preloaded);
       umma_commit(tc.mbar + (g % NST));
     }
     tc.g = g + 1;
@@ -396,7 +502,7 @@ __device__ bool tc_accumulate(const float* Abase, long long lda, const float* Bb
   return tc_drain(tc, status);
 }
 
-// Subtract (sign = -1) or store (sign = +1) the TMEM accumulator into the
+// Store the TMEM accumulator, multiplied by `sign` (+1 or -1), into the
 // 128 x 128 shared tile sC (row stride SC_LD); all 8 warps take part.
 __device__ __forceinline__ void tmem_to_tile(const TcCtx& tc, float* sC, float sign) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -408,15 +514,16 @@ __device__ __forceinline__ void tmem_to_tile(const TcCtx& tc, float* sC, float s
     tmem_ld_32x32(tc.tmem + ((uint32_t)((w & 3) * 32) << 16) + (uint32_t)(col0 + 32 * h), v);
 #pragma unroll
     for (int q = 0; q < 32; ++q) {
-      float* p = sC + row * SC_LD + col0 + 32 * h + q;
-      *p = sign < 0.0f ? *p - v[q] : v[q];
+      sC[row * SC_LD + col0 + 32 * h + q] = sign * v[q];
     }
   }
   tc_fence_before();
 }
 
 template <int DM>
-__device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
+__device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, int tidx) {
+  unsigned long long* tr = (jb.trace && threadIdx.x == 0) ? jb.trace + (size_t)tidx * 8 : nullptr;
+  if (tr) tr[0] = global_ns();
   float* sC = reinterpret_cast<float*>(tc.stages);
   float* sL = sC + T * SC_LD;
   const int nt = jb.nt;
@@ -427,12 +534,32 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
   const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
   const KernelParams kp = make_kp(jb.sh, jb.theta);
   if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
-    // the resident L tile is already the factor: publish it and move on
+    // the resident L tile (and, on the diagonal, its inverse) is already the
+    // factor: publish it and move on
     __syncthreads();
-    if (threadIdx.x == 0) st_release(jb.ready + (size_t)i * nt + j, 1);
+    if (threadIdx.x == 0) st_release(jb.ready + (size_t)i * nt + j, i == j ? 2 : 1);
     return;
   }
 
+  // -C_init into the accumulator (before any dependency wait)
+  float* sX = reinterpret_cast<float*>(tc.stages + UNION_BYTES);
+  stage_features<DM>(jb, kp, i, j, sX);
+  __syncthreads();
+  {
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int r = (w & 3) * 32 + lane;
+    const int cb = (w >> 2) * 64;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      float v[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) v[q] = -cinit_entry<DM>(jb, kp, i, j, r, cb + 32 * h + q, sX);
+      tmem_st_32x32(tc.tmem + ((uint32_t)((w & 3) * 32) << 16) + (uint32_t)(cb + 32 * h), v);
+    }
+    tmem_wait_st();
+    tc_fence_before();
+  }
+  __syncthreads();
   const bool have_acc = j > k0;
   if (have_acc) {
     const int* ready = jb.ready;
@@ -441,26 +568,52 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
       return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
              wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
     };
-    if (!tc_accumulate(rowbase, ld, jb.L + (size_t)j * T * ld, ld, k0, j, tc, s_ok, jb.status, wait_tile)) return;
+    if (!tc_accumulate(rowbase, ld, jb.L + (size_t)j * T * ld, ld, k0, j, tc, s_ok, jb.status, wait_tile, true))
+      return;
+  } else {
+    tc_fence_after();
   }
-  // the stage buffers are free (all MMAs completed): build C in sC
-  fill_init<DM>(jb, kp, i, j, sC);
-  __syncthreads();
-  if (have_acc) tmem_to_tile(tc, sC, -1.0f);
+  if (tr) tr[1] = global_ns();
+  // C = C_init - sum = -(accumulator)
+  tmem_to_tile(tc, sC, -1.0f);
+  if (tr) tr[6] = global_ns();
   __syncthreads();
   float* dst = rowbase + (size_t)j * T;
   float* Linv_j = jb.Linv + (size_t)j * T * T;
+  if (tr) tr[4] = global_ns();
   if (!is_rhs && i == j) {
-    // L_jj = chol(C) and its inverse, both published with the tile flag
-    potrf_tile(sC, j * T, jb.status);
+    // L_jj = chol(C), published (flag 1) before its inverse (flag 2), so the
+    // sub-diagonal tile can start while the inverse is computed
+    potrf_tile(sC, sX, j * T, jb.status, jb.ptrace ? jb.ptrace + (size_t)j * 16 : nullptr);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
+    }
+    __syncthreads();
+    if (jb.ptrace && threadIdx.x == 0) jb.ptrace[(size_t)j * 16 + 12] = global_ns();
+    if (threadIdx.x == 0) {
+      if (tr) tr[5] = global_ns();
+      __threadfence();
+      st_release(jb.ready + (size_t)i * nt + j, 1);
     }
     trinv_tile(sC, sL);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       Linv_j[(size_t)r * T + c] = c <= r ? sL[r * SC_LD + c] : 0.0f;
+    }
+  } else if (!is_rhs && i == j + 1) {
+    // critical path: substitution with L_jj as soon as it is published
+    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 1)) return;
+    const float* Ljj = jb.L + (size_t)j * T * ld + (size_t)j * T;
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      sL[r * SC_LD + c] = c <= r ? __ldcg(Ljj + (size_t)r * ld + c) : 0.0f;
+    }
+    __syncthreads();
+    trsm_subst(sC, sL, sX);
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
     }
   } else {
     // X = C L_jj^-T = C Linv_jj^T on the tensor cores (C staged through dst)
@@ -468,7 +621,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
     }
-    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2)) return;
+    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 2)) return;
     auto always = [](int) { return true; };
     if (!tc_accumulate(dst, ld, Linv_j, T, 0, 1, tc, s_ok, jb.status, always)) return;
     tmem_to_tile(tc, sC, 1.0f);
@@ -492,8 +645,11 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok) {
   }
   __syncthreads();
   if (threadIdx.x == 0) {
+    if (tr) tr[2] = global_ns();
     __threadfence();
-    st_release(jb.ready + (size_t)i * nt + j, 1);
+    // diagonal tiles: 2 = L_jj and its inverse published; others: 1 = tile ready
+    st_release(jb.ready + (size_t)i * nt + j, (!is_rhs && i == j) ? 2 : 1);
+    if (tr) tr[3] = global_ns();
   }
 }
 
@@ -541,7 +697,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     const int4 tk = tasks[t];
     const DagJob jb = jobs[tk.x];
     if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
-    dag_task<DM>(jb, tk.y, tk.z, tc, s_ok);
+    dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
   }
   tc_fence_before();
   __syncthreads();

@@ -38,8 +38,7 @@ __device__ __forceinline__ float d2_t(const KernelParams& kp, const float* xi, c
   for (int d = 0; d < DM; ++d) {
     if (d < kp.D) {
       if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-        const float t = (xi[d] - xj[d]) * kp.pi_over_p;
-        const float v = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
+        const float v = (2.0f * sinpif((xi[d] - xj[d]) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
         d2 += v * v;
       } else {
         const float v = xi[d] - xj[d];
@@ -83,22 +82,52 @@ void launch_gram_full(const Shape& sh, const float* theta, const float* X1f, int
 // ---------------------------------------------------------------- Gram matvec
 // y[r] = row_scale[r] * sum_c K(xr_r, xc_c) * (M ? M[r, c] : 1) * v[c]
 // One block owns MV_ROWS rows and sweeps all columns; the per-row sums are
-// reduced in a fixed order, so results are bitwise reproducible.
-constexpr int MV_ROWS = 32;
+// reduced in a fixed order, so results are bitwise reproducible.  The kernel
+// family is a template parameter and every per-entry quantity lives in
+// registers or shared memory.
 constexpr int MV_THREADS = 256;
+// rows per block: 32 for D <= 4, 16 for D <= 8, 8 for D <= 16 (constant
+// unrolled work per column)
+template <int DM>
+constexpr int mv_rows() { return 128 / DM; }
 
-template <int DM, bool HAS_M>
+template <int KIND, int DM>
+__device__ __forceinline__ float kval(const float* xi, const float* xj, int D, float s, float inv_p,
+                                      const float* sl) {
+  float d2 = 0.0f;
+#pragma unroll
+  for (int d = 0; d < DM; ++d) {
+    if (d < D) {
+      float q;
+      if (KIND == PGB_KERNEL_EQ_PERIODIC) {
+        q = (2.0f * sinpif((xi[d] - xj[d]) * inv_p)) / sl[d];
+      } else {
+        q = xi[d] - xj[d];
+      }
+      d2 += q * q;
+    }
+  }
+  if (KIND == PGB_KERNEL_MATERN12) return s * expf(-sqrtf(d2));
+  return s * expf(-0.5f * d2);
+}
+
+template <int KIND, int DM, bool HAS_M>
 __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(
     Shape sh, const float* __restrict__ theta, const float* __restrict__ Xr, int nr, const float* __restrict__ Xc,
     int nc, const float* __restrict__ M, long long ldm, const float* __restrict__ v,
     const float* __restrict__ row_scale, float* __restrict__ y) {
-  const KernelParams kp = make_kp(sh, theta);
+  constexpr int MV_ROWS = mv_rows<DM>();
   __shared__ float sx[MV_ROWS][DM];
   __shared__ float sred[MV_THREADS / 32][MV_ROWS];
+  __shared__ float sl[MAX_D];
+  const int D = sh.D, Dp = sh.Dp;
+  const float sv = __ldg(theta + sh.nl);
+  const float inv_p = sh.inv_p;
+  if (threadIdx.x < MAX_D) sl[threadIdx.x] = threadIdx.x < D ? __ldg(theta + (sh.nl == 1 ? 0 : threadIdx.x)) : 1.0f;
   const int r0 = blockIdx.x * MV_ROWS;
   for (int e = threadIdx.x; e < MV_ROWS * DM; e += MV_THREADS) {
     const int r = e / DM, d = e % DM;
-    sx[r][d] = (r0 + r < nr && d < sh.Dp) ? Xr[(size_t)(r0 + r) * sh.Dp + d] : 0.0f;
+    sx[r][d] = (r0 + r < nr && d < Dp) ? Xr[(size_t)(r0 + r) * Dp + d] : 0.0f;
   }
   __syncthreads();
   float acc[MV_ROWS];
@@ -108,50 +137,74 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(
   for (int c = threadIdx.x; c < nc; c += MV_THREADS) {
     float xc[DM];
 #pragma unroll
-    for (int d = 0; d < DM; ++d) xc[d] = d < sh.Dp ? __ldg(Xc + (size_t)c * sh.Dp + d) : 0.0f;
+    for (int d = 0; d < DM; ++d) xc[d] = d < Dp ? __ldg(Xc + (size_t)c * Dp + d) : 0.0f;
     const float vc = __ldg(v + c);
+    if (rmax == MV_ROWS) {
 #pragma unroll
-    for (int r = 0; r < MV_ROWS; ++r) {
-      if (r < rmax) {
-        float k = kernel_from_d2(kp, d2_t<DM>(kp, sx[r], xc));
+      for (int r = 0; r < MV_ROWS; ++r) {
+        float k = kval<KIND, DM>(sx[r], xc, D, sv, inv_p, sl);
         if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
         acc[r] = fmaf(k, vc, acc[r]);
+      }
+    } else {
+#pragma unroll
+      for (int r = 0; r < MV_ROWS; ++r) {
+        if (r < rmax) {
+          float k = kval<KIND, DM>(sx[r], xc, D, sv, inv_p, sl);
+          if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
+          acc[r] = fmaf(k, vc, acc[r]);
+        }
       }
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int r = 0; r < MV_ROWS; ++r) {
-    const float s = warp_sum(acc[r]);
-    if (lane == 0) sred[warp][r] = s;
+    const float t = warp_sum(acc[r]);
+    if (lane == 0) sred[warp][r] = t;
   }
   __syncthreads();
   if (threadIdx.x < MV_ROWS && threadIdx.x < rmax) {
-    float s = 0.0f;
+    float t = 0.0f;
 #pragma unroll
-    for (int w = 0; w < MV_THREADS / 32; ++w) s += sred[w][threadIdx.x];
-    if (row_scale) s *= row_scale[r0 + threadIdx.x];
-    y[r0 + threadIdx.x] = s;
+    for (int w = 0; w < MV_THREADS / 32; ++w) t += sred[w][threadIdx.x];
+    if (row_scale) t *= row_scale[r0 + threadIdx.x];
+    y[r0 + threadIdx.x] = t;
   }
+}
+
+template <int KIND, int DM>
+static void mv_dispatch_m(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
+                          const float* M, long long ldm, const float* v, const float* row_scale, float* y,
+                          cudaStream_t st) {
+  const int grid = ceil_div(nr, mv_rows<DM>());
+  if (M)
+    gram_matvec_kernel<KIND, DM, true><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y);
+  else
+    gram_matvec_kernel<KIND, DM, false><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y);
+}
+
+template <int KIND>
+static void mv_dispatch_d(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
+                          const float* M, long long ldm, const float* v, const float* row_scale, float* y,
+                          cudaStream_t st) {
+  if (sh.Dp <= 4)
+    mv_dispatch_m<KIND, 4>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+  else if (sh.Dp <= 8)
+    mv_dispatch_m<KIND, 8>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+  else
+    mv_dispatch_m<KIND, 16>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
 }
 
 void launch_gram_matvec(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
                         const float* M, long long ldm, const float* v, const float* row_scale, float* y,
                         cudaStream_t st) {
-  const int grid = ceil_div(nr, MV_ROWS);
-#define PGB_MV(DM)                                                                                          \
-  if (M)                                                                                                    \
-    gram_matvec_kernel<DM, true><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y); \
-  else                                                                                                      \
-    gram_matvec_kernel<DM, false><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y);
-  if (sh.Dp <= 4) {
-    PGB_MV(4)
-  } else if (sh.Dp <= 8) {
-    PGB_MV(8)
-  } else {
-    PGB_MV(16)
-  }
-#undef PGB_MV
+  if (sh.kind == PGB_KERNEL_MATERN12)
+    mv_dispatch_d<PGB_KERNEL_MATERN12>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+  else if (sh.kind == PGB_KERNEL_EQ_PERIODIC)
+    mv_dispatch_d<PGB_KERNEL_EQ_PERIODIC>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+  else
+    mv_dispatch_d<PGB_KERNEL_EQ>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
 }
 
 // ---------------------------------------------------------------- dense matvec
@@ -247,8 +300,7 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(Shape sh, const float* 
       if (d < sh.D) {
         float v;
         if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-          const float t = (xr[d] - sxc[c][d]) * kp.pi_over_p;
-          v = (2.0f * sinf(t)) / kp.l[kp.nl == 1 ? 0 : d];
+          v = (2.0f * sinpif((xr[d] - sxc[c][d]) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
         } else {
           v = xr[d] - sxc[c][d];
         }

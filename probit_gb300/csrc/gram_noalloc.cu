@@ -76,7 +76,7 @@ extern "C" int pgb_gram_noalloc(const pgb_desc* desc, const float* theta, const 
   sh.nl = desc->n_lengthscales;
   sh.lik = desc->likelihood;
   sh.J = 0;
-  sh.pi_over_p = desc->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(M_PI / (double)desc->period) : 0.0f;
+  sh.inv_p = desc->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(1.0 / (double)desc->period) : 0.0f;
   const size_t need = ((size_t)n1 + (size_t)n2) * (size_t)sh.Dp;
   if (need > kScratchFloats) {
     std::fprintf(stderr,

@@ -34,6 +34,11 @@ struct DagJob {
   // RHS with the triangular solve instead).
   const int* reuse;
   int reuse_mode;
+  // optional per-task timestamps (globaltimer ns): [task][8] = start, k-loop
+  // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
+  // C assembled (after the accumulator is applied)
+  unsigned long long* trace;
+  unsigned long long* ptrace;   // optional: [nt][16] phase times of the diagonal factorisations
 };
 
 // gram.cu

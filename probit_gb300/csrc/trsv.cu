@@ -13,6 +13,62 @@ namespace pgb {
 
 constexpr int TS_THREADS = 256;
 
+// acc[r] (+)= sign * sum_c A[r, c] v[c] for a 128 x 128 tile A (row stride
+// lda): thread t owns row t >> 1 and columns (t & 1) * 64 .. +63; its 16
+// float4 loads are issued before any use.
+__device__ __forceinline__ void tile_mv_rows(const float* __restrict__ A, long long lda, const float* sv,
+                                             float* sacc, bool assign) {
+  const int t = threadIdx.x;
+  const int r = t >> 1, h = t & 1;
+  const float* a = A + (size_t)r * lda + h * 64;
+  float4 v[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) v[q] = __ldcg(reinterpret_cast<const float4*>(a) + q);
+  float s = 0.0f;
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const float* x = sv + h * 64 + 4 * q;
+    s = fmaf(v[q].x, x[0], s);
+    s = fmaf(v[q].y, x[1], s);
+    s = fmaf(v[q].z, x[2], s);
+    s = fmaf(v[q].w, x[3], s);
+  }
+  s += __shfl_xor_sync(0xffffffffu, s, 1);
+  if (h == 0) sacc[r] = assign ? s : sacc[r] - s;
+}
+
+// acc[c] (+)= sign * sum_r A[r, c] v[r]: thread t owns columns 4 (t & 31) ..
+// +3 and rows (t >> 5) * 16 .. +15; partial sums combined in spart.
+__device__ __forceinline__ void tile_mv_cols(const float* __restrict__ A, long long lda, const float* sv,
+                                             float* sacc, float (*spart)[T], bool assign) {
+  const int t = threadIdx.x;
+  const int cq = t & 31, g = t >> 5;
+  float4 v[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q)
+    v[q] = __ldcg(reinterpret_cast<const float4*>(A + (size_t)(g * 16 + q) * lda + 4 * cq));
+  float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+  for (int q = 0; q < 16; ++q) {
+    const float x = sv[g * 16 + q];
+    s.x = fmaf(v[q].x, x, s.x);
+    s.y = fmaf(v[q].y, x, s.y);
+    s.z = fmaf(v[q].z, x, s.z);
+    s.w = fmaf(v[q].w, x, s.w);
+  }
+  spart[g][4 * cq + 0] = s.x;
+  spart[g][4 * cq + 1] = s.y;
+  spart[g][4 * cq + 2] = s.z;
+  spart[g][4 * cq + 3] = s.w;
+  __syncthreads();
+  if (t < T) {
+    float tot = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) tot += spart[k][t];
+    sacc[t] = assign ? tot : sacc[t] - tot;
+  }
+}
+
 __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long long ld, const float* __restrict__ L,
                                                              const float* __restrict__ Linv,
                                                              const float* __restrict__ b, float* __restrict__ x,
@@ -22,9 +78,9 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
   if (run_if && *run_if != run_when) return;
   __shared__ float sacc[T];
   __shared__ float sx[T];
-  __shared__ float spart[2][T];
+  __shared__ float spart[8][T];
   __shared__ int s_q, s_ok;
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int tid = threadIdx.x;
   while (true) {
     __syncthreads();
     if (tid == 0) {
@@ -40,10 +96,12 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
       const int gi = i * T + tid;
       sacc[tid] = gi < n ? __ldcg(b + gi) : 0.0f;
     }
-    const int k_begin = trans ? i + 1 : 0;
-    const int k_end = trans ? nt : i;
+    // dependencies oldest first (the order they were solved in), so a block
+    // accumulates everything already available while the newest is pending
+    const int ndep = trans ? nt - 1 - i : i;
     bool ok = true;
-    for (int k = k_begin; k < k_end; ++k) {
+    for (int kk = 0; kk < ndep; ++kk) {
+      const int k = trans ? nt - 1 - kk : kk;
       if (tid == 0) {
         s_ok = wait_flag_geq(flags + k, 1, status) ? 1 : 0;
         __threadfence();
@@ -55,25 +113,10 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
       }
       if (tid < T) sx[tid] = __ldcg(x + (size_t)k * T + tid);
       __syncthreads();
-      if (!trans) {
-        // sacc[r] -= sum_c L[iT + r, kT + c] x_k[c]; warp w owns rows 16w..16w+15
-        for (int rr = 0; rr < 16; ++rr) {
-          const int r = warp * 16 + rr;
-          const float4 lv = __ldcg(reinterpret_cast<const float4*>(L + (size_t)(i * T + r) * ld + k * T + lane * 4));
-          float s = lv.x * sx[lane * 4] + lv.y * sx[lane * 4 + 1] + lv.z * sx[lane * 4 + 2] + lv.w * sx[lane * 4 + 3];
-          s = warp_sum(s);
-          if (lane == 0) sacc[r] -= s;
-        }
-      } else {
-        // sacc[r] -= sum_c L[kT + c, iT + r] x_k[c]
-        const int r = tid & (T - 1), half = tid >> 7;
-        float s = 0.0f;
-        for (int c = half * 64; c < half * 64 + 64; ++c)
-          s = fmaf(__ldcg(L + (size_t)(k * T + c) * ld + i * T + r), sx[c], s);
-        spart[half][r] = s;
-        __syncthreads();
-        if (tid < T) sacc[tid] -= spart[0][tid] + spart[1][tid];
-      }
+      if (!trans)
+        tile_mv_rows(L + (size_t)(i * T) * ld + k * T, ld, sx, sacc, false);   // sacc -= L_ik x_k
+      else
+        tile_mv_cols(L + (size_t)(k * T) * ld + i * T, ld, sx, sacc, spart, false);   // sacc -= L_ki^T x_k
       __syncthreads();
     }
     if (!ok) continue;
@@ -81,22 +124,10 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
     const float* Li = Linv + (size_t)i * T * T;
     if (tid < T) sx[tid] = sacc[tid];
     __syncthreads();
-    if (!trans) {
-      for (int rr = 0; rr < 16; ++rr) {
-        const int r = warp * 16 + rr;
-        const float4 lv = __ldcg(reinterpret_cast<const float4*>(Li + (size_t)r * T + lane * 4));
-        float s = lv.x * sx[lane * 4] + lv.y * sx[lane * 4 + 1] + lv.z * sx[lane * 4 + 2] + lv.w * sx[lane * 4 + 3];
-        s = warp_sum(s);
-        if (lane == 0) sacc[r] = s;
-      }
-    } else {
-      const int c = tid & (T - 1), half = tid >> 7;
-      float s = 0.0f;
-      for (int r = half * 64; r < half * 64 + 64; ++r) s = fmaf(__ldcg(Li + (size_t)r * T + c), sx[r], s);
-      spart[half][c] = s;
-      __syncthreads();
-      if (tid < T) sacc[tid] = spart[0][tid] + spart[1][tid];
-    }
+    if (!trans)
+      tile_mv_rows(Li, T, sx, sacc, true);
+    else
+      tile_mv_cols(Li, T, sx, sacc, spart, true);
     __syncthreads();
     if (tid < T) x[(size_t)i * T + tid] = sacc[tid];
     __syncthreads();
