@@ -171,6 +171,54 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a,
                 const float* W, const float* Xs, int32_t m, float* mean_out,
                 float* var_out, int32_t reuse_factor, void* stream);
 
+/* ---------------------------------------------------------------- batches
+ * Many independent GP problems, each with its own pgb_desc (n, d, kernel,
+ * likelihood, J, tolerance, maxiter), evaluated together: every kernel of
+ * the path covers all problems in one launch and each problem keeps its own
+ * Newton stopping rule.  The reference evaluates many problems by
+ * vmap(value_and_grad(objective)) (README.md:238-239,
+ * examples/classification.py:489-492); a batch replaces that call for
+ * problems of different shapes.
+ *
+ * Packed inputs and outputs (device, problems in creation order):
+ *   X      concatenated row-major (n_b x d_b) blocks            float32
+ *   y      concatenated n_b labels                                4 bytes each
+ *   theta  concatenated pgb_theta_size(desc_b) blocks            float32
+ *   values one negative log evidence per problem                 float32
+ *   grads  same layout as theta                                  float32
+ * pgb_batch_layout gives the element offsets of each problem's block (count
+ * + 1 entries each, the last one the total).  Per-problem numerical failures
+ * are recorded in per-problem status words (pgb_batch_status) and give NaN
+ * outputs for that problem only. */
+typedef struct pgb_batch pgb_batch;
+
+/* Create a batch of `count` problems with one device arena on the current
+ * device. */
+int pgb_batch_create(const pgb_desc* descs, int32_t count, pgb_batch** out);
+
+/* Release a batch and its device memory (after its work completed). */
+int pgb_batch_destroy(pgb_batch* b);
+
+/* Element offsets of each problem's block in the packed X, y and theta
+ * (host arrays of count + 1 entries; any may be NULL). */
+int pgb_batch_layout(const pgb_batch* b, int64_t* x_offsets, int64_t* y_offsets,
+                     int64_t* theta_offsets);
+
+/* Negative log evidence of every problem: LaplaceGP.objective
+ * (approximators.py:248-263) under vmap. */
+int pgb_batch_objective(pgb_batch* b, const float* X, const void* y, const float* theta,
+                        float* values, void* stream);
+
+/* Negative log evidence and its theta gradient of every problem:
+ * Approximator.value_and_grad (approximators.py:132-134) under vmap. */
+int pgb_batch_value_and_grad(pgb_batch* b, const float* X, const void* y,
+                             const float* theta, float* values, float* grads,
+                             void* stream);
+
+/* Per-problem status words (host array of count entries); synchronises
+ * `stream` first. */
+int pgb_batch_status(pgb_batch* b, pgb_status* out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@ CUDA kernels behind the C-ABI declared in ``include/probit_gb300.h``.
 """
 
 from .approximators import LaplaceGP
+from .batch import LaplaceBatch
 from .kernels import EQ, Matern12
 from .utilities import (
     check_cutpoints,
@@ -18,7 +19,7 @@ from .utilities import (
 )
 
 __all__ = [
-    "LaplaceGP", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
+    "LaplaceGP", "LaplaceBatch", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
     "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
     "check_cutpoints",
 ]

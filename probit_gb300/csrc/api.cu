@@ -1,27 +1,36 @@
 // Host orchestration and the extern "C" entry points of include/probit_gb300.h.
 //
-// A handle owns device workspace for one problem shape.  Each reference
-// method becomes one CUDA graph, captured once per handle and replayed:
+// One engine serves any number of independent GP problems (a batch; a single
+// GP handle is a batch of one).  Every kernel of the path covers all problems
+// of the batch in one launch: per-point and matvec kernels through maps from
+// thread block to (problem, local block), the factorisations through one
+// merged task list over every problem's tile DAG, the triangular solves
+// through one merged claim list.  Each reference method becomes one CUDA
+// graph, captured once per engine and replayed:
 //   weight      prep -> WHILE(newton step)                       (LaplaceGP.weight)
 //   posterior   weight -> precision -> factor of B at the final W (approximate_posterior)
 //   objective   posterior + evidence                              (LaplaceGP.objective)
 //   value_grad  objective with L^-T + implicit gradient           (value_and_grad)
-// The Newton loop is a conditional WHILE node: its last kernel evaluates the
-// jaxopt stopping rule on the device and sets the loop condition, so no step
-// synchronises with the host.
+// The Newton loop is a conditional WHILE node: its last kernels evaluate the
+// jaxopt stopping rule of every problem on the device and keep the loop
+// going while any problem is still iterating; problems that stopped are
+// skipped by every kernel of the step.  No step synchronises with the host.
+#include <algorithm>
+#include <climits>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
-#include <cmath>
-#include <climits>
+#include <map>
 #include <mutex>
+#include <numeric>
 #include <vector>
 
 #include "kernels.cuh"
 
 using namespace pgb;
 
-#define PGB_VERSION_STRING "probit_gb300 0.1.0 (sm_103a)"
+#define PGB_VERSION_STRING "probit_gb300 0.2.0 (sm_103a)"
 
 #define CU_TRY(expr)                                                                    \
   do {                                                                                  \
@@ -33,99 +42,100 @@ using namespace pgb;
     }                                                                                   \
   } while (0)
 
+#define PGB_TRY(expr)          \
+  do {                         \
+    int _r = (expr);           \
+    if (_r != PGB_OK) return _r; \
+  } while (0)
+
 namespace {
 
 enum GraphOp { OP_WEIGHT = 0, OP_POSTERIOR = 1, OP_OBJECTIVE = 2, OP_VG = 3, OP_COUNT = 4 };
 enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_COUNT = 4 };
+enum Counter { C_DAG = 0, C_TRSV_T = 1, C_PREDICT = 2, C_TRSV_L = 3, C_SYRK = 4, C_COUNT = 8 };
 
 constexpr int kStatusWords = 8;
 
-__global__ void reset_status_kernel(int* status) {
-  if (threadIdx.x < kStatusWords) status[threadIdx.x] = 0;
-  if (threadIdx.x == 0) status[ST_NOTPD_COL] = INT_MAX;
-}
+// Bump allocator over one device allocation (256-byte aligned pieces).  Run
+// once with base 0 to size the arena, then with the real base.
+struct Bump {
+  uintptr_t base = 0;
+  size_t off = 0;
+  template <class Tp>
+  Tp* take(size_t count) {
+    off = (off + 255) & ~(size_t)255;
+    Tp* p = reinterpret_cast<Tp*>(base + off);
+    off += std::max<size_t>(count, 1) * sizeof(Tp);
+    return p;
+  }
+};
 
-}  // namespace
+int dm_of(int Dp) { return Dp <= 4 ? 4 : (Dp <= 8 ? 8 : 16); }
 
-struct pgb_gp {
-  pgb_desc desc;
-  Shape sh;
-  int n = 0, nt = 0, n_pad = 0, P = 0;
-  long long ld = 0;
-  int num_sms = 0;
-  int device = 0;
-  // inputs (copied in per call)
-  float* X_in = nullptr;
-  void* y_in = nullptr;
-  float* theta = nullptr;
-  // features and factor
-  float* Xf = nullptr;
-  float* L = nullptr;
-  float* Linv = nullptr;   // inverses of the diagonal tiles of L (nt x T x T)
-  float* Rv = nullptr;     // RHS_VEC row tile (T x ld)
-  float* Rz = nullptr;     // RHS_IDENT rows (n_pad x ld): L^-T
-  float* Binv = nullptr;   // n_pad x ld
-  // vectors (n_pad)
-  // b holds the Newton residual r = d1 - a, t the right-hand side r / sqrt W
-  float *a = nullptr, *f = nullptr, *d1 = nullptr, *W = nullptr, *sw = nullptr, *b = nullptr, *t = nullptr,
-        *x = nullptr, *logp = nullptr, *d3 = nullptr, *dsig = nullptr, *svec = nullptr, *rv = nullptr,
-        *zbar = nullptr, *tz = nullptr, *y2 = nullptr, *Ky2 = nullptr, *u = nullptr, *c = nullptr,
-        *rowdot = nullptr;
-  float* sw_prev = nullptr; // sqrt W of the resident factor (bitwise reuse test)
-  int* reuse = nullptr;    // [0] factor valid, [1] W differs, [2] reuse decision
-  float* scal = nullptr;   // [0] err, [1] value
-  float* grad = nullptr;
-  int* status = nullptr;
-  int* ready = nullptr;    // (2 nt) x nt
-  int* counters = nullptr; // [0] dag, [1] trsv (trans), [2] predict dag, [3] trsv (lower)
-  int* tflags = nullptr;   // 2 nt: trans solve, lower solve
-  double* part = nullptr;
-  double* tpart = nullptr;
-  double* lpart = nullptr;
-  // task lists (device)
-  int4* tasks[JOB_COUNT] = {nullptr, nullptr, nullptr, nullptr};
-  int ntasks[JOB_COUNT] = {0, 0, 0, 0};
-  int2* tiles_lower = nullptr;
-  int ntiles_lower = 0;
-  DagJob* jobs = nullptr;  // device [JOB_COUNT]
-  DagJob hjobs[JOB_COUNT];
-  // predict workspace (grown on demand)
-  float* Rc = nullptr;
-  float* rowsq = nullptr;
-  float* Xq = nullptr;
-  float* Xq_in = nullptr;
-  int* ready_c = nullptr;
-  int4* tasks_c = nullptr;
-  long long cap_c = 0;     // predict rows allocated
-  int m_tasks = -1;
+struct MvGroup {
+  int kind, DM;
+  std::vector<int2> h;
+  int2* map = nullptr;
+};
+struct TraceGroup {
+  int DM;
+  std::vector<int4> h;
+  int4* tiles = nullptr;
+};
+
+// Device state of a batch of problems.
+struct Engine {
+  int nprob = 0;
+  std::vector<pgb_desc> desc;
+  std::vector<Shape> sh;
+  std::vector<int> nt, th;                 // tiles per dimension, theta size
+  std::vector<size_t> x_off, y_off, th_off;   // offsets (elements) into the packed inputs
+  size_t x_total = 0, y_total = 0, th_total = 0;
+  int num_sms = 0, device = 0, dag_dm = 4, nt_max = 1;
+  std::vector<Prob> hp;                    // host copy of the problem table
+  Prob* probs = nullptr;
+  void* arena = nullptr;                   // everything but the gradient matrices
+  void* garena = nullptr;                  // L^-T and B^-1 of every problem
+  float* X_all = nullptr;
+  void* y_all = nullptr;
+  float* theta_all = nullptr;
+  float* value_all = nullptr;
+  float* err_all = nullptr;
+  float* grad_all = nullptr;
+  int* status_all = nullptr;
+  int* active_all = nullptr;
+  int* reuse_all = nullptr;
+  int* counters = nullptr;
+  int* any_active = nullptr;
+  int* ready_all = nullptr;
+  size_t ready_words = 0;
+  int* tflags_all = nullptr;
+  size_t tflags_words = 0;
+  // block maps
+  std::vector<int2> h_vmap, h_bmap, h_claims;
+  std::vector<int4> h_syrk;
+  std::vector<int4> h_tasks[3];
+  int2* vmap = nullptr;
+  int nvb = 0;
+  int2* bmap = nullptr;
+  int nbb = 0;
+  std::vector<MvGroup> mv;
+  std::vector<TraceGroup> tr;
+  int4* syrk_tiles = nullptr;
+  int nsyrk = 0;
+  DagJob* jobs = nullptr;                  // [problem * JOB_COUNT + slot]
+  std::vector<DagJob> hjobs;
+  int4* tasks[3] = {nullptr, nullptr, nullptr};
+  int ntasks[3] = {0, 0, 0};
+  int2* claims = nullptr;
+  int nclaims = 0;
   // graphs
   cudaGraphExec_t gexec[OP_COUNT] = {nullptr, nullptr, nullptr, nullptr};
   cudaStream_t cap_s = nullptr, cap_s2 = nullptr;
-  int grad_ready = 0;      // Rz / Binv allocated
-  int eager = 0;           // PGB_EAGER=1: launch kernels directly, host-driven Newton loop
-  unsigned long long* trace = nullptr;   // PGB_TRACE=1: per-task timestamps of the DAG
-  int factor_valid = 0;    // L is the factor of B at the resident W (same theta)
+  int grad_ready = 0;
+  int eager = 0;                           // PGB_EAGER=1: kernels launched directly, host-driven loop
+  unsigned long long* trace = nullptr;     // PGB_TRACE=1: per-task timestamps of the DAG
 };
-
-namespace {
-
-template <typename Tp>
-int dev_alloc(Tp** p, size_t count) {
-  if (count == 0) count = 1;
-  cudaError_t e = cudaMalloc(reinterpret_cast<void**>(p), count * sizeof(Tp));
-  if (e != cudaSuccess) {
-    *p = nullptr;
-    cudaGetLastError();
-    return PGB_ENOMEM;
-  }
-  return PGB_OK;
-}
-
-#define ALLOC_TRY(p, n)                   \
-  do {                                    \
-    int _r = dev_alloc(&(p), (size_t)(n)); \
-    if (_r != PGB_OK) return _r;          \
-  } while (0)
 
 int validate(const pgb_desc* d) {
   if (!d) return PGB_EINVAL;
@@ -154,6 +164,10 @@ Shape make_shape(const pgb_desc* d) {
   return s;
 }
 
+int theta_size_of(const pgb_desc* d) {
+  return theta_len(d->n_lengthscales, d->likelihood, d->likelihood == PGB_LIK_GAUSSIAN ? 0 : d->j);
+}
+
 std::once_flag g_attr_once;
 void setup_attributes() {
   std::call_once(g_attr_once, [] {
@@ -179,153 +193,428 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
   return v;
 }
 
-int upload_tasks(const std::vector<int4>& v, int4** dst) {
-  ALLOC_TRY(*dst, v.size());
-  CU_TRY(cudaMemcpy(*dst, v.data(), v.size() * sizeof(int4), cudaMemcpyHostToDevice));
+template <class Tp>
+int upload(Tp* dst, const std::vector<Tp>& v) {
+  if (!v.empty()) CU_TRY(cudaMemcpy(dst, v.data(), v.size() * sizeof(Tp), cudaMemcpyHostToDevice));
   return PGB_OK;
 }
 
-int dag_grid(const pgb_gp* gp, int ntasks) { return std::max(1, std::min(gp->num_sms, ntasks)); }
+// Assign every device pointer of the engine from `base` (0: sizing pass).
+size_t layout(Engine& e, uintptr_t base) {
+  Bump b;
+  b.base = base;
+  const int np = e.nprob;
+  e.X_all = b.take<float>(e.x_total);
+  e.y_all = b.take<int>(e.y_total);
+  e.theta_all = b.take<float>(e.th_total);
+  e.value_all = b.take<float>(np);
+  e.err_all = b.take<float>(np);
+  e.grad_all = b.take<float>(e.th_total);
+  e.status_all = b.take<int>((size_t)np * kStatusWords);
+  e.active_all = b.take<int>(np);
+  e.reuse_all = b.take<int>((size_t)np * 4);
+  e.counters = b.take<int>(C_COUNT);
+  e.any_active = b.take<int>(2);
+  e.ready_all = b.take<int>(e.ready_words);
+  e.tflags_all = b.take<int>(e.tflags_words);
+  e.probs = b.take<Prob>(np);
+  e.jobs = b.take<DagJob>((size_t)np * JOB_COUNT);
+  e.vmap = b.take<int2>(e.h_vmap.size());
+  e.bmap = b.take<int2>(e.h_bmap.size());
+  e.claims = b.take<int2>(e.h_claims.size());
+  e.syrk_tiles = b.take<int4>(e.h_syrk.size());
+  for (int k = 0; k < 3; ++k) e.tasks[k] = b.take<int4>(e.h_tasks[k].size());
+  for (MvGroup& g : e.mv) g.map = b.take<int2>(g.h.size());
+  for (TraceGroup& g : e.tr) g.tiles = b.take<int4>(g.h.size());
+  size_t ready_off = 0, tflags_off = 0;
+  for (int p = 0; p < np; ++p) {
+    Prob& q = e.hp[p];
+    const Shape& s = e.sh[p];
+    const int nt = e.nt[p];
+    const size_t npad = (size_t)nt * T;
+    const size_t ld = npad;
+    q.sh = s;
+    q.nt = nt;
+    q.n_pad = (int)npad;
+    q.ld = (long long)ld;
+    q.tol = e.desc[p].tolerance;
+    q.maxiter = e.desc[p].maxiter;
+    q.X = e.X_all + e.x_off[p];
+    q.y = static_cast<int*>(e.y_all) + e.y_off[p];
+    q.theta = e.theta_all + e.th_off[p];
+    q.Xf = b.take<float>(npad * s.Dp);
+    q.L = b.take<float>(npad * ld);
+    q.Linv = b.take<float>((size_t)nt * T * T);
+    q.Rv = b.take<float>((size_t)T * ld);
+    float** vecs[] = {&q.a,    &q.f,    &q.d1, &q.W,    &q.sw, &q.r,  &q.t, &q.x, &q.logp, &q.d3,
+                      &q.dsig, &q.svec, &q.rv, &q.zbar, &q.tz, &q.y2, &q.u, &q.c, &q.rowdot, &q.sw_prev};
+    for (float** v : vecs) *v = b.take<float>(npad);
+    const size_t nvb = (size_t)ceil_div((int)npad, VT);
+    q.part = b.take<double>(nvb + 8);
+    q.tpart = b.take<double>((size_t)nt * (nt + 1) / 2 * (MAX_D + 1));
+    q.lpart = b.take<double>(nvb * (MAX_THETA + 2));
+    q.err = e.err_all + p;
+    q.value = e.value_all + p;
+    q.grad = e.grad_all + e.th_off[p];
+    q.status = e.status_all + (size_t)p * kStatusWords;
+    q.active = e.active_all + p;
+    q.reuse = e.reuse_all + (size_t)p * 4;
+    q.tflags = e.tflags_all + tflags_off;
+    tflags_off += 2 * (size_t)nt;
+    q.Rz = nullptr;
+    q.Binv = nullptr;
+    // factorisation jobs of this problem
+    for (int k = 0; k < JOB_COUNT; ++k) {
+      DagJob& j = e.hjobs[(size_t)p * JOB_COUNT + k];
+      std::memset(&j, 0, sizeof(j));
+      j.n = s.n;
+      j.nt = nt;
+      j.ld = (long long)ld;
+      j.L = q.L;
+      j.Linv = q.Linv;
+      j.Xf = q.Xf;
+      j.sw = q.sw;
+      j.theta = q.theta;
+      j.sh = s;
+      j.ready = e.ready_all + ready_off;
+      j.status = q.status;
+      j.reuse = q.reuse + 2;
+      j.reuse_mode = 0;
+    }
+    ready_off += 2 * (size_t)nt * nt;
+    DagJob* jb = &e.hjobs[(size_t)p * JOB_COUNT];
+    jb[JOB_VEC].rhs_kind = RHS_VEC;
+    jb[JOB_VEC].nrt = 1;
+    jb[JOB_VEC].nrhs = 1;
+    jb[JOB_VEC].R = q.Rv;
+    jb[JOB_VEC].rhs_vec = q.t;
+    jb[JOB_VEC].reuse_mode = 2;
+    jb[JOB_VEC].active = q.active;
+    jb[JOB_NONE].rhs_kind = RHS_NONE;
+    jb[JOB_NONE].reuse_mode = 1;
+    jb[JOB_IDENT].rhs_kind = RHS_IDENT;
+    jb[JOB_IDENT].reuse_mode = 1;
+    jb[JOB_IDENT].nrt = nt;
+    jb[JOB_IDENT].nrhs = (int)npad;
+    jb[JOB_CROSS].rhs_kind = RHS_CROSS;
+  }
+  return b.off;
+}
+
+void engine_free(Engine& e) {
+  for (int k = 0; k < OP_COUNT; ++k)
+    if (e.gexec[k]) cudaGraphExecDestroy(e.gexec[k]);
+  if (e.arena) cudaFree(e.arena);
+  if (e.garena) cudaFree(e.garena);
+  if (e.trace) cudaFree(e.trace);
+  if (e.cap_s) cudaStreamDestroy(e.cap_s);
+  if (e.cap_s2) cudaStreamDestroy(e.cap_s2);
+  e.arena = e.garena = nullptr;
+  e.trace = nullptr;
+}
+
+int engine_upload_tables(Engine& e) {
+  CU_TRY(cudaMemcpy(e.probs, e.hp.data(), sizeof(Prob) * e.hp.size(), cudaMemcpyHostToDevice));
+  CU_TRY(cudaMemcpy(e.jobs, e.hjobs.data(), sizeof(DagJob) * e.hjobs.size(), cudaMemcpyHostToDevice));
+  return PGB_OK;
+}
+
+// Build the engine of `count` problems: shapes, maps, task lists, one
+// arena.  Problems are ranked by size (largest first) for the merged DAG and
+// solve orders, so the longest critical paths start first.
+int engine_init(Engine& e, const pgb_desc* descs, int count) {
+  if (!descs || count < 1) return PGB_EINVAL;
+  for (int p = 0; p < count; ++p) PGB_TRY(validate(descs + p));
+  setup_attributes();
+  e.nprob = count;
+  e.desc.assign(descs, descs + count);
+  e.sh.resize(count);
+  e.nt.resize(count);
+  e.th.resize(count);
+  e.x_off.resize(count);
+  e.y_off.resize(count);
+  e.th_off.resize(count);
+  e.hp.assign(count, Prob{});
+  e.hjobs.assign((size_t)count * JOB_COUNT, DagJob{});
+  e.dag_dm = 4;
+  e.nt_max = 1;
+  for (int p = 0; p < count; ++p) {
+    e.sh[p] = make_shape(descs + p);
+    e.nt[p] = ceil_div(descs[p].n, T);
+    e.th[p] = theta_size_of(descs + p);
+    e.x_off[p] = e.x_total;
+    e.y_off[p] = e.y_total;
+    e.th_off[p] = e.th_total;
+    e.x_total += (size_t)descs[p].n * descs[p].d;
+    e.y_total += (size_t)descs[p].n;
+    e.th_total += (size_t)e.th[p];
+    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p];
+    e.tflags_words += 2 * (size_t)e.nt[p];
+    e.dag_dm = std::max(e.dag_dm, dm_of(e.sh[p].Dp));
+    e.nt_max = std::max(e.nt_max, e.nt[p]);
+  }
+  CU_TRY(cudaGetDevice(&e.device));
+  CU_TRY(cudaDeviceGetAttribute(&e.num_sms, cudaDevAttrMultiProcessorCount, e.device));
+  // size ranking (largest n first, index order among equals)
+  std::vector<int> order(count), rank(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return descs[a].n > descs[b].n; });
+  for (int r = 0; r < count; ++r) rank[order[r]] = r;
+  // per-point map
+  for (int p = 0; p < count; ++p)
+    for (int blk = 0; blk < ceil_div(e.nt[p] * T, VT); ++blk) e.h_vmap.push_back(make_int2(p, blk));
+  e.nvb = (int)e.h_vmap.size();
+  // B^-1 row map (8 rows per block)
+  for (int p = 0; p < count; ++p)
+    for (int blk = 0; blk < ceil_div(descs[p].n, 8); ++blk) e.h_bmap.push_back(make_int2(p, blk));
+  e.nbb = (int)e.h_bmap.size();
+  // Gram matvec groups by (kernel, feature width)
+  {
+    std::map<std::pair<int, int>, int> gi;
+    for (int pr = 0; pr < count; ++pr) {
+      const int p = order[pr];
+      const int DM = dm_of(e.sh[p].Dp);
+      const auto key = std::make_pair(e.sh[p].kind, DM);
+      if (!gi.count(key)) {
+        gi[key] = (int)e.mv.size();
+        MvGroup g;
+        g.kind = key.first;
+        g.DM = DM;
+        e.mv.push_back(g);
+      }
+      MvGroup& g = e.mv[gi[key]];
+      const int rows = 128 / DM;
+      for (int blk = 0; blk < ceil_div(descs[p].n, rows); ++blk) g.h.push_back(make_int2(p, blk));
+    }
+  }
+  // gradient trace tiles by feature width; B^-1 tiles longest k-range first
+  {
+    std::map<int, int> gi;
+    std::vector<std::pair<int, int4>> sy;
+    for (int pr = 0; pr < count; ++pr) {
+      const int p = order[pr];
+      const int DM = dm_of(e.sh[p].Dp);
+      if (!gi.count(DM)) {
+        gi[DM] = (int)e.tr.size();
+        TraceGroup g;
+        g.DM = DM;
+        e.tr.push_back(g);
+      }
+      TraceGroup& g = e.tr[gi[DM]];
+      int ord = 0;
+      for (int I = 0; I < e.nt[p]; ++I)
+        for (int J = 0; J <= I; ++J) {
+          g.h.push_back(make_int4(p, I, J, ord++));
+          sy.push_back(std::make_pair(e.nt[p] - I, make_int4(p, I, J, 0)));
+        }
+    }
+    std::stable_sort(sy.begin(), sy.end(), [](const std::pair<int, int4>& a, const std::pair<int, int4>& b) {
+      return a.first > b.first;
+    });
+    for (auto& x : sy) e.h_syrk.push_back(x.second);
+    e.nsyrk = (int)e.h_syrk.size();
+  }
+  // merged DAG task lists: column by column, problems by rank within a column
+  {
+    const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
+    for (int k = 0; k < 3; ++k) {
+      struct Key {
+        int j, rank, seq;
+        int4 t;
+      };
+      std::vector<Key> all;
+      for (int p = 0; p < count; ++p) {
+        std::vector<int4> v = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
+        for (size_t s = 0; s < v.size(); ++s) all.push_back(Key{v[s].z, rank[p], (int)s, v[s]});
+      }
+      std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
+        if (a.j != b.j) return a.j < b.j;
+        if (a.rank != b.rank) return a.rank < b.rank;
+        return a.seq < b.seq;
+      });
+      for (const Key& x : all) e.h_tasks[k].push_back(x.t);
+      e.ntasks[k] = (int)e.h_tasks[k].size();
+    }
+  }
+  // merged solve claims: position by position, problems by rank
+  {
+    for (int q = 0; q < e.nt_max; ++q)
+      for (int r = 0; r < count; ++r) {
+        const int p = order[r];
+        if (q < e.nt[p]) e.h_claims.push_back(make_int2(p, q));
+      }
+    e.nclaims = (int)e.h_claims.size();
+  }
+  // one arena
+  const size_t bytes = layout(e, 0);
+  if (cudaMalloc(&e.arena, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    e.arena = nullptr;
+    return PGB_ENOMEM;
+  }
+  layout(e, reinterpret_cast<uintptr_t>(e.arena));
+  CU_TRY(cudaMemset(e.arena, 0, bytes));
+  PGB_TRY(upload(e.vmap, e.h_vmap));
+  PGB_TRY(upload(e.bmap, e.h_bmap));
+  PGB_TRY(upload(e.claims, e.h_claims));
+  PGB_TRY(upload(e.syrk_tiles, e.h_syrk));
+  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k]));
+  for (MvGroup& g : e.mv) PGB_TRY(upload(g.map, g.h));
+  for (TraceGroup& g : e.tr) PGB_TRY(upload(g.tiles, g.h));
+  {
+    const char* ev = std::getenv("PGB_EAGER");
+    e.eager = (ev && ev[0] == '1') ? 1 : 0;
+    const char* tv = std::getenv("PGB_TRACE");
+    if (tv && tv[0] == '1') {
+      size_t mx = 0;
+      for (int k = 0; k < 3; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
+      if (cudaMalloc(&e.trace, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 16)) == cudaSuccess) {
+        for (DagJob& j : e.hjobs) {
+          j.trace = e.trace;
+          j.ptrace = e.trace + mx * 8;
+        }
+      } else {
+        cudaGetLastError();
+        e.trace = nullptr;
+      }
+    }
+  }
+  PGB_TRY(engine_upload_tables(e));
+  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s, cudaStreamNonBlocking));
+  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s2, cudaStreamNonBlocking));
+  return PGB_OK;
+}
+
+// L^-T and B^-1 of every problem, allocated on the first gradient request.
+int ensure_grad_buffers(Engine& e) {
+  if (e.grad_ready) return PGB_OK;
+  size_t total = 0;
+  for (int p = 0; p < e.nprob; ++p) total += 2 * (((size_t)e.hp[p].n_pad * e.hp[p].ld * sizeof(float) + 255) & ~(size_t)255);
+  if (cudaMalloc(&e.garena, total) != cudaSuccess) {
+    cudaGetLastError();
+    e.garena = nullptr;
+    return PGB_ENOMEM;
+  }
+  CU_TRY(cudaMemset(e.garena, 0, total));
+  Bump b;
+  b.base = reinterpret_cast<uintptr_t>(e.garena);
+  for (int p = 0; p < e.nprob; ++p) {
+    const size_t mat = (size_t)e.hp[p].n_pad * e.hp[p].ld;
+    e.hp[p].Rz = b.take<float>(mat);
+    e.hp[p].Binv = b.take<float>(mat);
+    e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].R = e.hp[p].Rz;
+  }
+  PGB_TRY(engine_upload_tables(e));
+  e.grad_ready = 1;
+  return PGB_OK;
+}
+
+int dag_grid(const Engine& e, int ntasks) { return std::max(1, std::min(e.num_sms, ntasks)); }
+int trsv_grid(const Engine& e) { return std::max(1, std::min(e.nclaims, 4 * e.num_sms)); }
 
 // ---------------------------------------------------------------- enqueue helpers
-void enq_reset_status(pgb_gp* gp, cudaStream_t s) { reset_status_kernel<<<1, 32, 0, s>>>(gp->status); }
-
-void enq_prep(pgb_gp* gp, cudaStream_t s) {
-  launch_prep_features(gp->sh, gp->X_in, gp->theta, gp->Xf, gp->n, gp->n_pad, s);
+void enq_matvec(Engine& e, MatvecOp op, cudaStream_t s) {
+  for (MvGroup& g : e.mv) launch_gram_matvec(g.kind, g.DM, e.probs, g.map, (int)g.h.size(), op, s);
 }
 
-void enq_dag(pgb_gp* gp, int job, cudaStream_t s) {
-  const int nrt = gp->hjobs[job].nrt;
-  cudaMemsetAsync(gp->ready, 0, sizeof(int) * (size_t)(gp->nt + nrt) * gp->nt, s);
-  cudaMemsetAsync(gp->counters, 0, sizeof(int), s);
-  launch_dag_factor(gp->jobs, gp->tasks[job], gp->ntasks[job], gp->counters, gp->sh.Dp,
-                    dag_grid(gp, gp->ntasks[job]), s);
+void enq_dag(Engine& e, int slot, cudaStream_t s) {
+  cudaMemsetAsync(e.ready_all, 0, sizeof(int) * e.ready_words, s);
+  cudaMemsetAsync(e.counters + C_DAG, 0, sizeof(int), s);
+  launch_dag_factor(e.jobs, e.tasks[slot], e.ntasks[slot], e.counters + C_DAG, e.dag_dm,
+                    dag_grid(e, e.ntasks[slot]), s);
 }
 
-void enq_newton_step(pgb_gp* gp, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
-  const Shape& sh = gp->sh;
+void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
   // f = K a
-  launch_gram_matvec(sh, gp->theta, gp->Xf, gp->n, gp->Xf, gp->n, nullptr, 0, gp->a, nullptr, gp->f, s);
+  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);
   // d1, W, sqrt W, r = d1 - a, t = r / sqrt W
-  launch_newton_lik(sh, gp->theta, gp->f, gp->y_in, gp->a, gp->n_pad, gp->d1, gp->W, gp->sw, gp->b, gp->t, s);
+  launch_newton_lik(e.probs, e.vmap, e.nvb, s);
   // bitwise-unchanged W keeps the resident factor
-  launch_reuse_check(gp->n, gp->sw, gp->sw_prev, gp->reuse, s);
+  launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
   // new W: L L^T = B and w = L^-1 t in one factorisation (skipped on reuse)
-  enq_dag(gp, JOB_VEC, s);
-  launch_reuse_mark_valid(gp->reuse, gp->status, s);
-  // reused W: w = L^-1 t by the forward wavefront solve (skipped otherwise)
-  cudaMemsetAsync(gp->tflags + gp->nt, 0, sizeof(int) * gp->nt, s);
-  cudaMemsetAsync(gp->counters + 3, 0, sizeof(int), s);
-  launch_trsv(gp->n, gp->nt, gp->ld, gp->L, gp->Linv, gp->t, gp->Rv, 0, gp->tflags + gp->nt, gp->counters + 3, gp->status,
-              std::min(gp->nt, gp->num_sms), gp->reuse + 2, 1, s);
-  // x = L^-T w
-  cudaMemsetAsync(gp->tflags, 0, sizeof(int) * gp->nt, s);
-  cudaMemsetAsync(gp->counters + 1, 0, sizeof(int), s);
-  launch_trsv(gp->n, gp->nt, gp->ld, gp->L, gp->Linv, gp->Rv, gp->x, 1, gp->tflags, gp->counters + 1, gp->status,
-              std::min(gp->nt, gp->num_sms), nullptr, 0, s);
+  enq_dag(e, JOB_VEC, s);
+  launch_reuse_mark_valid(e.probs, e.nprob, s);
+  // reused W: w = L^-1 t by the forward wavefront solve; then x = L^-T w
+  cudaMemsetAsync(e.tflags_all, 0, sizeof(int) * e.tflags_words, s);
+  cudaMemsetAsync(e.counters + C_TRSV_T, 0, sizeof(int) * 3, s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 0, e.counters + C_TRSV_L, 1, 1, trsv_grid(e), s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 1, e.counters + C_TRSV_T, 0, 1, trsv_grid(e), s);
   // a += W^1/2 x, stopping rule
-  launch_newton_update(gp->n, gp->sw, gp->x, gp->a, gp->part, s);
-  launch_newton_finalize(gp->part, ceil_div(gp->n, 256), gp->desc.tolerance, gp->desc.maxiter, gp->status,
-                         gp->scal, h, use_cond, s);
+  launch_newton_update(e.probs, e.vmap, e.nvb, s);
+  launch_newton_finalize(e.probs, e.nprob, e.any_active, h, use_cond, s);
 }
 
-void enq_precision(pgb_gp* gp, cudaStream_t s) {
-  launch_gram_matvec(gp->sh, gp->theta, gp->Xf, gp->n, gp->Xf, gp->n, nullptr, 0, gp->a, nullptr, gp->f, s);
-  launch_lik_full(gp->sh, gp->theta, gp->f, gp->y_in, gp->n_pad, gp->logp, gp->d1, gp->d3, gp->W, gp->sw, s);
+void enq_precision(Engine& e, cudaStream_t s) {
+  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 0}, s);
+  launch_lik_full(e.probs, e.vmap, e.nvb, s);
 }
 
-void enq_grad(pgb_gp* gp, cudaStream_t s) {
-  const Shape& sh = gp->sh;
-  const int n = gp->n, np = gp->n_pad;
-  cudaMemsetAsync(gp->counters + 4, 0, sizeof(int), s);
-  launch_syrk_zzt(gp->Rz, gp->ld, gp->nt, gp->tiles_lower, gp->ntiles_lower, gp->Binv, gp->ld, gp->counters + 4,
-                  gp->status, std::max(1, std::min(gp->num_sms, gp->ntiles_lower)), s);
+void enq_grad(Engine& e, cudaStream_t s) {
+  cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
+  launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);
   // rowdot_i = sum_j B^-1_ij K_ij sw_j  ->  diag(Sigma)_i = rowdot_i / sw_i
-  launch_gram_matvec(sh, gp->theta, gp->Xf, n, gp->Xf, n, gp->Binv, gp->ld, gp->sw, nullptr, gp->rowdot, s);
-  launch_grad_vec1(n, np, gp->rowdot, gp->sw, gp->d3, gp->a, gp->d1, gp->dsig, gp->svec, gp->rv, s);
+  enq_matvec(e, MatvecOp{F_SW, F_NONE, F_ROWDOT, 1, 0}, s);
+  launch_grad_vec1(e.probs, e.vmap, e.nvb, s);
   // zbar = K (a - d1 - s)
-  launch_gram_matvec(sh, gp->theta, gp->Xf, n, gp->Xf, n, nullptr, 0, gp->rv, nullptr, gp->zbar, s);
+  enq_matvec(e, MatvecOp{F_RV, F_NONE, F_ZBAR, 0, 0}, s);
   // u = (I + K W)^-1 zbar = W^-1/2 B^-1 W^1/2 zbar
-  launch_scale_vec(n, np, gp->sw, gp->zbar, gp->tz, s);
-  launch_dense_matvec(gp->Binv, gp->ld, n, n, gp->tz, nullptr, gp->y2, s);
-  launch_grad_vec3(n, np, gp->y2, gp->sw, gp->a, gp->d1, gp->svec, gp->W, gp->u, gp->c, s);
-  launch_grad_trace(sh, gp->theta, gp->Xf, gp->Binv, gp->ld, gp->sw, gp->c, gp->a, gp->tiles_lower,
-                    gp->ntiles_lower, gp->tpart, s);
-  launch_grad_lik_final(sh, gp->theta, gp->f, gp->y_in, gp->dsig, gp->u, gp->tpart, gp->ntiles_lower, gp->lpart,
-                        gp->grad, s);
+  launch_scale_tz(e.probs, e.vmap, e.nvb, s);
+  launch_binv_matvec(e.probs, e.bmap, e.nbb, s);
+  launch_grad_vec3(e.probs, e.vmap, e.nvb, s);
+  for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, e.probs, g.tiles, (int)g.h.size(), s);
+  launch_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
 }
 
-int ensure_grad_buffers(pgb_gp* gp) {
-  if (gp->grad_ready) return PGB_OK;
-  const size_t mat = (size_t)gp->n_pad * gp->ld;
-  ALLOC_TRY(gp->Rz, mat);
-  ALLOC_TRY(gp->Binv, mat);
-  CU_TRY(cudaMemset(gp->Rz, 0, mat * sizeof(float)));
-  gp->hjobs[JOB_IDENT].R = gp->Rz;
-  CU_TRY(cudaMemcpy(gp->jobs + JOB_IDENT, &gp->hjobs[JOB_IDENT], sizeof(DagJob), cudaMemcpyHostToDevice));
-  gp->grad_ready = 1;
-  return PGB_OK;
+void enq_prologue(Engine& e, cudaStream_t s) {
+  launch_reset_problems(e.probs, e.vmap, e.nvb, 1, s);
+  launch_prep_features(e.probs, e.vmap, e.nvb, s);
 }
 
-void enq_prologue(pgb_gp* gp, cudaStream_t s) {
-  enq_reset_status(gp, s);
-  enq_prep(gp, s);
-  cudaMemsetAsync(gp->a, 0, sizeof(float) * gp->n_pad, s);
-  cudaMemsetAsync(gp->reuse, 0, sizeof(int) * 4, s);   // new theta: no resident factor
-}
-
-void enq_epilogue(pgb_gp* gp, int op, cudaStream_t s) {
+void enq_epilogue(Engine& e, int op, cudaStream_t s) {
   if (op >= OP_POSTERIOR) {
-    enq_precision(gp, s);
-    launch_reuse_check(gp->n, gp->sw, gp->sw_prev, gp->reuse, s);
-    enq_dag(gp, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
-    launch_reuse_mark_valid(gp->reuse, gp->status, s);
-    if (op >= OP_OBJECTIVE) launch_evidence(gp->n, gp->logp, gp->f, gp->a, gp->L, gp->ld, gp->part, gp->scal + 1, s);
-    if (op == OP_VG) enq_grad(gp, s);
+    launch_set_active(e.probs, e.nprob, 1, s);   // every problem takes part from here on
+    enq_precision(e, s);
+    launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
+    enq_dag(e, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
+    launch_reuse_mark_valid(e.probs, e.nprob, s);
+    if (op >= OP_OBJECTIVE) launch_evidence(e.probs, e.vmap, e.nvb, e.nprob, s);
+    if (op == OP_VG) enq_grad(e, s);
   }
 }
 
 // The same work without graphs: kernels launched directly, the Newton loop
-// driven from the host (one status read per step).  For profilers that do
-// not follow kernels inside conditional graph nodes.
-int run_eager(pgb_gp* gp, int op, cudaStream_t s) {
-  if (op == OP_VG) {
-    int r = ensure_grad_buffers(gp);
-    if (r != PGB_OK) return r;
-  }
-  enq_prologue(gp, s);
-  const char* tr = std::getenv("PGB_TRACE");
-  const bool trace = tr && tr[0] == '1';
-  for (int it = 0; it < gp->desc.maxiter; ++it) {
-    enq_newton_step(gp, s, 0, 0);
+// driven from the host (one flag read per step).  For profilers that do not
+// follow kernels inside conditional graph nodes.
+int run_eager(Engine& e, int op, cudaStream_t s) {
+  if (op == OP_VG) PGB_TRY(ensure_grad_buffers(e));
+  enq_prologue(e, s);
+  const char* tv = std::getenv("PGB_TRACE");
+  const bool trace = tv && tv[0] == '1';
+  int maxiter = 1;
+  for (const pgb_desc& d : e.desc) maxiter = std::max(maxiter, d.maxiter);
+  for (int it = 0; it < maxiter; ++it) {
+    enq_newton_step(e, s, 0, 0);
     int again = 0;
     float err = 0.0f;
-    int reuse[4] = {0, 0, 0, 0};
-    CU_TRY(cudaMemcpyAsync(&again, gp->status + ST_SPARE0, sizeof(int), cudaMemcpyDeviceToHost, s));
-    if (trace) {
-      CU_TRY(cudaMemcpyAsync(&err, gp->scal, sizeof(float), cudaMemcpyDeviceToHost, s));
-      CU_TRY(cudaMemcpyAsync(reuse, gp->reuse, sizeof(reuse), cudaMemcpyDeviceToHost, s));
-    }
+    CU_TRY(cudaMemcpyAsync(&again, e.any_active + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if (trace) CU_TRY(cudaMemcpyAsync(&err, e.err_all, sizeof(float), cudaMemcpyDeviceToHost, s));
     CU_TRY(cudaStreamSynchronize(s));
-    if (trace) std::fprintf(stderr, "probit_gb300: newton %d ||delta||=%.6g reuse=%d\n", it + 1, err, reuse[2]);
+    if (trace) std::fprintf(stderr, "probit_gb300: newton %d ||delta||[0]=%.6g\n", it + 1, err);
     if (!again) break;
   }
-  enq_epilogue(gp, op, s);
+  enq_epilogue(e, op, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
 }
 
 // Capture the graph of one operation.
-int build_graph(pgb_gp* gp, int op) {
-  if (gp->gexec[op]) return PGB_OK;
-  if (op == OP_VG) {
-    int r = ensure_grad_buffers(gp);
-    if (r != PGB_OK) return r;
-  }
-  cudaStream_t s = gp->cap_s, s2 = gp->cap_s2;
+int build_graph(Engine& e, int op) {
+  if (e.gexec[op]) return PGB_OK;
+  if (op == OP_VG) PGB_TRY(ensure_grad_buffers(e));
+  cudaStream_t s = e.cap_s, s2 = e.cap_s2;
   cudaGraph_t g = nullptr;
   CU_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-  enq_prologue(gp, s);
+  enq_prologue(e, s);
   // WHILE node for the Newton loop
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg = nullptr;
@@ -344,44 +633,59 @@ int build_graph(pgb_gp* gp, int op) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CU_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
   CU_TRY(cudaStreamBeginCaptureToGraph(s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  enq_newton_step(gp, s2, h, 1);
+  enq_newton_step(e, s2, h, 1);
   cudaGraph_t body_out = nullptr;
   CU_TRY(cudaStreamEndCapture(s2, &body_out));
-  enq_epilogue(gp, op, s);
+  enq_epilogue(e, op, s);
   CU_TRY(cudaStreamEndCapture(s, &g));
-  CU_TRY(cudaGraphInstantiate(&gp->gexec[op], g, 0));
+  CU_TRY(cudaGraphInstantiate(&e.gexec[op], g, 0));
   cudaGraphDestroy(g);
   return PGB_OK;
 }
 
-int ingest(pgb_gp* gp, const float* X, const void* y, const float* theta, cudaStream_t s) {
-  if (!X || !theta) return PGB_EINVAL;
-  CU_TRY(cudaMemcpyAsync(gp->X_in, X, sizeof(float) * (size_t)gp->n * gp->sh.D, cudaMemcpyDeviceToDevice, s));
-  CU_TRY(cudaMemcpyAsync(gp->theta, theta, sizeof(float) * gp->P, cudaMemcpyDeviceToDevice, s));
-  if (y) CU_TRY(cudaMemcpyAsync(gp->y_in, y, 4 * (size_t)gp->n, cudaMemcpyDeviceToDevice, s));
+int run_op(Engine& e, int op, cudaStream_t s) {
+  if (e.eager) return run_eager(e, op, s);
+  PGB_TRY(build_graph(e, op));
+  CU_TRY(cudaGraphLaunch(e.gexec[op], s));
   return PGB_OK;
 }
 
-int run_op(pgb_gp* gp, int op, const float* X, const void* y, const float* theta, cudaStream_t s) {
-  if (!y) return PGB_EINVAL;
-  if (gp->eager) {
-    int r = ingest(gp, X, y, theta, s);
-    if (r != PGB_OK) return r;
-    r = run_eager(gp, op, s);
-    if (r != PGB_OK) return r;
-    gp->factor_valid = op >= OP_POSTERIOR;
-    return PGB_OK;
-  }
-  int r = build_graph(gp, op);
-  if (r != PGB_OK) return r;
-  r = ingest(gp, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaGraphLaunch(gp->gexec[op], s));
-  gp->factor_valid = op >= OP_POSTERIOR;
+// Copy the caller's packed inputs into the engine (stream-ordered).
+int ingest(Engine& e, const float* X, const void* y, const float* theta, cudaStream_t s) {
+  if (!X || !theta) return PGB_EINVAL;
+  CU_TRY(cudaMemcpyAsync(e.X_all, X, sizeof(float) * e.x_total, cudaMemcpyDeviceToDevice, s));
+  CU_TRY(cudaMemcpyAsync(e.theta_all, theta, sizeof(float) * e.th_total, cudaMemcpyDeviceToDevice, s));
+  if (y) CU_TRY(cudaMemcpyAsync(e.y_all, y, 4 * e.y_total, cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
+}
+
+void status_from_words(const int* h, pgb_status* out) {
+  out->code = h[ST_CODE];
+  out->iterations = h[ST_ITERS];
+  out->notpd_col = h[ST_NOTPD_COL] == INT_MAX ? -1 : h[ST_NOTPD_COL];
+  out->converged = h[ST_CONVERGED];
 }
 
 }  // namespace
+
+struct pgb_gp {
+  Engine e;
+  // predict workspace (grown on demand)
+  float* Rc = nullptr;
+  float* rowsq = nullptr;
+  float* Xq = nullptr;
+  float* Xq_in = nullptr;
+  int* ready_c = nullptr;
+  int4* tasks_c = nullptr;
+  int ntasks_c = 0;
+  long long cap_c = 0;     // predict rows allocated
+  int m_tasks = -1;
+  int factor_valid = 0;    // L is the factor of B at the resident W (same theta)
+};
+
+struct pgb_batch {
+  Engine e;
+};
 
 // ==================================================================== C-ABI
 extern "C" {
@@ -406,7 +710,7 @@ const char* pgb_strerror(int code) {
 int pgb_theta_size(const pgb_desc* desc) {
   int r = validate(desc);
   if (r != PGB_OK) return r;
-  return theta_len(desc->n_lengthscales, desc->likelihood, desc->likelihood == PGB_LIK_GAUSSIAN ? 0 : desc->j);
+  return theta_size_of(desc);
 }
 
 int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
@@ -414,143 +718,22 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
   *out = nullptr;
   int r = validate(desc);
   if (r != PGB_OK) return r;
-  setup_attributes();
   pgb_gp* gp = new pgb_gp();
-  gp->desc = *desc;
-  gp->sh = make_shape(desc);
-  gp->n = desc->n;
-  gp->nt = ceil_div(desc->n, T);
-  gp->n_pad = gp->nt * T;
-  gp->ld = gp->n_pad;
-  gp->P = pgb_theta_size(desc);
-  CU_TRY(cudaGetDevice(&gp->device));
-  CU_TRY(cudaDeviceGetAttribute(&gp->num_sms, cudaDevAttrMultiProcessorCount, gp->device));
-  const size_t np = gp->n_pad;
-  const size_t mat = np * (size_t)gp->ld;
-#define A(p, cnt)                         \
-  do {                                    \
-    if (dev_alloc(&(p), (cnt)) != PGB_OK) { \
-      pgb_gp_destroy(gp);                 \
-      return PGB_ENOMEM;                  \
-    }                                     \
-  } while (0)
-  A(gp->X_in, (size_t)gp->n * desc->d);
-  {
-    int* yy = nullptr;
-    A(yy, np);
-    gp->y_in = yy;
+  r = engine_init(gp->e, desc, 1);
+  if (r != PGB_OK) {
+    pgb_gp_destroy(gp);
+    return r;
   }
-  A(gp->theta, (size_t)MAX_THETA);
-  A(gp->Xf, np * gp->sh.Dp);
-  A(gp->L, mat);
-  A(gp->Linv, (size_t)gp->nt * T * T);
-  A(gp->Rv, (size_t)T * gp->ld);
-  float** vecs[] = {&gp->a, &gp->f, &gp->d1, &gp->W, &gp->sw, &gp->b, &gp->t, &gp->x, &gp->logp, &gp->d3,
-                    &gp->dsig, &gp->svec, &gp->rv, &gp->zbar, &gp->tz, &gp->y2, &gp->Ky2, &gp->u, &gp->c,
-                    &gp->rowdot};
-  for (float** v : vecs) A(*v, np);
-  A(gp->sw_prev, np);
-  A(gp->reuse, 4);
-  A(gp->scal, 8);
-  A(gp->grad, (size_t)MAX_THETA);
-  A(gp->status, kStatusWords);
-  A(gp->ready, (size_t)2 * gp->nt * gp->nt);
-  A(gp->counters, 8);
-  A(gp->tflags, 2 * (size_t)gp->nt);
-  A(gp->part, (size_t)ceil_div((int)np, 256) + 8);
-  // lower tile pairs
-  std::vector<int2> tl;
-  for (int I = 0; I < gp->nt; ++I)
-    for (int J = 0; J <= I; ++J) tl.push_back(make_int2(I, J));
-  gp->ntiles_lower = (int)tl.size();
-  A(gp->tiles_lower, tl.size());
-  A(gp->tpart, tl.size() * (size_t)(MAX_D + 1));
-  A(gp->lpart, (size_t)ceil_div((int)np, 256) * (size_t)(MAX_THETA + 2));
-  A(gp->jobs, JOB_COUNT);
-#undef A
-  CU_TRY(cudaMemcpy(gp->tiles_lower, tl.data(), tl.size() * sizeof(int2), cudaMemcpyHostToDevice));
-  CU_TRY(cudaMemset(gp->a, 0, np * sizeof(float)));
-  CU_TRY(cudaMemset(gp->Rv, 0, (size_t)T * gp->ld * sizeof(float)));
-  CU_TRY(cudaMemset(gp->status, 0, kStatusWords * sizeof(int)));
-  CU_TRY(cudaMemset(gp->reuse, 0, 4 * sizeof(int)));
-  // jobs
-  for (int k = 0; k < JOB_COUNT; ++k) {
-    DagJob& j = gp->hjobs[k];
-    std::memset(&j, 0, sizeof(j));
-    j.n = gp->n;
-    j.nt = gp->nt;
-    j.ld = gp->ld;
-    j.L = gp->L;
-    j.Linv = gp->Linv;
-    j.Xf = gp->Xf;
-    j.sw = gp->sw;
-    j.theta = gp->theta;
-    j.sh = gp->sh;
-    j.ready = gp->ready;
-    j.status = gp->status;
-    j.reuse = gp->reuse + 2;
-    j.reuse_mode = 0;
-  }
-  gp->hjobs[JOB_VEC].rhs_kind = RHS_VEC;
-  gp->hjobs[JOB_VEC].nrt = 1;
-  gp->hjobs[JOB_VEC].nrhs = 1;
-  gp->hjobs[JOB_VEC].R = gp->Rv;
-  gp->hjobs[JOB_VEC].rhs_vec = gp->t;
-  gp->hjobs[JOB_VEC].reuse_mode = 2;
-  gp->hjobs[JOB_NONE].rhs_kind = RHS_NONE;
-  gp->hjobs[JOB_NONE].reuse_mode = 1;
-  gp->hjobs[JOB_IDENT].reuse_mode = 1;
-  gp->hjobs[JOB_IDENT].rhs_kind = RHS_IDENT;
-  gp->hjobs[JOB_IDENT].nrt = gp->nt;
-  gp->hjobs[JOB_IDENT].nrhs = gp->n_pad;
-  gp->hjobs[JOB_CROSS].rhs_kind = RHS_CROSS;
-  CU_TRY(cudaMemcpy(gp->jobs, gp->hjobs, sizeof(gp->hjobs), cudaMemcpyHostToDevice));
-  const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
-  for (int k = 0; k < 3; ++k) {
-    std::vector<int4> v = build_tasks(k, gp->nt, kinds[k], gp->hjobs[k].nrt, true);
-    gp->ntasks[k] = (int)v.size();
-    int rr = upload_tasks(v, &gp->tasks[k]);
-    if (rr != PGB_OK) {
-      pgb_gp_destroy(gp);
-      return rr;
-    }
-  }
-  {
-    const char* e = std::getenv("PGB_EAGER");
-    gp->eager = (e && e[0] == '1') ? 1 : 0;
-    const char* t = std::getenv("PGB_TRACE");
-    if (t && t[0] == '1') {
-      size_t mx = 0;
-      for (int k = 0; k < JOB_COUNT; ++k) mx = std::max(mx, (size_t)gp->ntasks[k]);
-      if (dev_alloc(&gp->trace, mx * 8 + (size_t)gp->nt * 16) == PGB_OK) {
-        for (int k = 0; k < JOB_COUNT; ++k) {
-          gp->hjobs[k].trace = gp->trace;
-          gp->hjobs[k].ptrace = gp->trace + mx * 8;
-        }
-        CU_TRY(cudaMemcpy(gp->jobs, gp->hjobs, sizeof(gp->hjobs), cudaMemcpyHostToDevice));
-      }
-    }
-  }
-  CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s, cudaStreamNonBlocking));
-  CU_TRY(cudaStreamCreateWithFlags(&gp->cap_s2, cudaStreamNonBlocking));
   *out = gp;
   return PGB_OK;
 }
 
 int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
-  for (int k = 0; k < OP_COUNT; ++k)
-    if (gp->gexec[k]) cudaGraphExecDestroy(gp->gexec[k]);
-  void* ptrs[] = {gp->trace, gp->Linv, gp->sw_prev, gp->reuse, gp->X_in, gp->y_in, gp->theta, gp->Xf, gp->L, gp->Rv, gp->Rz, gp->Binv, gp->a, gp->f, gp->d1,
-                  gp->W, gp->sw, gp->b, gp->t, gp->x, gp->logp, gp->d3, gp->dsig, gp->svec, gp->rv, gp->zbar,
-                  gp->tz, gp->y2, gp->Ky2, gp->u, gp->c, gp->rowdot, gp->scal, gp->grad, gp->status, gp->ready,
-                  gp->counters, gp->tflags, gp->part, gp->tpart, gp->lpart, gp->tiles_lower, gp->jobs, gp->Rc,
-                  gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c, gp->tasks[0], gp->tasks[1],
-                  gp->tasks[2], gp->tasks[3]};
+  engine_free(gp->e);
+  void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c};
   for (void* p : ptrs)
     if (p) cudaFree(p);
-  if (gp->cap_s) cudaStreamDestroy(gp->cap_s);
-  if (gp->cap_s2) cudaStreamDestroy(gp->cap_s2);
   delete gp;
   return PGB_OK;
 }
@@ -558,12 +741,9 @@ int pgb_gp_destroy(pgb_gp* gp) {
 int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream) {
   if (!gp || !out) return PGB_EINVAL;
   int h[kStatusWords];
-  CU_TRY(cudaMemcpyAsync(h, gp->status, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+  CU_TRY(cudaMemcpyAsync(h, gp->e.status_all, sizeof(h), cudaMemcpyDeviceToHost, (cudaStream_t)stream));
   CU_TRY(cudaStreamSynchronize((cudaStream_t)stream));
-  out->code = h[ST_CODE];
-  out->iterations = h[ST_ITERS];
-  out->notpd_col = h[ST_NOTPD_COL] == INT_MAX ? -1 : h[ST_NOTPD_COL];
-  out->converged = h[ST_CONVERGED];
+  status_from_words(h, out);
   return PGB_OK;
 }
 
@@ -576,8 +756,8 @@ int pgb_gram(const pgb_desc* desc, const float* theta, const float* X1, int32_t 
   float *f1 = nullptr, *f2 = nullptr;
   CU_TRY(cudaMallocAsync(reinterpret_cast<void**>(&f1), sizeof(float) * (size_t)n1 * sh.Dp, s));
   CU_TRY(cudaMallocAsync(reinterpret_cast<void**>(&f2), sizeof(float) * (size_t)n2 * sh.Dp, s));
-  launch_prep_features(sh, X1, theta, f1, n1, n1, s);
-  launch_prep_features(sh, X2, theta, f2, n2, n2, s);
+  launch_prep_features_raw(sh, X1, theta, f1, n1, n1, s);
+  launch_prep_features_raw(sh, X2, theta, f2, n2, n2, s);
   launch_gram_full(sh, theta, f1, n1, f2, n2, K, ldk, s);
   CU_TRY(cudaFreeAsync(f1, s));
   CU_TRY(cudaFreeAsync(f2, s));
@@ -597,11 +777,13 @@ int pgb_log_likelihood(const pgb_desc* desc, const float* theta, const float* f,
 }
 
 int pgb_weight(pgb_gp* gp, const float* X, const void* y, const float* theta, float* a_out, void* stream) {
-  if (!gp || !a_out) return PGB_EINVAL;
+  if (!gp || !a_out || !y) return PGB_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int r = run_op(gp, OP_WEIGHT, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaMemcpyAsync(a_out, gp->a, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_WEIGHT, s));
+  gp->factor_valid = 0;
+  CU_TRY(cudaMemcpyAsync(a_out, e.hp[0].a, sizeof(float) * e.sh[0].n, cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 
@@ -609,14 +791,15 @@ int pgb_precision(pgb_gp* gp, const float* X, const void* y, const float* theta,
                   float* f_out, void* stream) {
   if (!gp || !a || !y) return PGB_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int r = ingest(gp, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaMemsetAsync(gp->a, 0, sizeof(float) * gp->n_pad, s));
-  CU_TRY(cudaMemcpyAsync(gp->a, a, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
-  enq_prep(gp, s);
-  enq_precision(gp, s);
-  if (W_out) CU_TRY(cudaMemcpyAsync(W_out, gp->W, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
-  if (f_out) CU_TRY(cudaMemcpyAsync(f_out, gp->f, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
+  Engine& e = gp->e;
+  const Prob& q = e.hp[0];
+  PGB_TRY(ingest(e, X, y, theta, s));
+  CU_TRY(cudaMemsetAsync(q.a, 0, sizeof(float) * q.n_pad, s));
+  CU_TRY(cudaMemcpyAsync(q.a, a, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
+  launch_prep_features(e.probs, e.vmap, e.nvb, s);
+  enq_precision(e, s);
+  if (W_out) CU_TRY(cudaMemcpyAsync(W_out, q.W, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
+  if (f_out) CU_TRY(cudaMemcpyAsync(f_out, q.f, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
   gp->factor_valid = 0;
   CU_TRY(cudaGetLastError());
   return PGB_OK;
@@ -624,32 +807,38 @@ int pgb_precision(pgb_gp* gp, const float* X, const void* y, const float* theta,
 
 int pgb_approximate_posterior(pgb_gp* gp, const float* X, const void* y, const float* theta, float* a_out,
                               float* W_out, void* stream) {
-  if (!gp || !a_out || !W_out) return PGB_EINVAL;
+  if (!gp || !a_out || !W_out || !y) return PGB_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int r = run_op(gp, OP_POSTERIOR, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaMemcpyAsync(a_out, gp->a, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
-  CU_TRY(cudaMemcpyAsync(W_out, gp->W, sizeof(float) * gp->n, cudaMemcpyDeviceToDevice, s));
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_POSTERIOR, s));
+  gp->factor_valid = 1;
+  CU_TRY(cudaMemcpyAsync(a_out, e.hp[0].a, sizeof(float) * e.sh[0].n, cudaMemcpyDeviceToDevice, s));
+  CU_TRY(cudaMemcpyAsync(W_out, e.hp[0].W, sizeof(float) * e.sh[0].n, cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 
 int pgb_objective(pgb_gp* gp, const float* X, const void* y, const float* theta, float* value_out, void* stream) {
-  if (!gp || !value_out) return PGB_EINVAL;
+  if (!gp || !value_out || !y) return PGB_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int r = run_op(gp, OP_OBJECTIVE, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaMemcpyAsync(value_out, gp->scal + 1, sizeof(float), cudaMemcpyDeviceToDevice, s));
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_OBJECTIVE, s));
+  gp->factor_valid = 1;
+  CU_TRY(cudaMemcpyAsync(value_out, e.value_all, sizeof(float), cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 
 int pgb_value_and_grad(pgb_gp* gp, const float* X, const void* y, const float* theta, float* value_out,
                        float* grad_out, void* stream) {
-  if (!gp || !value_out || !grad_out) return PGB_EINVAL;
+  if (!gp || !value_out || !grad_out || !y) return PGB_EINVAL;
   cudaStream_t s = (cudaStream_t)stream;
-  int r = run_op(gp, OP_VG, X, y, theta, s);
-  if (r != PGB_OK) return r;
-  CU_TRY(cudaMemcpyAsync(value_out, gp->scal + 1, sizeof(float), cudaMemcpyDeviceToDevice, s));
-  CU_TRY(cudaMemcpyAsync(grad_out, gp->grad, sizeof(float) * gp->P, cudaMemcpyDeviceToDevice, s));
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_VG, s));
+  gp->factor_valid = 1;
+  CU_TRY(cudaMemcpyAsync(value_out, e.value_all, sizeof(float), cudaMemcpyDeviceToDevice, s));
+  CU_TRY(cudaMemcpyAsync(grad_out, e.grad_all, sizeof(float) * e.th_total, cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 
@@ -657,8 +846,9 @@ int pgb_factor(pgb_gp* gp, void* stream) {
   if (!gp) return PGB_EINVAL;
   if (!gp->factor_valid) return PGB_ESTATE;
   cudaStream_t s = (cudaStream_t)stream;
-  CU_TRY(cudaMemsetAsync(gp->reuse + 2, 0, sizeof(int), s));   // always a full factorisation
-  enq_dag(gp, JOB_NONE, s);
+  Engine& e = gp->e;
+  CU_TRY(cudaMemsetAsync(e.hp[0].reuse + 2, 0, sizeof(int), s));   // always a full factorisation
+  enq_dag(e, JOB_NONE, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
 }
@@ -670,23 +860,34 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
   if (!reuse_factor && !W) return PGB_EINVAL;
   if (reuse_factor && !gp->factor_valid) return PGB_ESTATE;
   cudaStream_t s = (cudaStream_t)stream;
-  const int nt = gp->nt;
+  Engine& e = gp->e;
+  const Prob& q = e.hp[0];
+  const Shape& sh = q.sh;
+  const int nt = q.nt;
   const int mt = ceil_div(m, T);
   const long long mpad = (long long)mt * T;
   // grow the cross-kernel workspace
   if (mpad > gp->cap_c) {
     CU_TRY(cudaStreamSynchronize(s));
-    float* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in};
-    for (float* p : ptrs)
+    void* old[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c};
+    for (void* p : old)
       if (p) cudaFree(p);
-    if (gp->ready_c) cudaFree(gp->ready_c);
     gp->Rc = gp->rowsq = gp->Xq = gp->Xq_in = nullptr;
     gp->ready_c = nullptr;
-    ALLOC_TRY(gp->Rc, (size_t)mpad * gp->ld);
-    ALLOC_TRY(gp->rowsq, (size_t)mpad * nt);
-    ALLOC_TRY(gp->Xq, (size_t)mpad * gp->sh.Dp);
-    ALLOC_TRY(gp->Xq_in, (size_t)mpad * gp->sh.D);
-    ALLOC_TRY(gp->ready_c, (size_t)(nt + mt) * nt);
+    gp->cap_c = 0;
+    auto grab = [](void** p, size_t bytes) {
+      if (cudaMalloc(p, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        *p = nullptr;
+        return PGB_ENOMEM;
+      }
+      return PGB_OK;
+    };
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->Rc), sizeof(float) * (size_t)mpad * q.ld));
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->rowsq), sizeof(float) * (size_t)mpad * nt));
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq), sizeof(float) * (size_t)mpad * sh.Dp));
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq_in), sizeof(float) * (size_t)mpad * sh.D));
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->ready_c), sizeof(int) * (size_t)(nt + mt) * nt));
     gp->cap_c = mpad;
   }
   if (gp->m_tasks != mt) {
@@ -696,48 +897,112 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
       gp->tasks_c = nullptr;
     }
     std::vector<int4> v = build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false);
-    int r = upload_tasks(v, &gp->tasks_c);
-    if (r != PGB_OK) return r;
-    gp->ntasks[JOB_CROSS] = (int)v.size();
+    if (cudaMalloc(reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)) != cudaSuccess) {
+      cudaGetLastError();
+      gp->tasks_c = nullptr;
+      return PGB_ENOMEM;
+    }
+    PGB_TRY(upload(gp->tasks_c, v));
+    gp->ntasks_c = (int)v.size();
     gp->m_tasks = mt;
   }
-  const Shape& sh = gp->sh;
+  PGB_TRY(ingest(e, X, nullptr, theta, s));
+  launch_prep_features(e.probs, e.vmap, e.nvb, s);
   if (!reuse_factor) {
-    int r = ingest(gp, X, nullptr, theta, s);
-    if (r != PGB_OK) return r;
-    enq_reset_status(gp, s);
-    enq_prep(gp, s);
-    launch_sqrt_w(gp->n, gp->n_pad, W, gp->sw, s);
-    CU_TRY(cudaMemsetAsync(gp->reuse, 0, sizeof(int) * 4, s));   // factor of the caller's W, not reusable
-    enq_dag(gp, JOB_NONE, s);
-    gp->factor_valid = 0;
-  } else {
-    int r = ingest(gp, X, nullptr, theta, s);
-    if (r != PGB_OK) return r;
-    enq_prep(gp, s);
+    launch_reset_problems(e.probs, e.vmap, e.nvb, 0, s);
+    launch_sqrt_w(sh.n, q.n_pad, W, q.sw, s);
+    enq_dag(e, JOB_NONE, s);
+    gp->factor_valid = 0;   // factor of the caller's W, not of the resident posterior
   }
   CU_TRY(cudaMemcpyAsync(gp->Xq_in, Xs, sizeof(float) * (size_t)m * sh.D, cudaMemcpyDeviceToDevice, s));
-  launch_prep_features(sh, gp->Xq_in, gp->theta, gp->Xq, m, (int)mpad, s);
-  if (mean_out)
-    launch_gram_matvec(sh, gp->theta, gp->Xq, m, gp->Xf, gp->n, nullptr, 0, a, nullptr, mean_out, s);
+  launch_prep_features_raw(sh, gp->Xq_in, q.theta, gp->Xq, m, (int)mpad, s);
+  if (mean_out) launch_gram_matvec_raw(sh, q.theta, gp->Xq, m, q.Xf, sh.n, a, mean_out, s);
   if (var_out) {
-    DagJob jb = gp->hjobs[JOB_CROSS];
+    DagJob jb = e.hjobs[JOB_CROSS];
     jb.nrt = mt;
     jb.nrhs = m;
     jb.R = gp->Rc;
     jb.Xq = gp->Xq;
     jb.rowsq = gp->rowsq;
     jb.ready = gp->ready_c;
-    CU_TRY(cudaMemcpyAsync(gp->jobs + JOB_CROSS, &jb, sizeof(DagJob), cudaMemcpyHostToDevice, s));
+    CU_TRY(cudaMemcpyAsync(e.jobs + JOB_CROSS, &jb, sizeof(DagJob), cudaMemcpyHostToDevice, s));
     // L tiles are done: mark them ready; RHS tiles start unready
     CU_TRY(cudaMemsetAsync(gp->ready_c, 1, sizeof(int) * (size_t)nt * nt, s));
     CU_TRY(cudaMemsetAsync(gp->ready_c + (size_t)nt * nt, 0, sizeof(int) * (size_t)mt * nt, s));
-    CU_TRY(cudaMemsetAsync(gp->counters + 2, 0, sizeof(int), s));
-    launch_dag_factor(gp->jobs, gp->tasks_c, gp->ntasks[JOB_CROSS], gp->counters + 2, sh.Dp,
-                      dag_grid(gp, gp->ntasks[JOB_CROSS]), s);
-    launch_predict_var(sh, gp->theta, gp->rowsq, nt, m, var_out, s);
+    CU_TRY(cudaMemsetAsync(e.counters + C_PREDICT, 0, sizeof(int), s));
+    launch_dag_factor(e.jobs, gp->tasks_c, gp->ntasks_c, e.counters + C_PREDICT, e.dag_dm,
+                      dag_grid(e, gp->ntasks_c), s);
+    launch_predict_var(sh, q.theta, gp->rowsq, nt, m, var_out, s);
   }
   CU_TRY(cudaGetLastError());
+  return PGB_OK;
+}
+
+// ---------------------------------------------------------------- batches
+int pgb_batch_create(const pgb_desc* descs, int32_t count, pgb_batch** out) {
+  if (!out) return PGB_EINVAL;
+  *out = nullptr;
+  if (!descs || count < 1) return PGB_EINVAL;
+  for (int p = 0; p < count; ++p) PGB_TRY(validate(descs + p));
+  pgb_batch* b = new pgb_batch();
+  int r = engine_init(b->e, descs, count);
+  if (r != PGB_OK) {
+    pgb_batch_destroy(b);
+    return r;
+  }
+  *out = b;
+  return PGB_OK;
+}
+
+int pgb_batch_destroy(pgb_batch* b) {
+  if (!b) return PGB_OK;
+  engine_free(b->e);
+  delete b;
+  return PGB_OK;
+}
+
+int pgb_batch_layout(const pgb_batch* b, int64_t* x_offsets, int64_t* y_offsets, int64_t* theta_offsets) {
+  if (!b) return PGB_EINVAL;
+  const Engine& e = b->e;
+  for (int p = 0; p <= e.nprob; ++p) {
+    if (x_offsets) x_offsets[p] = (int64_t)(p < e.nprob ? e.x_off[p] : e.x_total);
+    if (y_offsets) y_offsets[p] = (int64_t)(p < e.nprob ? e.y_off[p] : e.y_total);
+    if (theta_offsets) theta_offsets[p] = (int64_t)(p < e.nprob ? e.th_off[p] : e.th_total);
+  }
+  return PGB_OK;
+}
+
+int pgb_batch_objective(pgb_batch* b, const float* X, const void* y, const float* theta, float* values,
+                        void* stream) {
+  if (!b || !y || !values) return PGB_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  Engine& e = b->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_OBJECTIVE, s));
+  CU_TRY(cudaMemcpyAsync(values, e.value_all, sizeof(float) * e.nprob, cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_batch_value_and_grad(pgb_batch* b, const float* X, const void* y, const float* theta, float* values,
+                             float* grads, void* stream) {
+  if (!b || !y || !values || !grads) return PGB_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  Engine& e = b->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_VG, s));
+  CU_TRY(cudaMemcpyAsync(values, e.value_all, sizeof(float) * e.nprob, cudaMemcpyDeviceToDevice, s));
+  CU_TRY(cudaMemcpyAsync(grads, e.grad_all, sizeof(float) * e.th_total, cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_batch_status(pgb_batch* b, pgb_status* out, void* stream) {
+  if (!b || !out) return PGB_EINVAL;
+  const Engine& e = b->e;
+  std::vector<int> h((size_t)e.nprob * kStatusWords);
+  CU_TRY(cudaMemcpyAsync(h.data(), e.status_all, sizeof(int) * h.size(), cudaMemcpyDeviceToHost,
+                         (cudaStream_t)stream));
+  CU_TRY(cudaStreamSynchronize((cudaStream_t)stream));
+  for (int p = 0; p < e.nprob; ++p) status_from_words(h.data() + (size_t)p * kStatusWords, out + p);
   return PGB_OK;
 }
 
@@ -745,15 +1010,21 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
 // one of a handle's intermediate buffers, for the test suite.
 void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
   if (!gp || !name) return nullptr;
-  struct Item { const char* n; void* p; };
-  const Item items[] = {{"a", gp->a}, {"f", gp->f}, {"d1", gp->d1}, {"W", gp->W}, {"sw", gp->sw}, {"d3", gp->d3},
-                        {"dsig", gp->dsig}, {"svec", gp->svec}, {"zbar", gp->zbar}, {"u", gp->u}, {"c", gp->c},
-                        {"rowdot", gp->rowdot}, {"L", gp->L}, {"Linv", gp->Linv}, {"Rz", gp->Rz}, {"Binv", gp->Binv},
-                        {"logp", gp->logp}, {"grad", gp->grad}, {"scal", gp->scal}, {"reuse", gp->reuse},
-                        {"trace", gp->trace}, {"tasks_none", gp->tasks[JOB_NONE]},
-                        {"ptrace", gp->hjobs[JOB_NONE].ptrace}};
+  const Prob& q = gp->e.hp[0];
+  struct Item {
+    const char* n;
+    const void* p;
+  };
+  const Item items[] = {{"a", q.a},         {"f", q.f},         {"d1", q.d1},       {"W", q.W},
+                        {"sw", q.sw},       {"d3", q.d3},       {"dsig", q.dsig},   {"svec", q.svec},
+                        {"zbar", q.zbar},   {"u", q.u},         {"c", q.c},         {"rowdot", q.rowdot},
+                        {"L", q.L},         {"Linv", q.Linv},   {"Rz", q.Rz},       {"Binv", q.Binv},
+                        {"logp", q.logp},   {"grad", q.grad},   {"err", q.err},     {"value", q.value},
+                        {"reuse", q.reuse}, {"trace", gp->e.trace},
+                        {"tasks_none", gp->e.tasks[JOB_NONE]},
+                        {"ptrace", gp->e.hjobs[JOB_NONE].ptrace}};
   for (const Item& it : items)
-    if (std::strcmp(it.n, name) == 0) return it.p;
+    if (std::strcmp(it.n, name) == 0) return const_cast<void*>(it.p);
   return nullptr;
 }
 

@@ -413,16 +413,18 @@ __device__ __forceinline__ void store_chunk(uint8_t* stage, const float4 (&ra)[4
   }
 }
 
-// Thread 0: the 12 MMAs of one 32-wide k-chunk (4 k-steps x 3 products).
+// Thread 0: the 12 MMAs of one 32-wide k-chunk, 4 k-steps x (hi lo, lo hi,
+// hi hi), the small terms first so they are not lost against the large one
+// (a fourth product lo lo changed no measured error).
 __device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, bool first) {
   const uint32_t a_hi = smem_u32(stage), a_lo = a_hi + CHUNK_BYTES;
   const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {
     const uint32_t o = ks * 32;
-    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
-    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, 1u);
+    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
     umma_tf32(tc.tmem, sdesc_sw128(a_lo + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
   }
 }
 
@@ -630,17 +632,18 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
     }
-    if (is_rhs && jb.rhs_kind == RHS_CROSS && threadIdx.x < T) {
-      const int r = threadIdx.x;
-      const int gi = ri * T + r;
-      if (gi < jb.nrhs) {
-        float s = 0.0f;
-        for (int c = 0; c < T; ++c) {
-          const float x = sC[r * SC_LD + c];
-          s = fmaf(x, x, s);
-        }
-        jb.rowsq[(size_t)gi * nt + j] = s;
+  }
+  if (is_rhs && jb.rhs_kind == RHS_CROSS && threadIdx.x < T) {
+    // predictive variance terms: squared norm of this tile's part of each row
+    const int r = threadIdx.x;
+    const int gi = ri * T + r;
+    if (gi < jb.nrhs) {
+      float s = 0.0f;
+      for (int c = 0; c < T; ++c) {
+        const float x = sC[r * SC_LD + c];
+        s = fmaf(x, x, s);
       }
+      jb.rowsq[(size_t)gi * nt + j] = s;
     }
   }
   __syncthreads();
@@ -696,6 +699,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     if (t >= ntasks) break;
     const int4 tk = tasks[t];
     const DagJob jb = jobs[tk.x];
+    if (jb.active && __ldcg(jb.active) == 0) continue;           // problem has stopped
     if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
     dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
   }
@@ -746,9 +750,8 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const flo
   if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
 }
 
-__global__ void syrk_zzt_kernel(const float* __restrict__ Z, long long ldz, int nt, const int2* __restrict__ tiles,
-                                int ntiles, float* __restrict__ Binv, long long ldb, int* __restrict__ counter,
-                                int* __restrict__ status);
+__global__ void syrk_zzt_kernel(const Prob* __restrict__ probs, const int4* __restrict__ tiles, int ntiles,
+                                int* __restrict__ counter);
 
 void dag_set_attributes() {
   cudaFuncSetAttribute(tc_tile_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
@@ -758,11 +761,12 @@ void dag_set_attributes() {
   cudaFuncSetAttribute(dag_factor_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
 }
 
-void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int Dp, int grid,
+void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int DM, int grid,
                        cudaStream_t st) {
-  if (Dp <= 4)
+  if (ntasks <= 0) return;
+  if (DM <= 4)
     dag_factor_kernel<4><<<grid, DAG_THREADS, DAG_SMEM, st>>>(jobs_dev, tasks, ntasks, counter);
-  else if (Dp <= 8)
+  else if (DM <= 8)
     dag_factor_kernel<8><<<grid, DAG_THREADS, DAG_SMEM, st>>>(jobs_dev, tasks, ntasks, counter);
   else
     dag_factor_kernel<16><<<grid, DAG_THREADS, DAG_SMEM, st>>>(jobs_dev, tasks, ntasks, counter);
@@ -772,12 +776,12 @@ void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, in
 // Z = L^-T (upper, stored in the RHS rows of an RHS_IDENT factorisation).
 // Tile (I, J), I >= J: sum over k >= I of Z_Ik Z_Jk^T on the tensor cores;
 // written to (I, J) and, transposed through shared memory, to (J, I), so
-// B^-1 is stored full.  Persistent blocks take tiles in list order (longest
-// k-range first) through an atomic counter.
-__global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const float* __restrict__ Z, long long ldz, int nt,
-                                                                  const int2* __restrict__ tiles, int ntiles,
-                                                                  float* __restrict__ Binv, long long ldb,
-                                                                  int* __restrict__ counter, int* __restrict__ status) {
+// B^-1 is stored full.  tiles: (problem, I, J, -) of every problem, longest
+// k-range first; persistent blocks take them in list order through an
+// atomic counter.
+__global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __restrict__ probs,
+                                                                  const int4* __restrict__ tiles, int ntiles,
+                                                                  int* __restrict__ counter) {
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
   __shared__ int s_ok[4];
@@ -809,23 +813,29 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const float* _
     __syncthreads();
     if (threadIdx.x == 0) {
       int t = atomicAdd(counter, 1);
-      if (t < ntiles && ld_relaxed(status + ST_ABORT)) t = ntiles;
+      // an aborted problem's tiles are skipped (uniformly for the block)
+      if (t < ntiles && ld_relaxed(probs[tiles[t].x].status + ST_ABORT)) t = -1;
       s_task = t;
     }
     __syncthreads();
     const int t = s_task;
     if (t >= ntiles) break;
-    const int2 tl = tiles[t];
-    const int I = tl.x, J = tl.y;
+    if (t < 0) continue;
+    const int4 tl = tiles[t];
+    const Prob& P = probs[tl.x];
+    const int I = tl.y, J = tl.z;
+    const long long ld = P.ld;
+    const float* Z = P.Rz;
+    float* Binv = P.Binv;
     auto always = [](int) { return true; };
-    if (!tc_accumulate(Z + (size_t)I * T * ldz, ldz, Z + (size_t)J * T * ldz, ldz, I, nt, tc, s_ok, status, always))
-      break;
+    if (!tc_accumulate(Z + (size_t)I * T * ld, ld, Z + (size_t)J * T * ld, ld, I, P.nt, tc, s_ok, P.status, always))
+      break;   // the MMA pipeline timed out: this block stops
     tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      Binv[(size_t)(I * T + r) * ldb + J * T + c] = sC[r * SC_LD + c];
-      if (I != J) Binv[(size_t)(J * T + r) * ldb + I * T + c] = sC[c * SC_LD + r];
+      Binv[(size_t)(I * T + r) * ld + J * T + c] = sC[r * SC_LD + c];
+      if (I != J) Binv[(size_t)(J * T + r) * ld + I * T + c] = sC[c * SC_LD + r];
     }
   }
   tc_fence_before();
@@ -833,9 +843,9 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const float* _
   if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
 }
 
-void launch_syrk_zzt(const float* Z, long long ldz, int nt, const int2* tiles, int ntiles, float* Binv, long long ldb,
-                     int* counter, int* status, int grid, cudaStream_t st) {
-  syrk_zzt_kernel<<<grid, DAG_THREADS, DAG_SMEM, st>>>(Z, ldz, nt, tiles, ntiles, Binv, ldb, counter, status);
+void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* counter, int grid, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  syrk_zzt_kernel<<<grid, DAG_THREADS, DAG_SMEM, st>>>(probs, tiles, ntiles, counter);
 }
 
 }  // namespace pgb

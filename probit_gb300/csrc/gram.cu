@@ -4,6 +4,10 @@
 //
 // Kernel algebra restated from mlkernels as used by the reference
 // (Laplace.py:7,21,24; approximators.py:172-174,192-194,272).
+//
+// The batched kernels take a device table of problems and a map from thread
+// block to (problem, local block), so one launch covers every problem of a
+// batch whatever their sizes.
 #include "kernels.cuh"
 
 namespace pgb {
@@ -11,10 +15,8 @@ namespace pgb {
 // ---------------------------------------------------------------- features
 // eq / matern12: x_d / l_d (mlkernels' stretch divides the inputs);
 // eq_periodic: the raw inputs (the lengthscale is applied after the sine).
-__global__ void prep_features_kernel(Shape sh, const float* __restrict__ X, const float* __restrict__ theta,
-                                     float* __restrict__ Xf, int n, int n_pad) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n_pad) return;
+__device__ __forceinline__ void prep_point(const Shape& sh, const float* __restrict__ X,
+                                           const float* __restrict__ theta, float* __restrict__ Xf, int n, int i) {
   for (int d = 0; d < sh.Dp; ++d) {
     float v = 0.0f;
     if (i < n && d < sh.D) {
@@ -25,9 +27,28 @@ __global__ void prep_features_kernel(Shape sh, const float* __restrict__ X, cons
   }
 }
 
-void launch_prep_features(const Shape& sh, const float* X, const float* theta, float* Xf, int n, int n_pad,
-                          cudaStream_t st) {
-  prep_features_kernel<<<ceil_div(n_pad, 256), 256, 0, st>>>(sh, X, theta, Xf, n, n_pad);
+__global__ void prep_features_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  prep_point(P.sh, P.X, P.theta, P.Xf, P.sh.n, i);
+}
+
+void launch_prep_features(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) prep_features_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+__global__ void prep_features_raw_kernel(Shape sh, const float* __restrict__ X, const float* __restrict__ theta,
+                                         float* __restrict__ Xf, int n, int n_pad) {
+  const int i = blockIdx.x * VT + threadIdx.x;
+  if (i >= n_pad) return;
+  prep_point(sh, X, theta, Xf, n, i);
+}
+
+void launch_prep_features_raw(const Shape& sh, const float* X, const float* theta, float* Xf, int n, int n_pad,
+                              cudaStream_t st) {
+  if (n_pad > 0) prep_features_raw_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, X, theta, Xf, n, n_pad);
 }
 
 // Summed scaled squared distance with the feature loop unrolled to DM.
@@ -81,7 +102,7 @@ void launch_gram_full(const Shape& sh, const float* theta, const float* X1f, int
 
 // ---------------------------------------------------------------- Gram matvec
 // y[r] = row_scale[r] * sum_c K(xr_r, xc_c) * (M ? M[r, c] : 1) * v[c]
-// One block owns MV_ROWS rows and sweeps all columns; the per-row sums are
+// One block owns 128 / DM rows and sweeps all columns; the per-row sums are
 // reduced in a fixed order, so results are bitwise reproducible.  The kernel
 // family is a template parameter and every per-entry quantity lives in
 // registers or shared memory.
@@ -99,11 +120,10 @@ __device__ __forceinline__ float kval(const float* xi, const float* xj, int D, f
   for (int d = 0; d < DM; ++d) {
     if (d < D) {
       float q;
-      if (KIND == PGB_KERNEL_EQ_PERIODIC) {
+      if (KIND == PGB_KERNEL_EQ_PERIODIC)
         q = (2.0f * sinpif((xi[d] - xj[d]) * inv_p)) / sl[d];
-      } else {
+      else
         q = xi[d] - xj[d];
-      }
       d2 += q * q;
     }
   }
@@ -112,10 +132,10 @@ __device__ __forceinline__ float kval(const float* xi, const float* xj, int D, f
 }
 
 template <int KIND, int DM, bool HAS_M>
-__global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(
-    Shape sh, const float* __restrict__ theta, const float* __restrict__ Xr, int nr, const float* __restrict__ Xc,
-    int nc, const float* __restrict__ M, long long ldm, const float* __restrict__ v,
-    const float* __restrict__ row_scale, float* __restrict__ y) {
+__device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict__ theta,
+                                        const float* __restrict__ Xr, int nr, const float* __restrict__ Xc, int nc,
+                                        const float* __restrict__ M, long long ldm, const float* __restrict__ v,
+                                        const float* __restrict__ row_scale, float* __restrict__ y, int r0) {
   constexpr int MV_ROWS = mv_rows<DM>();
   __shared__ float sx[MV_ROWS][DM];
   __shared__ float sred[MV_THREADS / 32][MV_ROWS];
@@ -124,7 +144,6 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(
   const float sv = __ldg(theta + sh.nl);
   const float inv_p = sh.inv_p;
   if (threadIdx.x < MAX_D) sl[threadIdx.x] = threadIdx.x < D ? __ldg(theta + (sh.nl == 1 ? 0 : threadIdx.x)) : 1.0f;
-  const int r0 = blockIdx.x * MV_ROWS;
   for (int e = threadIdx.x; e < MV_ROWS * DM; e += MV_THREADS) {
     const int r = e / DM, d = e % DM;
     sx[r][d] = (r0 + r < nr && d < Dp) ? Xr[(size_t)(r0 + r) * Dp + d] : 0.0f;
@@ -173,52 +192,121 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(
   }
 }
 
+__device__ __forceinline__ float* prob_field(const Prob& P, int f) {
+  switch (f) {
+    case F_A: return P.a;
+    case F_F: return P.f;
+    case F_D1: return P.d1;
+    case F_W: return P.W;
+    case F_SW: return P.sw;
+    case F_R: return P.r;
+    case F_T: return P.t;
+    case F_X: return P.x;
+    case F_LOGP: return P.logp;
+    case F_D3: return P.d3;
+    case F_DSIG: return P.dsig;
+    case F_SVEC: return P.svec;
+    case F_RV: return P.rv;
+    case F_ZBAR: return P.zbar;
+    case F_TZ: return P.tz;
+    case F_Y2: return P.y2;
+    case F_U: return P.u;
+    case F_C: return P.c;
+    case F_ROWDOT: return P.rowdot;
+    default: return nullptr;
+  }
+}
+
+template <int KIND, int DM, bool HAS_M>
+__global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(const Prob* __restrict__ probs,
+                                                                 const int2* __restrict__ mvmap, MatvecOp op) {
+  const int2 m = mvmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (op.only_active && *P.active == 0) return;
+  const int n = P.sh.n;
+  mv_core<KIND, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
+                           prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>());
+}
+
 template <int KIND, int DM>
-static void mv_dispatch_m(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
-                          const float* M, long long ldm, const float* v, const float* row_scale, float* y,
-                          cudaStream_t st) {
-  const int grid = ceil_div(nr, mv_rows<DM>());
-  if (M)
-    gram_matvec_kernel<KIND, DM, true><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y);
+__global__ void __launch_bounds__(MV_THREADS) gram_matvec_raw_kernel(Shape sh, const float* __restrict__ theta,
+                                                                     const float* __restrict__ Xr, int nr,
+                                                                     const float* __restrict__ Xc, int nc,
+                                                                     const float* __restrict__ v,
+                                                                     float* __restrict__ y) {
+  mv_core<KIND, DM, false>(sh, theta, Xr, nr, Xc, nc, nullptr, 0, v, nullptr, y, blockIdx.x * mv_rows<DM>());
+}
+
+template <int KIND, int DM>
+static void mv_launch(const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
+  if (op.use_binv)
+    gram_matvec_kernel<KIND, DM, true><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
   else
-    gram_matvec_kernel<KIND, DM, false><<<grid, MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y);
+    gram_matvec_kernel<KIND, DM, false><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
 }
 
 template <int KIND>
-static void mv_dispatch_d(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
-                          const float* M, long long ldm, const float* v, const float* row_scale, float* y,
-                          cudaStream_t st) {
-  if (sh.Dp <= 4)
-    mv_dispatch_m<KIND, 4>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
-  else if (sh.Dp <= 8)
-    mv_dispatch_m<KIND, 8>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+static void mv_launch_d(int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
+  if (DM <= 4)
+    mv_launch<KIND, 4>(probs, mvmap, nblocks, op, st);
+  else if (DM <= 8)
+    mv_launch<KIND, 8>(probs, mvmap, nblocks, op, st);
   else
-    mv_dispatch_m<KIND, 16>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+    mv_launch<KIND, 16>(probs, mvmap, nblocks, op, st);
 }
 
-void launch_gram_matvec(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
-                        const float* M, long long ldm, const float* v, const float* row_scale, float* y,
+void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
                         cudaStream_t st) {
-  if (sh.kind == PGB_KERNEL_MATERN12)
-    mv_dispatch_d<PGB_KERNEL_MATERN12>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
-  else if (sh.kind == PGB_KERNEL_EQ_PERIODIC)
-    mv_dispatch_d<PGB_KERNEL_EQ_PERIODIC>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+  if (nblocks <= 0) return;
+  if (kind == PGB_KERNEL_MATERN12)
+    mv_launch_d<PGB_KERNEL_MATERN12>(DM, probs, mvmap, nblocks, op, st);
+  else if (kind == PGB_KERNEL_EQ_PERIODIC)
+    mv_launch_d<PGB_KERNEL_EQ_PERIODIC>(DM, probs, mvmap, nblocks, op, st);
   else
-    mv_dispatch_d<PGB_KERNEL_EQ>(sh, theta, Xr, nr, Xc, nc, M, ldm, v, row_scale, y, st);
+    mv_launch_d<PGB_KERNEL_EQ>(DM, probs, mvmap, nblocks, op, st);
 }
 
-// ---------------------------------------------------------------- dense matvec
-// y[r] = row_scale[r] * sum_c A[r, c] v[c]   (A row-major, lda)
-__global__ void __launch_bounds__(256) dense_matvec_kernel(const float* __restrict__ A, long long lda, int nr, int nc,
-                                                           const float* __restrict__ v, const float* __restrict__ row_scale,
-                                                           float* __restrict__ y) {
+template <int KIND>
+static void mv_raw_d(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
+                     const float* v, float* y, cudaStream_t st) {
+  if (sh.Dp <= 4)
+    gram_matvec_raw_kernel<KIND, 4>
+        <<<ceil_div(nr, mv_rows<4>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
+  else if (sh.Dp <= 8)
+    gram_matvec_raw_kernel<KIND, 8>
+        <<<ceil_div(nr, mv_rows<8>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
+  else
+    gram_matvec_raw_kernel<KIND, 16>
+        <<<ceil_div(nr, mv_rows<16>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
+}
+
+void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
+                            const float* v, float* y, cudaStream_t st) {
+  if (nr <= 0) return;
+  if (sh.kind == PGB_KERNEL_MATERN12)
+    mv_raw_d<PGB_KERNEL_MATERN12>(sh, theta, Xr, nr, Xc, nc, v, y, st);
+  else if (sh.kind == PGB_KERNEL_EQ_PERIODIC)
+    mv_raw_d<PGB_KERNEL_EQ_PERIODIC>(sh, theta, Xr, nr, Xc, nc, v, y, st);
+  else
+    mv_raw_d<PGB_KERNEL_EQ>(sh, theta, Xr, nr, Xc, nc, v, y, st);
+}
+
+// ---------------------------------------------------------------- B^-1 matvec
+// y2[r] = sum_c B^-1[r, c] tz[c]: one warp per row, 8 rows per block
+// (bmap: block -> (problem, row block)).
+__global__ void __launch_bounds__(256) binv_matvec_kernel(const Prob* __restrict__ probs,
+                                                          const int2* __restrict__ bmap) {
+  const int2 m = bmap[blockIdx.x];
+  const Prob& P = probs[m.x];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int r = blockIdx.x * 8 + warp;
-  if (r >= nr) return;
-  const float* a = A + (size_t)r * lda;
+  const int r = m.y * 8 + warp;
+  const int n = P.sh.n;
+  if (r >= n) return;
+  const float* a = P.Binv + (size_t)r * P.ld;
+  const float* v = P.tz;
   float s = 0.0f;
-  for (int c = lane * 4; c < nc; c += 128) {
-    if (c + 3 < nc) {
+  for (int c = lane * 4; c < n; c += 128) {
+    if (c + 3 < n) {
       const float4 x = __ldg(reinterpret_cast<const float4*>(a + c));
       const float4 w = __ldg(reinterpret_cast<const float4*>(v + c));
       s = fmaf(x.x, w.x, s);
@@ -226,16 +314,15 @@ __global__ void __launch_bounds__(256) dense_matvec_kernel(const float* __restri
       s = fmaf(x.z, w.z, s);
       s = fmaf(x.w, w.w, s);
     } else {
-      for (int e = c; e < nc; ++e) s = fmaf(a[e], v[e], s);
+      for (int e = c; e < n; ++e) s = fmaf(a[e], v[e], s);
     }
   }
   s = warp_sum(s);
-  if (lane == 0) y[r] = row_scale ? s * row_scale[r] : s;
+  if (lane == 0) P.y2[r] = s;
 }
 
-void launch_dense_matvec(const float* A, long long lda, int nr, int nc, const float* v, const float* row_scale,
-                         float* y, cudaStream_t st) {
-  dense_matvec_kernel<<<ceil_div(nr, 8), 256, 0, st>>>(A, lda, nr, nc, v, row_scale, y);
+void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) binv_matvec_kernel<<<nblocks, 256, 0, st>>>(probs, bmap);
 }
 
 // ---------------------------------------------------------------- gradient trace
@@ -244,18 +331,24 @@ void launch_dense_matvec(const float* A, long long lda, int nr, int nc, const fl
 // folded to the lower triangle: off-diagonal pairs carry R_ij + c_i a_j +
 // c_j a_i, the diagonal 1/2 R_ii + c_i a_i (only dK/ds is nonzero there).
 // dK/dl_d = K q_d / l_d (Matern12: times 1/r, 0 at r = 0), dK/ds = K / s.
-// Each block writes its partial sums (double) to part[block * P + k].
+// tiles: (problem, I, J, ordinal of the tile within its problem); each block
+// writes its partial sums (double) to tpart[ordinal * (nl + 1) + k].
 template <int DM>
-__global__ void __launch_bounds__(256) grad_trace_kernel(Shape sh, const float* __restrict__ theta,
-                                                         const float* __restrict__ Xf, const float* __restrict__ Binv,
-                                                         long long ld, const float* __restrict__ sw,
-                                                         const float* __restrict__ cvec, const float* __restrict__ avec,
-                                                         const int2* __restrict__ tiles, double* __restrict__ part) {
-  const KernelParams kp = make_kp(sh, theta);
-  const int P = sh.nl + 1;
-  const int2 tl = tiles[blockIdx.x];
-  const int I = tl.x, J = tl.y;
+__global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict__ probs,
+                                                         const int4* __restrict__ tiles) {
+  const int4 tl = tiles[blockIdx.x];
+  const Prob& P = probs[tl.x];
+  const int I = tl.y, J = tl.z, ord = tl.w;
+  const Shape sh = P.sh;
+  const KernelParams kp = make_kp(sh, P.theta);
+  const int NP = sh.nl + 1;
   const int n = sh.n;
+  const float* __restrict__ Xf = P.Xf;
+  const float* __restrict__ Binv = P.Binv;
+  const long long ld = P.ld;
+  const float* __restrict__ sw = P.sw;
+  const float* __restrict__ cvec = P.c;
+  const float* __restrict__ avec = P.a;
   __shared__ float sxc[T][DM];
   __shared__ float ssw[T], sc[T], sa[T];
   __shared__ double sred[8][MAX_D + 1];
@@ -291,7 +384,6 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(Shape sh, const float* 
       m = 0.5f * swr * bij * swr + cr * ar;
     else
       m = swr * bij * ssw[c] + cr * sa[c] + sc[c] * ar;
-    // distances
     float q[DM];
     float d2 = 0.0f;
 #pragma unroll
@@ -299,11 +391,10 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(Shape sh, const float* 
       q[d] = 0.0f;
       if (d < sh.D) {
         float v;
-        if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
+        if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
           v = (2.0f * sinpif((xr[d] - sxc[c][d]) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
-        } else {
+        else
           v = xr[d] - sxc[c][d];
-        }
         q[d] = v * v;
         d2 += q[d];
       }
@@ -323,33 +414,31 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(Shape sh, const float* 
     }
     acc_s += K * m / kp.s;
   }
-  // block reduction of P partials
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
   for (int k = 0; k < DM + 1; ++k) {
-    if (k < P) {
-      const float v = (k == P - 1) ? acc_s : acc[k < DM ? k : 0];
+    if (k < NP) {
+      const float v = (k == NP - 1) ? acc_s : acc[k < DM ? k : 0];
       const double s = warp_sum_d((double)v);
       if (lane == 0) sred[warp][k] = s;
     }
   }
   __syncthreads();
-  if (threadIdx.x < P) {
+  if (threadIdx.x < NP) {
     double s = 0.0;
     for (int w = 0; w < 8; ++w) s += sred[w][threadIdx.x];
-    part[(size_t)blockIdx.x * P + threadIdx.x] = s;
+    P.tpart[(size_t)ord * NP + threadIdx.x] = s;
   }
 }
 
-void launch_grad_trace(const Shape& sh, const float* theta, const float* Xf, const float* Binv, long long ld,
-                       const float* sw, const float* c, const float* a, const int2* tiles, int ntiles, double* part,
-                       cudaStream_t st) {
-  if (sh.Dp <= 4)
-    grad_trace_kernel<4><<<ntiles, 256, 0, st>>>(sh, theta, Xf, Binv, ld, sw, c, a, tiles, part);
-  else if (sh.Dp <= 8)
-    grad_trace_kernel<8><<<ntiles, 256, 0, st>>>(sh, theta, Xf, Binv, ld, sw, c, a, tiles, part);
+void launch_grad_trace(int DM, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st) {
+  if (ntiles <= 0) return;
+  if (DM <= 4)
+    grad_trace_kernel<4><<<ntiles, 256, 0, st>>>(probs, tiles);
+  else if (DM <= 8)
+    grad_trace_kernel<8><<<ntiles, 256, 0, st>>>(probs, tiles);
   else
-    grad_trace_kernel<16><<<ntiles, 256, 0, st>>>(sh, theta, Xf, Binv, ld, sw, c, a, tiles, part);
+    grad_trace_kernel<16><<<ntiles, 256, 0, st>>>(probs, tiles);
 }
 
 }  // namespace pgb

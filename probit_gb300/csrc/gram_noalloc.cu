@@ -91,8 +91,8 @@ extern "C" int pgb_gram_noalloc(const pgb_desc* desc, const float* theta, const 
   float* f1 = scratch;
   float* f2 = scratch + (size_t)n1 * sh.Dp;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  pgb::launch_prep_features(sh, X1, theta, f1, n1, n1, s);
-  pgb::launch_prep_features(sh, X2, theta, f2, n2, n2, s);
+  pgb::launch_prep_features_raw(sh, X1, theta, f1, n1, n1, s);
+  pgb::launch_prep_features_raw(sh, X2, theta, f2, n2, n2, s);
   pgb::launch_gram_full(sh, theta, f1, n1, f2, n2, K, ldk, s);
   return cudaGetLastError() == cudaSuccess ? PGB_OK : PGB_ECUDA;
 }

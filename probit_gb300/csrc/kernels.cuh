@@ -1,5 +1,9 @@
-// Launch wrappers of the device kernels (one translation unit each) used by
-// the host orchestration in api.cu.
+// Device-side problem table and launch wrappers of the kernels (one
+// translation unit each) used by the host orchestration in api.cu.
+//
+// Every kernel works on a batch: a device array of Prob records (one per GP
+// problem, each with its own shape and buffers) and a map from thread block
+// to (problem, local block).  A single GP is a batch of one.
 #pragma once
 
 #include "common.cuh"
@@ -7,6 +11,39 @@
 namespace pgb {
 
 enum RhsKind { RHS_NONE = 0, RHS_VEC = 1, RHS_IDENT = 2, RHS_CROSS = 3 };
+
+constexpr int VT = 256;   // points per block of the per-point kernels
+
+// One GP problem: shape, Newton settings and every device buffer it uses.
+struct Prob {
+  Shape sh;
+  int nt;             // tiles per dimension (ceil(n / T))
+  int n_pad;          // nt * T
+  long long ld;       // floats per row of L, Rz, Binv
+  float tol;          // Newton stop: ||a_k - a_{k-1}||_2 <= tol
+  int maxiter;
+  const float* X;     // inputs (n x D), y (n), theta
+  const void* y;
+  const float* theta;
+  float* Xf;          // features (n_pad x Dp)
+  float* L;           // factor of B (n_pad x ld), lower tiles
+  float* Linv;        // inverses of the diagonal tiles (nt x T x T)
+  float* Rv;          // Newton RHS row tile (T x ld)
+  float* Rz;          // L^-T (n_pad x ld), gradient only
+  float* Binv;        // B^-1 (n_pad x ld), gradient only
+  // vectors (n_pad each)
+  float *a, *f, *d1, *W, *sw, *r, *t, *x, *logp, *d3, *dsig, *svec, *rv, *zbar, *tz, *y2, *u, *c, *rowdot, *sw_prev;
+  float* err;         // last ||a_k - a_{k-1}||_2
+  float* value;       // negative log evidence
+  float* grad;        // theta-sized gradient
+  int* status;        // 8 status words
+  int* active;        // 1 while the Newton loop of this problem runs
+  int* reuse;         // [0] factor valid, [1] W differs, [2] reuse decision
+  double* part;       // per-block partial sums (ceil(n_pad / VT))
+  double* tpart;      // per-tile trace partials (lower tiles x (MAX_D + 1))
+  double* lpart;      // per-block likelihood partials (ceil(n / VT) x (MAX_THETA + 2))
+  int* tflags;        // 2 nt flags of the two wavefront solves
+};
 
 // One factorisation job of the tile-DAG kernel (dag.cu).
 struct DagJob {
@@ -30,10 +67,11 @@ struct DagJob {
   int* status;
   // factor reuse: when *reuse is 1 the resident L is already the factor of
   // this B (bitwise equal W, same theta).  reuse_mode 1: skip the L tiles and
-  // solve only the RHS rows; 2: skip the whole launch (the caller solves the
+  // solve only the RHS rows; 2: skip the whole job (the caller solves the
   // RHS with the triangular solve instead).
   const int* reuse;
   int reuse_mode;
+  const int* active;     // when non-null and 0 the job is skipped (converged problem)
   // optional per-task timestamps (globaltimer ns): [task][8] = start, k-loop
   // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
   // C assembled (after the accumulator is applied)
@@ -41,58 +79,82 @@ struct DagJob {
   unsigned long long* ptrace;   // optional: [nt][16] phase times of the diagonal factorisations
 };
 
-// gram.cu
-void launch_prep_features(const Shape& sh, const float* X, const float* theta, float* Xf, int n, int n_pad,
-                          cudaStream_t st);
+// gram.cu ---------------------------------------------------------------------
+// Features of every problem in the map (vmap: block -> (problem, block)).
+void launch_prep_features(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+// Features of one point set (stand-alone use).
+void launch_prep_features_raw(const Shape& sh, const float* X, const float* theta, float* Xf, int n, int n_pad,
+                              cudaStream_t st);
 void launch_gram_full(const Shape& sh, const float* theta, const float* X1f, int n1, const float* X2f, int n2,
                       float* K, long long ldk, cudaStream_t st);
-void launch_gram_matvec(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
-                        const float* M, long long ldm, const float* v, const float* row_scale, float* y,
-                        cudaStream_t st);
-void launch_dense_matvec(const float* A, long long lda, int nr, int nc, const float* v, const float* row_scale,
-                         float* y, cudaStream_t st);
-void launch_grad_trace(const Shape& sh, const float* theta, const float* Xf, const float* Binv, long long ld,
-                       const float* sw, const float* c, const float* a, const int2* tiles, int ntiles, double* part,
-                       cudaStream_t st);
 
-// vec.cu
+// Vector operands of the batched Gram matvec, named by Prob field.
+enum VecField {
+  F_A, F_F, F_D1, F_W, F_SW, F_R, F_T, F_X, F_LOGP, F_D3, F_DSIG, F_SVEC, F_RV, F_ZBAR, F_TZ, F_Y2, F_U, F_C,
+  F_ROWDOT, F_NONE
+};
+struct MatvecOp {
+  int v;            // VecField of the vector
+  int row_scale;    // VecField or F_NONE
+  int y;            // VecField of the output
+  int use_binv;     // multiply K by B^-1 elementwise
+  int only_active;  // skip problems whose Newton loop has stopped
+};
+// y = row_scale * ((K [o B^-1]) v) for every problem of one (kind, DM)
+// group; mvmap: block -> (problem, row block of 128 / DM rows).
+void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
+                        cudaStream_t st);
+// Stand-alone Gram matvec over explicit pointers (predict mean).
+void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
+                            const float* v, float* y, cudaStream_t st);
+// y2 = B^-1 tz, 8 rows per block: bmap block -> (problem, row block)
+void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaStream_t st);
+// trace partials over the lower tiles (problem, I, J, -) of one DM group
+void launch_grad_trace(int DM, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st);
+
+// vec.cu ----------------------------------------------------------------------
 void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const void* y, int n, float* logp,
                      float* d1, float* d2, float* d3, cudaStream_t st);
-void launch_newton_lik(const Shape& sh, const float* theta, const float* f, const void* y, const float* a,
-                       int n_pad, float* d1, float* W, float* sw, float* r, float* rhs, cudaStream_t st);
-void launch_newton_update(int n, const float* sw, const float* x, float* a, double* part, cudaStream_t st);
-void launch_newton_finalize(const double* part, int nparts, float tol, int maxiter, int* status, float* err_out,
-                            cudaGraphConditionalHandle cond, int use_cond, cudaStream_t st);
-void launch_lik_full(const Shape& sh, const float* theta, const float* f, const void* y, int n_pad, float* logp,
-                     float* d1, float* d3, float* W, float* sw, cudaStream_t st);
-void launch_evidence(int n, const float* logp, const float* f, const float* a, const float* L, long long ld,
-                     double* part, float* value, cudaStream_t st);
-void launch_grad_vec1(int n, int n_pad, const float* rowdot, const float* sw, const float* d3, const float* a,
-                      const float* d1, float* dsig, float* svec, float* r, cudaStream_t st);
-void launch_scale_vec(int n, int n_pad, const float* sw, const float* in, float* out, cudaStream_t st);
-void launch_grad_vec3(int n, int n_pad, const float* y1, const float* sw, const float* a, const float* d1,
-                      const float* svec, const float* W, float* u, float* c, cudaStream_t st);
-void launch_grad_lik_final(const Shape& sh, const float* theta, const float* f, const void* y, const float* dsig,
-                           const float* u, const double* tpart, int ntp, double* lpart, float* grad,
-                           cudaStream_t st);
+void launch_newton_lik(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_newton_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+// per-problem stopping rule; any_active[0] collects whether a problem goes
+// on, then becomes the graph condition (use_cond) and is copied to
+// any_active[1] for a host-driven loop
+void launch_newton_finalize(const Prob* probs, int nprob, int* any_active, cudaGraphConditionalHandle cond,
+                            int use_cond, cudaStream_t st);
+void launch_lik_full(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
+void launch_grad_vec1(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_scale_tz(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_grad_vec3(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+// likelihood-parameter partials (vmap blocks) and the final theta gradient
+// of every problem
+void launch_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_predict_var(const Shape& sh, const float* theta, const float* rowsq, int nt, int m, float* var,
                         cudaStream_t st);
 void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st);
-// factor reuse: flags[0] = factor valid, flags[1] = W differs, flags[2] = reuse
-void launch_reuse_check(int n, const float* sw, float* sw_prev, int* flags, cudaStream_t st);
-void launch_reuse_mark_valid(int* flags, const int* status, cudaStream_t st);
+// factor reuse per active problem: differs |= any(sw != sw_prev); decide
+void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
+void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st);
+// status words, reuse flags, active = 1 and (zero_a) a = 0
+void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int zero_a, cudaStream_t st);
+// active = v for every problem
+void launch_set_active(const Prob* probs, int nprob, int v, cudaStream_t st);
 
-// dag.cu
+// dag.cu ----------------------------------------------------------------------
 void dag_set_attributes();
-void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int Dp, int grid,
+// DM: feature loop bound (4, 8 or 16), at least every job's Dp
+void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int DM, int grid,
                        cudaStream_t st);
-void launch_syrk_zzt(const float* Z, long long ldz, int nt, const int2* tiles, int ntiles, float* Binv, long long ldb,
-                     int* counter, int* status, int grid, cudaStream_t st);
+// B^-1 = Z Z^T over the merged lower-tile list (tiles: problem, I, J, -)
+void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* counter, int grid, cudaStream_t st);
 
-// trsv.cu
+// trsv.cu ---------------------------------------------------------------------
 void trsv_set_attributes();
-// run_if: when non-null the launch does nothing unless *run_if == run_when
-void launch_trsv(int n, int nt, long long ld, const float* L, const float* Linv, const float* b, float* x, int trans,
-                 int* flags, int* counter, int* status, int grid, const int* run_if, int run_when, cudaStream_t st);
+// Wavefront solves of every problem in the claim list (problem, position):
+// trans = 1: L^T x = w (w = Rv row 0, x = x); trans = 0: L w = t (t, w = Rv
+// row 0).  run_on_reuse = 1: only problems whose reuse decision is 1.
+void launch_trsv(const Prob* probs, const int2* claims, int nclaims, int trans, int* counter, int run_on_reuse,
+                 int only_active, int grid, cudaStream_t st);
 
 }  // namespace pgb

@@ -1,10 +1,11 @@
 // Blocked triangular solve with one factor L (row-major lower tiles):
 //   lower: L x = b        trans: L^T x = b
-// Wavefront over 128-row blocks: blocks are claimed in solve order through an
-// atomic counter, each block accumulates the contributions of already-solved
-// blocks as their flags are released, then applies the inverse of its
-// diagonal tile (kept by the factorisation).  A block only waits on blocks
-// claimed before it, so the launch cannot deadlock.
+// Wavefront over 128-row blocks of every problem of a batch: blocks are
+// claimed in solve order through an atomic counter, each block accumulates
+// the contributions of already-solved blocks as their flags are released,
+// then applies the inverse of its diagonal tile (kept by the factorisation).
+// A block only waits on blocks claimed before it, so the launch cannot
+// deadlock.
 // Replaces the triangular part of the reference's LU solve
 // (implicit/solvers.py:24) in the B form L L^T = B.
 #include "kernels.cuh"
@@ -69,13 +70,17 @@ __device__ __forceinline__ void tile_mv_cols(const float* __restrict__ A, long l
   }
 }
 
-__global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long long ld, const float* __restrict__ L,
-                                                             const float* __restrict__ Linv,
-                                                             const float* __restrict__ b, float* __restrict__ x,
-                                                             int trans, int* __restrict__ flags,
-                                                             int* __restrict__ counter, int* __restrict__ status,
-                                                             const int* __restrict__ run_if, int run_when) {
-  if (run_if && *run_if != run_when) return;
+// Claims (problem, position) are taken in list order; each problem's claims
+// appear in solve order, so a claim only waits on claims taken before it.
+//   trans = 1: L^T x = w   (w = row 0 of Rv, x = x)
+//   trans = 0: L w = t     (t, w = row 0 of Rv)
+// A claim is skipped when its problem has stopped (only_active), when the
+// problem does not reuse its factor this step (run_on_reuse) or when the
+// problem has aborted; every claim of such a problem is skipped alike.
+__global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(const Prob* __restrict__ probs,
+                                                             const int2* __restrict__ claims, int nclaims, int trans,
+                                                             int* __restrict__ counter, int run_on_reuse,
+                                                             int only_active) {
   __shared__ float sacc[T];
   __shared__ float sx[T];
   __shared__ float spart[8][T];
@@ -85,13 +90,27 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
     __syncthreads();
     if (tid == 0) {
       int q = atomicAdd(counter, 1);
-      if (q < nt && ld_relaxed(status + ST_ABORT)) q = nt;
+      if (q < nclaims) {
+        const Prob& P = probs[claims[q].x];
+        if ((only_active && *P.active == 0) || (run_on_reuse && P.reuse[2] != 1) || ld_relaxed(P.status + ST_ABORT))
+          q = -1;
+      }
       s_q = q;
     }
     __syncthreads();
     const int q = s_q;
-    if (q >= nt) break;
-    const int i = trans ? nt - 1 - q : q;
+    if (q >= nclaims) break;
+    if (q < 0) continue;
+    const int2 cl = claims[q];
+    const Prob& P = probs[cl.x];
+    const int n = P.sh.n, nt = P.nt;
+    const long long ld = P.ld;
+    const float* __restrict__ L = P.L;
+    const float* __restrict__ b = trans ? P.Rv : P.t;
+    float* __restrict__ x = trans ? P.x : P.Rv;
+    int* flags = P.tflags + (trans ? 0 : nt);
+    int* status = P.status;
+    const int i = trans ? nt - 1 - cl.y : cl.y;
     if (tid < T) {
       const int gi = i * T + tid;
       sacc[tid] = gi < n ? __ldcg(b + gi) : 0.0f;
@@ -121,7 +140,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
     }
     if (!ok) continue;
     // diagonal tile: x_i = Linv_ii acc (lower) or Linv_ii^T acc (trans)
-    const float* Li = Linv + (size_t)i * T * T;
+    const float* Li = P.Linv + (size_t)i * T * T;
     if (tid < T) sx[tid] = sacc[tid];
     __syncthreads();
     if (!trans)
@@ -140,9 +159,10 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(int n, int nt, long
 
 void trsv_set_attributes() {}
 
-void launch_trsv(int n, int nt, long long ld, const float* L, const float* Linv, const float* b, float* x, int trans,
-                 int* flags, int* counter, int* status, int grid, const int* run_if, int run_when, cudaStream_t st) {
-  trsv_kernel<<<grid, TS_THREADS, 0, st>>>(n, nt, ld, L, Linv, b, x, trans, flags, counter, status, run_if, run_when);
+void launch_trsv(const Prob* probs, const int2* claims, int nclaims, int trans, int* counter, int run_on_reuse,
+                 int only_active, int grid, cudaStream_t st) {
+  if (nclaims <= 0) return;
+  trsv_kernel<<<grid, TS_THREADS, 0, st>>>(probs, claims, nclaims, trans, counter, run_on_reuse, only_active);
 }
 
 }  // namespace pgb

@@ -151,11 +151,22 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parit
 }
 
 // ---------------------------------------------------------------- 3xTF32 split
-// x = hi + lo exactly, hi = x with the 13 low mantissa bits cleared (a TF32
-// value), lo = x - hi (representable; its own TF32 rounding costs ~2^-21 x).
+// Round to the nearest TF32 value (10 explicit mantissa bits, ties away from
+// zero); the result is an fp32 bit pattern whose 13 low mantissa bits are 0.
+__device__ __forceinline__ float round_tf32(float x) {
+  uint32_t r;
+  asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+  return __uint_as_float(r);
+}
+
+// x ~ hi + lo with hi and lo both TF32 values (what the tensor core reads):
+// hi = x rounded to TF32 (|x - hi| <= 2^-11 |x|), lo = (x - hi) rounded to
+// TF32 (x - hi is exact in fp32), so |x - hi - lo| <= 2^-22 |x|.  (Clearing
+// the 13 low bits instead and letting the tensor core truncate lo is 16x
+// coarser; it tripled the gradient error of the factorisation path.)
 __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
-  hi = __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
-  lo = x - hi;
+  hi = round_tf32(x);
+  lo = round_tf32(x - hi);
 }
 
 __device__ __forceinline__ uint32_t sw128_offset(int row, int unit) {

@@ -1,12 +1,17 @@
 // Per-point kernels of the Newton step, the evidence and the gradient, and
 // their deterministic two-phase reductions (block partials in double, then
-// one block summing them in a fixed order).
+// one warp per problem summing them in a fixed order).
+//
+// Batched kernels take the device problem table and vmap, a map from thread
+// block to (problem, local block of VT points over the padded length).
+#include <climits>
+
 #include "kernels.cuh"
 #include "lik.cuh"
 
 namespace pgb {
 
-constexpr int VT = 256;   // threads per block for vector kernels
+constexpr int MAX_LIK_SLOTS = 1 + 41;   // sigma_n + cutpoints b_0 .. b_J for J <= 40
 
 __device__ __forceinline__ float load_y(const Shape& sh, const void* y, int i, int* yi) {
   if (sh.lik == PGB_LIK_GAUSSIAN) {
@@ -20,7 +25,7 @@ __device__ __forceinline__ float load_y(const Shape& sh, const void* y, int i, i
 // ---------------------------------------------------------------- likelihood
 // Stand-alone per-point evaluation (pgb_log_likelihood).
 __global__ void lik_eval_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ f,
-                               const void* __restrict__ y, int n, float* logp, float* d1, float* d2, float* d3) {
+                                const void* __restrict__ y, int n, float* logp, float* d1, float* d2, float* d3) {
   const int i = blockIdx.x * VT + threadIdx.x;
   if (i >= n) return;
   int yi;
@@ -35,7 +40,37 @@ __global__ void lik_eval_kernel(Shape sh, const float* __restrict__ theta, const
 
 void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const void* y, int n, float* logp,
                      float* d1, float* d2, float* d3, cudaStream_t st) {
-  lik_eval_kernel<<<ceil_div(n, VT), VT, 0, st>>>(sh, theta, f, y, n, logp, d1, d2, d3);
+  if (n > 0) lik_eval_kernel<<<ceil_div(n, VT), VT, 0, st>>>(sh, theta, f, y, n, logp, d1, d2, d3);
+}
+
+// ---------------------------------------------------------------- reset
+// Per problem: status words (no error, no iterations, no bad column), reuse
+// flags cleared (new theta: no resident factor), active = 1; a = 0 over the
+// padded length when zero_a.
+__global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap, int zero_a) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (zero_a && i < P.n_pad) P.a[i] = 0.0f;
+  if (m.y == 0) {
+    if (threadIdx.x < 8) P.status[threadIdx.x] = threadIdx.x == ST_NOTPD_COL ? INT_MAX : 0;
+    if (threadIdx.x < 4) P.reuse[threadIdx.x] = 0;
+    if (threadIdx.x == 0) *P.active = 1;
+  }
+}
+
+void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int zero_a, cudaStream_t st) {
+  if (nblocks > 0) reset_problems_kernel<<<nblocks, VT, 0, st>>>(probs, vmap, zero_a);
+}
+
+// active = v for every problem (the phases after the Newton loop act on all)
+__global__ void set_active_kernel(const Prob* __restrict__ probs, int nprob, int v) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p < nprob) *probs[p].active = v;
+}
+
+void launch_set_active(const Prob* probs, int nprob, int v, cudaStream_t st) {
+  set_active_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob, v);
 }
 
 // ---------------------------------------------------------------- Newton step
@@ -48,225 +83,239 @@ void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const 
 // is that of the reference's LU solve.  W^1/2 is floored at 1e-18 so a W
 // that underflows to 0 keeps every quantity finite.
 // From f = K a this kernel writes d1, W, W^1/2, r and the right-hand side
-// y = r / W^1/2.  Padding entries (i >= n, up to n_pad) are zeroed.
+// t = r / W^1/2.  Padding entries (i >= n, up to n_pad) are zeroed.
 constexpr float kSwFloor = 1e-18f;
 
-__global__ void newton_lik_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ f,
-                                  const void* __restrict__ y, const float* __restrict__ a, int n_pad,
-                                  float* __restrict__ d1, float* __restrict__ W, float* __restrict__ sw,
-                                  float* __restrict__ r, float* __restrict__ rhs) {
-  const int i = blockIdx.x * VT + threadIdx.x;
-  if (i >= n_pad) return;
-  if (i >= sh.n) {
-    d1[i] = 0.0f; W[i] = 0.0f; sw[i] = 0.0f; r[i] = 0.0f; rhs[i] = 0.0f;
+__global__ void newton_lik_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.d1[i] = 0.0f; P.W[i] = 0.0f; P.sw[i] = 0.0f; P.r[i] = 0.0f; P.t[i] = 0.0f;
     return;
   }
+  const Shape sh = P.sh;
   int yi;
-  const float yv = load_y(sh, y, i, &yi);
+  const float yv = load_y(sh, P.y, i, &yi);
   LikOut o;
-  lik_point<false>(sh.lik, f[i], yv, yi, theta_sigma(sh, theta), theta_cutpoints(sh, theta), o);
+  lik_point<false>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
   const float w = -o.d2;
   const float s = fmaxf(sqrtf(w), kSwFloor);
-  const float ri = o.d1 - a[i];
-  d1[i] = o.d1;
-  W[i] = w;
-  sw[i] = s;
-  r[i] = ri;
-  rhs[i] = ri / s;
+  const float ri = o.d1 - P.a[i];
+  P.d1[i] = o.d1;
+  P.W[i] = w;
+  P.sw[i] = s;
+  P.r[i] = ri;
+  P.t[i] = ri / s;
 }
 
-void launch_newton_lik(const Shape& sh, const float* theta, const float* f, const void* y, const float* a,
-                       int n_pad, float* d1, float* W, float* sw, float* r, float* rhs, cudaStream_t st) {
-  newton_lik_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, theta, f, y, a, n_pad, d1, W, sw, r, rhs);
+void launch_newton_lik(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) newton_lik_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
 }
 
 // a_new = a + sw * x; block partial of ||a_new - a||^2 (as jaxopt measures
 // it, on the rounded new iterate); a <- a_new
-__global__ void newton_update_kernel(int n, const float* __restrict__ sw, const float* __restrict__ x,
-                                     float* __restrict__ a, double* __restrict__ part) {
+__global__ void newton_update_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   __shared__ double sred[VT / 32];
-  const int i = blockIdx.x * VT + threadIdx.x;
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;   // uniform per block
+  const int i = m.y * VT + threadIdx.x;
   float e = 0.0f;
-  if (i < n) {
-    const float ai = a[i];
-    const float an = ai + sw[i] * x[i];
+  if (i < P.sh.n) {
+    const float ai = P.a[i];
+    const float an = ai + P.sw[i] * P.x[i];
     const float dlt = an - ai;
     e = dlt * dlt;
-    a[i] = an;
+    P.a[i] = an;
   }
   const double s = block_sum_d<VT>(e, sred);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (threadIdx.x == 0) P.part[m.y] = s;
 }
 
-// One block: err = sqrt(sum part); iterations += 1; decide whether to loop.
-// jaxopt FixedPointIteration semantics (solvers.py:7-15): keep going while
-// err > tol and fewer than maxiter updates were made; a NaN error stops.
-__global__ void newton_finalize_kernel(const double* __restrict__ part, int nparts, float tol, int maxiter,
-                                       int* __restrict__ status, float* __restrict__ err_out,
-                                       cudaGraphConditionalHandle cond, int use_cond) {
+void launch_newton_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) newton_update_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// One warp per active problem: err = sqrt(sum part); iterations += 1; decide
+// whether this problem goes on.  jaxopt FixedPointIteration semantics
+// (solvers.py:7-15): keep going while err > tol and fewer than maxiter
+// updates were made; a NaN error stops.
+__global__ void newton_finalize_kernel(const Prob* __restrict__ probs, int nprob, int* __restrict__ any_active) {
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= nprob) return;
+  const Prob& P = probs[w];
+  if (*P.active == 0) return;
+  const int nparts = ceil_div(P.n_pad, VT);
   double s = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += 32) s += part[k];
+  for (int k = lane; k < nparts; k += 32) s += P.part[k];
   s = warp_sum_d(s);
-  if (threadIdx.x == 0) {
+  if (lane == 0) {
+    int* status = P.status;
     const float err = (float)sqrt(s);
     const int it = status[ST_ITERS] + 1;
     status[ST_ITERS] = it;
-    *err_out = err;
-    const bool conv = !(err > tol);
-    if (conv) status[ST_CONVERGED] = 1;
+    *P.err = err;
+    if (!(err > P.tol)) status[ST_CONVERGED] = 1;
     if (err != err) atomicCAS(status + ST_CODE, 0, PGB_ENAN);
-    const bool again = (err > tol) && (it < maxiter) && (status[ST_ABORT] == 0);
-    status[ST_SPARE0] = again ? 1 : 0;   // read by the host-driven (eager) loop
-    if (use_cond) cudaGraphSetConditional(cond, again ? 1u : 0u);
+    const bool again = (err > P.tol) && (it < P.maxiter) && (status[ST_ABORT] == 0);
+    status[ST_SPARE0] = again ? 1 : 0;
+    *P.active = again ? 1 : 0;
+    if (again) atomicOr(any_active, 1);
   }
 }
 
-void launch_newton_update(int n, const float* sw, const float* x, float* a, double* part, cudaStream_t st) {
-  newton_update_kernel<<<ceil_div(n, VT), VT, 0, st>>>(n, sw, x, a, part);
+// any_active[0] -> loop condition; copied to any_active[1] for a host-driven
+// loop; any_active[0] cleared for the next step.
+__global__ void newton_cond_kernel(int* any_active, cudaGraphConditionalHandle cond, int use_cond) {
+  const int v = any_active[0];
+  any_active[1] = v;
+  any_active[0] = 0;
+  if (use_cond) cudaGraphSetConditional(cond, v ? 1u : 0u);
 }
 
-void launch_newton_finalize(const double* part, int nparts, float tol, int maxiter, int* status, float* err_out,
-                            cudaGraphConditionalHandle cond, int use_cond, cudaStream_t st) {
-  newton_finalize_kernel<<<1, 32, 0, st>>>(part, nparts, tol, maxiter, status, err_out, cond, use_cond);
+void launch_newton_finalize(const Prob* probs, int nprob, int* any_active, cudaGraphConditionalHandle cond,
+                            int use_cond, cudaStream_t st) {
+  newton_finalize_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob, any_active);
+  newton_cond_kernel<<<1, 1, 0, st>>>(any_active, cond, use_cond);
 }
 
 // ---------------------------------------------------------------- precision
-// Full per-point terms at the final f: logp, d1, d2, d3, W, sw (padding 0).
-__global__ void lik_full_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ f,
-                                const void* __restrict__ y, int n_pad, float* __restrict__ logp,
-                                float* __restrict__ d1, float* __restrict__ d3, float* __restrict__ W,
-                                float* __restrict__ sw) {
-  const int i = blockIdx.x * VT + threadIdx.x;
-  if (i >= n_pad) return;
-  if (i >= sh.n) {
-    logp[i] = 0.0f; d1[i] = 0.0f; d3[i] = 0.0f; W[i] = 0.0f; sw[i] = 0.0f;
+// Full per-point terms at the final f: logp, d1, d3, W, sw (padding 0).
+__global__ void lik_full_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.logp[i] = 0.0f; P.d1[i] = 0.0f; P.d3[i] = 0.0f; P.W[i] = 0.0f; P.sw[i] = 0.0f;
     return;
   }
+  const Shape sh = P.sh;
   int yi;
-  const float yv = load_y(sh, y, i, &yi);
+  const float yv = load_y(sh, P.y, i, &yi);
   LikOut o;
-  lik_point<false>(sh.lik, f[i], yv, yi, theta_sigma(sh, theta), theta_cutpoints(sh, theta), o);
-  logp[i] = o.logp;
-  d1[i] = o.d1;
-  d3[i] = o.d3;
-  W[i] = -o.d2;
-  sw[i] = fmaxf(sqrtf(-o.d2), kSwFloor);
+  lik_point<false>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
+  P.logp[i] = o.logp;
+  P.d1[i] = o.d1;
+  P.d3[i] = o.d3;
+  P.W[i] = -o.d2;
+  P.sw[i] = fmaxf(sqrtf(-o.d2), kSwFloor);
 }
 
-void launch_lik_full(const Shape& sh, const float* theta, const float* f, const void* y, int n_pad, float* logp,
-                     float* d1, float* d3, float* W, float* sw, cudaStream_t st) {
-  lik_full_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, theta, f, y, n_pad, logp, d1, d3, W, sw);
+void launch_lik_full(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) lik_full_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
 }
 
 // ---------------------------------------------------------------- evidence
 // -log Z = -sum log p(f) + 1/2 f^T a + sum log diag L_B   (objective_LA,
 // Laplace.py:25-30, with sum log diag chol(K + W^-1) + 1/2 sum log W
-// = sum log diag chol(B)).  Block partials, then evidence_finalize.
-__global__ void evidence_partial_kernel(int n, const float* __restrict__ logp, const float* __restrict__ f,
-                                        const float* __restrict__ a, const float* __restrict__ L, long long ld,
-                                        double* __restrict__ part) {
+// = sum log diag chol(B)).  Block partials, then one warp per problem.
+__global__ void evidence_partial_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   __shared__ double sred[VT / 32];
-  const int i = blockIdx.x * VT + threadIdx.x;
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
   float v = 0.0f;
-  if (i < n) v = -logp[i] + 0.5f * f[i] * a[i] + logf(__ldcg(L + (size_t)i * ld + i));
+  if (i < P.sh.n) v = -P.logp[i] + 0.5f * P.f[i] * P.a[i] + logf(__ldcg(P.L + (size_t)i * P.ld + i));
   const double s = block_sum_d<VT>(v, sred);
-  if (threadIdx.x == 0) part[blockIdx.x] = s;
+  if (threadIdx.x == 0) P.part[m.y] = s;
 }
 
-__global__ void sum_parts_kernel(const double* __restrict__ part, int nparts, float* __restrict__ out) {
+__global__ void evidence_sum_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= nprob) return;
+  const Prob& P = probs[w];
+  const int nparts = ceil_div(P.n_pad, VT);
   double s = 0.0;
-  for (int k = threadIdx.x; k < nparts; k += 32) s += part[k];
+  for (int k = lane; k < nparts; k += 32) s += P.part[k];
   s = warp_sum_d(s);
-  if (threadIdx.x == 0) *out = (float)s;
+  if (lane == 0) *P.value = (float)s;
 }
 
-void launch_evidence(int n, const float* logp, const float* f, const float* a, const float* L, long long ld,
-                     double* part, float* value, cudaStream_t st) {
-  const int nb = ceil_div(n, VT);
-  evidence_partial_kernel<<<nb, VT, 0, st>>>(n, logp, f, a, L, ld, part);
-  sum_parts_kernel<<<1, 32, 0, st>>>(part, nb, value);
+void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  evidence_partial_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+  evidence_sum_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob);
 }
 
 // ---------------------------------------------------------------- gradient
 // s = 1/2 diag(Sigma) d3 with diag(Sigma)_i = rowdot_i / sw_i
 // (rowdot_i = sum_j B^-1_ij sw_j K_ji, i.e. Sigma = W^-1/2 B^-1 W^1/2 K),
-// r = a - d1 - s.
-__global__ void grad_vec1_kernel(int n, int n_pad, const float* __restrict__ rowdot, const float* __restrict__ sw,
-                                 const float* __restrict__ d3, const float* __restrict__ a,
-                                 const float* __restrict__ d1, float* __restrict__ dsig, float* __restrict__ svec,
-                                 float* __restrict__ r) {
-  const int i = blockIdx.x * VT + threadIdx.x;
-  if (i >= n_pad) return;
-  if (i >= n) {
-    dsig[i] = 0.0f; svec[i] = 0.0f; r[i] = 0.0f;
+// rv = a - d1 - s.
+__global__ void grad_vec1_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.dsig[i] = 0.0f; P.svec[i] = 0.0f; P.rv[i] = 0.0f;
     return;
   }
-  const float ds = rowdot[i] / sw[i];
-  const float s = 0.5f * ds * d3[i];
-  dsig[i] = ds;
-  svec[i] = s;
-  r[i] = a[i] - d1[i] - s;
+  const float ds = P.rowdot[i] / P.sw[i];
+  const float s = 0.5f * ds * P.d3[i];
+  P.dsig[i] = ds;
+  P.svec[i] = s;
+  P.rv[i] = P.a[i] - P.d1[i] - s;
 }
 
-void launch_grad_vec1(int n, int n_pad, const float* rowdot, const float* sw, const float* d3, const float* a,
-                      const float* d1, float* dsig, float* svec, float* r, cudaStream_t st) {
-  grad_vec1_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, rowdot, sw, d3, a, d1, dsig, svec, r);
+void launch_grad_vec1(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) grad_vec1_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
 }
 
-// out = sw * in (padding zero)
-__global__ void scale_vec_kernel(int n, int n_pad, const float* __restrict__ sw, const float* __restrict__ in,
-                                 float* __restrict__ out) {
-  const int i = blockIdx.x * VT + threadIdx.x;
-  if (i >= n_pad) return;
-  out[i] = i < n ? sw[i] * in[i] : 0.0f;
+// tz = sw * zbar (padding zero)
+__global__ void scale_tz_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  P.tz[i] = i < P.sh.n ? P.sw[i] * P.zbar[i] : 0.0f;
 }
 
-void launch_scale_vec(int n, int n_pad, const float* sw, const float* in, float* out, cudaStream_t st) {
-  scale_vec_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, sw, in, out);
+void launch_scale_tz(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) scale_tz_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
 }
 
-// u = (I + K W)^-1 zbar = W^-1/2 B^-1 (W^1/2 zbar) = y1 / sw (no cancellation);
+// u = (I + K W)^-1 zbar = W^-1/2 B^-1 (W^1/2 zbar) = y2 / sw (no cancellation);
 // c = a/2 - d1 - s - W u
-__global__ void grad_vec3_kernel(int n, int n_pad, const float* __restrict__ y1, const float* __restrict__ sw,
-                                 const float* __restrict__ a, const float* __restrict__ d1,
-                                 const float* __restrict__ svec, const float* __restrict__ W, float* __restrict__ u,
-                                 float* __restrict__ c) {
-  const int i = blockIdx.x * VT + threadIdx.x;
-  if (i >= n_pad) return;
-  if (i >= n) {
-    u[i] = 0.0f; c[i] = 0.0f;
+__global__ void grad_vec3_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.u[i] = 0.0f; P.c[i] = 0.0f;
     return;
   }
-  const float ui = y1[i] / sw[i];
-  u[i] = ui;
-  c[i] = 0.5f * a[i] - d1[i] - svec[i] - W[i] * ui;
+  const float ui = P.y2[i] / P.sw[i];
+  P.u[i] = ui;
+  P.c[i] = 0.5f * P.a[i] - P.d1[i] - P.svec[i] - P.W[i] * ui;
 }
 
-void launch_grad_vec3(int n, int n_pad, const float* y1, const float* sw, const float* a, const float* d1,
-                      const float* svec, const float* W, float* u, float* c, cudaStream_t st) {
-  grad_vec3_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, y1, sw, a, d1, svec, W, u, c);
+void launch_grad_vec3(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) grad_vec3_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
 }
 
 // Likelihood-parameter gradient, per block: slot 0 = sigma_n, slots
 // 1 .. J+1 = cutpoints b_0 .. b_J.  Per point:
 //   -dlogp/dt - 1/2 Sigma_ii dd2/dt + u_i dd1/dt
-__global__ void grad_lik_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ f,
-                                const void* __restrict__ y, const float* __restrict__ dsig,
-                                const float* __restrict__ u, double* __restrict__ part) {
+__global__ void grad_lik_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sacc[VT / 32][MAX_LIK_SLOTS];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  const Shape sh = P.sh;
   const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
-  extern __shared__ float sacc[];   // [VT/32 warps][nslots] as double below
-  double* sw_acc = reinterpret_cast<double*>(sacc);
-  for (int e = threadIdx.x; e < nslots * (VT / 32); e += VT) sw_acc[e] = 0.0;
-  __syncthreads();
-  const int i = blockIdx.x * VT + threadIdx.x;
+  const int i = m.y * VT + threadIdx.x;
   float gs = 0.0f, glo = 0.0f, ghi = 0.0f;
   int ylo = -1;
   if (i < sh.n) {
     int yi;
-    const float yv = load_y(sh, y, i, &yi);
+    const float yv = load_y(sh, P.y, i, &yi);
     LikOut o;
-    lik_point<true>(sh.lik, f[i], yv, yi, theta_sigma(sh, theta), theta_cutpoints(sh, theta), o);
-    const float ds = dsig[i], ui = u[i];
+    lik_point<true>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
+    const float ds = P.dsig[i], ui = P.u[i];
     gs = -o.lp_s - 0.5f * ds * o.d2_s + ui * o.d1_s;
     if (sh.lik != PGB_LIK_GAUSSIAN) {
       glo = -o.lp_lo - 0.5f * ds * o.d2_lo + ui * o.d1_lo;
@@ -275,9 +324,8 @@ __global__ void grad_lik_kernel(Shape sh, const float* __restrict__ theta, const
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  // sigma slot: warp sum
   const double s = warp_sum_d((double)gs);
-  if (lane == 0) sw_acc[warp * nslots + 0] = s;
+  if (lane == 0) sacc[warp][0] = s;
   if (sh.lik != PGB_LIK_GAUSSIAN) {
     // per-class sums within the warp, in lane order (deterministic)
     for (int cls = 0; cls <= sh.J; ++cls) {
@@ -285,47 +333,49 @@ __global__ void grad_lik_kernel(Shape sh, const float* __restrict__ theta, const
       if (ylo == cls) v += glo;
       if (ylo >= 0 && ylo + 1 == cls) v += ghi;
       v = warp_sum_d(v);
-      if (lane == 0) sw_acc[warp * nslots + 1 + cls] = v;
+      if (lane == 0) sacc[warp][1 + cls] = v;
     }
   }
   __syncthreads();
   for (int k = threadIdx.x; k < nslots; k += VT) {
     double t = 0.0;
-    for (int w = 0; w < VT / 32; ++w) t += sw_acc[w * nslots + k];
-    part[(size_t)blockIdx.x * nslots + k] = t;
+    for (int w = 0; w < VT / 32; ++w) t += sacc[w][k];
+    P.lpart[(size_t)m.y * nslots + k] = t;
   }
 }
 
-// Assemble the theta gradient from the trace partials (nl+1 prior slots)
-// and the likelihood partials (1 + J+1 slots).  Infinite cutpoints get 0.
-__global__ void grad_final_kernel(Shape sh, const float* __restrict__ theta, const double* __restrict__ tpart,
-                                  int ntp, const double* __restrict__ lpart, int nlp, float* __restrict__ grad) {
-  const int P = sh.nl + 1;
+// One block per problem: the theta gradient from the trace partials (nl + 1
+// prior slots, one row per lower tile) and the likelihood partials (1 + J+1
+// slots, one row per vmap block).  Infinite cutpoints get 0.
+__global__ void grad_final_kernel(const Prob* __restrict__ probs) {
+  const Prob& P = probs[blockIdx.x];
+  const Shape sh = P.sh;
+  const int NP = sh.nl + 1;
   const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
-  const int k = threadIdx.x;
-  if (k < P) {
-    double s = 0.0;
-    for (int b = 0; b < ntp; ++b) s += tpart[(size_t)b * P + k];
-    grad[k] = (float)s;
-  } else if (k < P + nslots) {
-    const int slot = k - P;
-    double s = 0.0;
-    for (int b = 0; b < nlp; ++b) s += lpart[(size_t)b * nslots + slot];
-    if (slot >= 1) {
-      const float bv = theta[sh.nl + 2 + slot - 1];
-      if (!isfinite(bv)) s = 0.0;
+  const int ntp = P.nt * (P.nt + 1) / 2;
+  const int nlp = ceil_div(P.n_pad, VT);
+  for (int k = threadIdx.x; k < NP + nslots; k += blockDim.x) {
+    if (k < NP) {
+      double s = 0.0;
+      for (int b = 0; b < ntp; ++b) s += P.tpart[(size_t)b * NP + k];
+      P.grad[k] = (float)s;
+    } else {
+      const int slot = k - NP;
+      double s = 0.0;
+      for (int b = 0; b < nlp; ++b) s += P.lpart[(size_t)b * nslots + slot];
+      if (slot >= 1) {
+        const float bv = P.theta[sh.nl + 2 + slot - 1];
+        if (!isfinite(bv)) s = 0.0;
+      }
+      P.grad[NP + slot] = (float)s;
     }
-    grad[P + slot] = (float)s;
   }
 }
 
-void launch_grad_lik_final(const Shape& sh, const float* theta, const float* f, const void* y, const float* dsig,
-                           const float* u, const double* tpart, int ntp, double* lpart, float* grad,
-                           cudaStream_t st) {
-  const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
-  const int nb = ceil_div(sh.n, VT);
-  grad_lik_kernel<<<nb, VT, sizeof(double) * nslots * (VT / 32), st>>>(sh, theta, f, y, dsig, u, lpart);
-  grad_final_kernel<<<1, 64, 0, st>>>(sh, theta, tpart, ntp, lpart, nb, grad);
+void launch_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  grad_lik_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+  grad_final_kernel<<<nprob, 64, 0, st>>>(probs);
 }
 
 // ---------------------------------------------------------------- predict
@@ -341,7 +391,7 @@ __global__ void predict_var_kernel(Shape sh, const float* __restrict__ theta, co
 
 void launch_predict_var(const Shape& sh, const float* theta, const float* rowsq, int nt, int m, float* var,
                         cudaStream_t st) {
-  predict_var_kernel<<<ceil_div(m, VT), VT, 0, st>>>(sh, theta, rowsq, nt, m, var);
+  if (m > 0) predict_var_kernel<<<ceil_div(m, VT), VT, 0, st>>>(sh, theta, rowsq, nt, m, var);
 }
 
 // sw = sqrt(W) for a caller-supplied precision (padding 0)
@@ -352,41 +402,54 @@ __global__ void sqrt_w_kernel(int n, int n_pad, const float* __restrict__ W, flo
 }
 
 void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st) {
-  sqrt_w_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, W, sw);
+  if (n_pad > 0) sqrt_w_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(n, n_pad, W, sw);
 }
 
 // ---------------------------------------------------------------- factor reuse
-// flags[1] |= any(sw != sw_prev) (bitwise; NaN always differs); sw_prev <- sw.
-__global__ void reuse_check_kernel(int n, const float* __restrict__ sw, float* __restrict__ sw_prev,
-                                   int* __restrict__ flags) {
-  const int i = blockIdx.x * VT + threadIdx.x;
+// Per active problem: reuse[1] |= any(sw != sw_prev) (bitwise; NaN always
+// differs); sw_prev <- sw.  Then per problem: reuse[2] = valid && !differs,
+// differs <- 0.
+__global__ void reuse_check_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;   // uniform per block
+  const int i = m.y * VT + threadIdx.x;
   bool diff = false;
-  if (i < n) {
-    const float a = sw[i];
-    diff = __float_as_uint(a) != __float_as_uint(sw_prev[i]) || a != a;
-    sw_prev[i] = a;
+  if (i < P.sh.n) {
+    const float a = P.sw[i];
+    diff = __float_as_uint(a) != __float_as_uint(P.sw_prev[i]) || a != a;
+    P.sw_prev[i] = a;
   }
-  if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(flags + 1, 1);
+  if (__syncthreads_or(diff) && threadIdx.x == 0) atomicOr(P.reuse + 1, 1);
 }
 
-// flags[2] = valid && !differs; differs <- 0
-__global__ void reuse_decide_kernel(int* flags) {
-  flags[2] = (flags[0] != 0 && flags[1] == 0) ? 1 : 0;
-  flags[1] = 0;
+__global__ void reuse_decide_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  if (*P.active == 0) return;
+  int* f = P.reuse;
+  f[2] = (f[0] != 0 && f[1] == 0) ? 1 : 0;
+  f[1] = 0;
 }
 
-void launch_reuse_check(int n, const float* sw, float* sw_prev, int* flags, cudaStream_t st) {
-  reuse_check_kernel<<<ceil_div(n, VT), VT, 0, st>>>(n, sw, sw_prev, flags);
-  reuse_decide_kernel<<<1, 1, 0, st>>>(flags);
+void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  reuse_check_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+  reuse_decide_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
 }
 
 // After a factorisation that computed L: the resident L matches sw_prev.
-__global__ void reuse_mark_valid_kernel(int* flags, const int* status) {
-  flags[0] = status[ST_CODE] == 0 ? 1 : 0;
+__global__ void reuse_mark_valid_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  if (*P.active == 0) return;
+  P.reuse[0] = P.status[ST_CODE] == 0 ? 1 : 0;
 }
 
-void launch_reuse_mark_valid(int* flags, const int* status, cudaStream_t st) {
-  reuse_mark_valid_kernel<<<1, 1, 0, st>>>(flags, status);
+void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st) {
+  reuse_mark_valid_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
 }
 
 }  // namespace pgb

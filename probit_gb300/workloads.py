@@ -94,18 +94,85 @@ def gram64(kernel, X1, X2, ell, s, period=0.5):
     return s * np.exp(-0.5 * d2)
 
 
-def draw_latent(rng, kernel, X, ell, s, period=0.5, jitter=1e-6):
-    K = gram64(kernel, X, X, ell, s, period)
-    K[np.diag_indices_from(K)] += jitter
-    L = np.linalg.cholesky(K)
+def gram64_gemm(kernel, X, ell, s, period=0.5):
+    """Float64 K(X, X) through matrix products, for large draws.
+
+    Squared distances as |z_i|^2 + |z_j|^2 - 2 z_i.z_j with z = x / l, and for
+    the periodic kernel sum_d (2 / l_d^2)(1 - cos(w x_id) cos(w x_jd)
+    - sin(w x_id) sin(w x_jd)), w = 2 pi / period, which equals
+    sum_d (2 sin(pi (x_id - x_jd) / period) / l_d)^2.
+    """
+    X = np.asarray(X, np.float64)
+    D = X.shape[1]
+    ell = np.broadcast_to(np.asarray(ell, dtype=np.float64).reshape(-1), (D,))
+    if kernel == "eq_periodic":
+        ang = X * (2.0 * math.pi / period)
+        C, S = np.cos(ang), np.sin(ang)
+        w = 2.0 / ell ** 2
+        d2 = w.sum() - (C * w) @ C.T - (S * w) @ S.T
+    else:
+        Z = X / ell
+        sq = np.einsum("ij,ij->i", Z, Z)
+        d2 = sq[:, None] + sq[None, :] - 2.0 * (Z @ Z.T)
+    np.maximum(d2, 0.0, out=d2)
+    if kernel == "matern12":
+        return s * np.exp(-np.sqrt(d2))
+    return s * np.exp(-0.5 * d2)
+
+
+def _draw_latent_torch(kernel, X, ell, s, period, jitter, z, device):
+    """The large-draw path of draw_latent in float64 torch on `device`."""
+    import torch
+
+    Xt = torch.as_tensor(np.asarray(X, np.float64), device=device)
+    D = Xt.shape[1]
+    ell_t = torch.as_tensor(np.broadcast_to(np.asarray(ell, np.float64).reshape(-1), (D,)).copy(), device=device)
+    if kernel == "eq_periodic":
+        ang = Xt * (2.0 * math.pi / period)
+        C, S = torch.cos(ang), torch.sin(ang)
+        w = 2.0 / ell_t ** 2
+        d2 = w.sum() - (C * w) @ C.T - (S * w) @ S.T
+    else:
+        Z = Xt / ell_t
+        sq = (Z * Z).sum(1)
+        d2 = sq[:, None] + sq[None, :] - 2.0 * (Z @ Z.T)
+    d2.clamp_(min=0.0)
+    K = s * (torch.exp(-torch.sqrt(d2)) if kernel == "matern12" else torch.exp(-0.5 * d2))
+    K.diagonal().add_(jitter)
+    L = torch.linalg.cholesky(K)
+    return (L @ torch.as_tensor(z, device=device)).cpu().numpy()
+
+
+def draw_latent(rng, kernel, X, ell, s, period=0.5, jitter=1e-6, device=None):
+    """f ~ GP(0, K) at X (float64 Cholesky of K + jitter I).
+
+    Draws of more than 1024 points build K by matrix products and factor it
+    with SciPy's LAPACK Cholesky (or, given a torch `device`, in float64 on
+    that device), which is much faster for large N; smaller draws keep the
+    direct per-dimension form (the fixtures under tests/golden were generated
+    with it).  The random numbers come from `rng` either way.
+    """
+    if X.shape[0] > 1024 and device is not None:
+        z = rng.standard_normal(X.shape[0])
+        return _draw_latent_torch(kernel, X, ell, s, period, jitter, z, device)
+    if X.shape[0] > 1024:
+        import scipy.linalg as sla
+
+        K = gram64_gemm(kernel, X, ell, s, period)
+        K[np.diag_indices_from(K)] += jitter
+        L = sla.cholesky(K, lower=True, check_finite=False)
+    else:
+        K = gram64(kernel, X, X, ell, s, period)
+        K[np.diag_indices_from(K)] += jitter
+        L = np.linalg.cholesky(K)
     return L @ rng.standard_normal(X.shape[0])
 
 
 def ordinal_problem(rng, N, D, J, kernel, ell, s, noise_std, cut_interior, X_low=-2.0, X_high=2.0,
-                    period=0.5, jitter=1e-6, n_test=0):
+                    period=0.5, jitter=1e-6, n_test=0, device=None):
     X = rng.uniform(X_low, X_high, size=(N, D))
     ell = np.atleast_1d(np.asarray(ell, dtype=np.float64))
-    f = draw_latent(rng, kernel, X, ell, s, period, jitter)
+    f = draw_latent(rng, kernel, X, ell, s, period, jitter, device)
     g = f + noise_std * rng.standard_normal(N)
     cut = np.concatenate([[-np.inf], np.asarray(cut_interior, dtype=np.float64), [np.inf]])
     y = np.searchsorted(cut[1:-1], g).astype(np.int32)
@@ -114,10 +181,10 @@ def ordinal_problem(rng, N, D, J, kernel, ell, s, noise_std, cut_interior, X_low
                    f.astype(np.float32))
 
 
-def regression_problem(rng, N, D, kernel, ell, s, noise_std, period=0.5, jitter=1e-6, n_test=0):
+def regression_problem(rng, N, D, kernel, ell, s, noise_std, period=0.5, jitter=1e-6, n_test=0, device=None):
     X = rng.standard_normal((N, D))
     ell = np.atleast_1d(np.asarray(ell, dtype=np.float64))
-    f = draw_latent(rng, kernel, X, ell, s, period, jitter)
+    f = draw_latent(rng, kernel, X, ell, s, period, jitter, device)
     y = f + noise_std * rng.standard_normal(N)
     Xt = rng.standard_normal((n_test, D)).astype(np.float32) if n_test else None
     return Problem(X.astype(np.float32), y.astype(np.float32), kernel, ell, float(s), float(noise_std), None,
@@ -132,16 +199,16 @@ def ordinal_c0() -> Problem:
     return p
 
 
-def regression_c1(N=8192, M=65536) -> Problem:
+def regression_c1(N=8192, M=65536, device=None) -> Problem:
     rng = np.random.default_rng(1)
-    return regression_problem(rng, N, 4, "eq", [0.5, 1.0, 1.5, 2.0], 1.0, 0.2, n_test=M)
+    return regression_problem(rng, N, 4, "eq", [0.5, 1.0, 1.5, 2.0], 1.0, 0.2, n_test=M, device=device)
 
 
 def _cut_interior(J):
     return [0.0] if J == 2 else list(np.linspace(-1.5, 1.5, J - 1))
 
 
-def batched_c2(B=1024, n_min=32, n_max=4096, seed=2) -> list[Problem]:
+def batched_c2(B=1024, n_min=32, n_max=4096, seed=2, device=None) -> list[Problem]:
     rng = np.random.default_rng(seed)
     kinds = ["eq", "matern12", "eq_periodic"]
     out = []
@@ -152,14 +219,15 @@ def batched_c2(B=1024, n_min=32, n_max=4096, seed=2) -> list[Problem]:
         kind = kinds[int(rng.integers(0, 3))]
         ell = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
         s = math.exp(rng.uniform(math.log(0.5), math.log(2.0)))
-        out.append(ordinal_problem(rng, N, D, J, kind, ell, s, math.sqrt(0.4), _cut_interior(J)))
+        out.append(ordinal_problem(rng, N, D, J, kind, ell, s, math.sqrt(0.4), _cut_interior(J), device=device))
     return out
 
 
-def hyperopt_c3(B=256, seed=3) -> list[Problem]:
+def hyperopt_c3(B=256, seed=3, device=None) -> list[Problem]:
     rng = np.random.default_rng(seed)
     out = []
     for _ in range(B):
         N = int(rng.integers(256, 2049))
-        out.append(ordinal_problem(rng, N, 3, 5, "matern12", 1.0, 1.0, math.sqrt(0.4), _cut_interior(5)))
+        out.append(ordinal_problem(rng, N, 3, 5, "matern12", 1.0, 1.0, math.sqrt(0.4), _cut_interior(5),
+                                   device=device))
     return out
