@@ -193,6 +193,46 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
   return v;
 }
 
+// Lookahead stage of tile task (i, j) of a problem with nt tile rows
+// (i >= nt: right-hand-side rows):
+//   diagonal (j, j) -> 2j,  sub-diagonal (j+1, j) -> 2j+1,
+//   other tiles of column j and right-hand-side tiles -> 2j+3,
+// so the diagonal and sub-diagonal of column j+1 (the critical path) are
+// handed out before the rest of column j, whose tiles need the inverse of
+// the diagonal tile L_jj; by the time they are taken that inverse is
+// usually published, and their blocks do not sit waiting for it.  Sorting
+// by (stage, j, i) keeps every task after all tasks it waits for: a task
+// (i, j) waits for (i, k), (j, k) with k < j (stages <= 2j+1, and at stage
+// 2j+1 only column j-1 < j) and for (j, j) (stage 2j).
+int dag_stage(int i, int j, int nt) {
+  if (i < nt && i == j) return 2 * j;
+  if (i < nt && i == j + 1) return 2 * j + 1;
+  return 2 * j + 3;
+}
+
+// One task list from every problem's tasks: by stage, then problem rank,
+// then column, then row.
+std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const std::vector<int>& nt,
+                              const std::vector<int>& rank) {
+  struct Key {
+    int stage, rank, j, i;
+    int4 t;
+  };
+  std::vector<Key> all;
+  for (size_t p = 0; p < per.size(); ++p)
+    for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p]), rank[p], t.z, t.y, t});
+  std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
+    if (a.stage != b.stage) return a.stage < b.stage;
+    if (a.rank != b.rank) return a.rank < b.rank;
+    if (a.j != b.j) return a.j < b.j;
+    return a.i < b.i;
+  });
+  std::vector<int4> out;
+  out.reserve(all.size());
+  for (const Key& x : all) out.push_back(x.t);
+  return out;
+}
+
 template <class Tp>
 int upload(Tp* dst, const std::vector<Tp>& v) {
   if (!v.empty()) CU_TRY(cudaMemcpy(dst, v.data(), v.size() * sizeof(Tp), cudaMemcpyHostToDevice));
@@ -414,25 +454,15 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     for (auto& x : sy) e.h_syrk.push_back(x.second);
     e.nsyrk = (int)e.h_syrk.size();
   }
-  // merged DAG task lists: column by column, problems by rank within a column
+  // merged DAG task lists in lookahead order (dag_stage), problems by rank
+  // within a stage
   {
     const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
     for (int k = 0; k < 3; ++k) {
-      struct Key {
-        int j, rank, seq;
-        int4 t;
-      };
-      std::vector<Key> all;
-      for (int p = 0; p < count; ++p) {
-        std::vector<int4> v = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
-        for (size_t s = 0; s < v.size(); ++s) all.push_back(Key{v[s].z, rank[p], (int)s, v[s]});
-      }
-      std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
-        if (a.j != b.j) return a.j < b.j;
-        if (a.rank != b.rank) return a.rank < b.rank;
-        return a.seq < b.seq;
-      });
-      for (const Key& x : all) e.h_tasks[k].push_back(x.t);
+      std::vector<std::vector<int4>> per(count);
+      for (int p = 0; p < count; ++p)
+        per[p] = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
+      e.h_tasks[k] = merge_tasks(per, e.nt, rank);
       e.ntasks[k] = (int)e.h_tasks[k].size();
     }
   }
@@ -896,7 +926,7 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
       cudaFree(gp->tasks_c);
       gp->tasks_c = nullptr;
     }
-    std::vector<int4> v = build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false);
+    std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0});
     if (cudaMalloc(reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)) != cudaSuccess) {
       cudaGetLastError();
       gp->tasks_c = nullptr;
@@ -1026,6 +1056,41 @@ void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
   for (const Item& it : items)
     if (std::strcmp(it.n, name) == 0) return const_cast<void*>(it.p);
   return nullptr;
+}
+
+// Internal diagnostic entries (not part of the public C-ABI): the merged
+// task list of one factorisation kind (0 Newton step, 1 factor only, 2 with
+// L^-T) and the per-task timestamps of the last factorisation launch
+// (PGB_TRACE=1), for the test suite and profiling scripts.
+int pgbx_batch_tasks(pgb_batch* b, int slot, const void** tasks, const void** trace) {
+  if (!b || slot < 0 || slot > 2) return -1;
+  if (tasks) *tasks = b->e.tasks[slot];
+  if (trace) *trace = b->e.trace;
+  return b->e.ntasks[slot];
+}
+
+// Internal diagnostic entry (host only, no GPU needed): the merged task list
+// the engine builds for `count` problems of nt[p] tile rows (kind 0 Newton
+// step, 1 factor only, 2 with L^-T), written to out[4 * task] as (job, i, j,
+// 0); returns the task count (call with out = NULL to size).
+int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, int32_t* out) {
+  if (!nt || count < 1 || kind < 0 || kind > 2) return -1;
+  const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
+  std::vector<std::vector<int4>> per(count);
+  std::vector<int> ntv(nt, nt + count), order(count), rank(count);
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nt[a] > nt[b]; });
+  for (int r = 0; r < count; ++r) rank[order[r]] = r;
+  for (int p = 0; p < count; ++p) per[p] = build_tasks(p * JOB_COUNT + kind, nt[p], kinds[kind], kind == 0 ? 1 : nt[p], true);
+  std::vector<int4> v = merge_tasks(per, ntv, rank);
+  if (out)
+    for (size_t t = 0; t < v.size(); ++t) {
+      out[4 * t] = v[t].x;
+      out[4 * t + 1] = v[t].y;
+      out[4 * t + 2] = v[t].z;
+      out[4 * t + 3] = 0;
+    }
+  return (int)v.size();
 }
 
 }  // extern "C"

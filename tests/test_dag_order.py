@@ -1,0 +1,70 @@
+"""The merged tile-task order of the factorisation kernel is topological.
+
+The persistent factorisation hands tasks out in list order through one
+atomic counter and a task only waits for tasks it depends on; the launch
+cannot deadlock as long as every dependency comes earlier in the list.  The
+list is built on the host (pgbx_dag_order returns it without a GPU), so this
+is checked here for single problems and for mixed-size batches, for the
+Newton-step (one right-hand-side row), factor-only and L^-T (identity
+right-hand side) task lists.
+"""
+
+import ctypes as C
+
+import numpy as np
+import pytest
+
+
+def _order(lib, nts, kind):
+    lib.pgbx_dag_order.restype = C.c_int
+    lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
+    arr = (C.c_int32 * len(nts))(*nts)
+    n = lib.pgbx_dag_order(arr, len(nts), kind, None)
+    assert n > 0
+    out = (C.c_int32 * (4 * n))()
+    assert lib.pgbx_dag_order(arr, len(nts), kind, out) == n
+    return np.array(out[:], dtype=np.int64).reshape(n, 4)
+
+
+def _deps(i, j, nt, kind):
+    """Tasks (i', j') that task (i, j) waits for."""
+    if i < nt:
+        d = [(i, k) for k in range(j)] + [(j, k) for k in range(j)]
+        if i != j:
+            d.append((j, j))
+        return d
+    r = i - nt
+    k0 = r if kind == 2 else 0   # identity rows start at their own column
+    return [(i, k) for k in range(k0, j)] + [(j, k) for k in range(k0, j)] + [(j, j)]
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("nts", [[1], [2], [5], [17], [3, 1, 7, 2, 7], [32, 1, 1, 4, 9, 2, 16]])
+def test_dag_order_topological(native_lib, nts, kind):
+    tasks = _order(native_lib, nts, kind)
+    pos = {}
+    for t, (job, i, j, _) in enumerate(tasks):
+        p = job // 4
+        assert job % 4 == kind
+        key = (p, i, j)
+        assert key not in pos, key
+        pos[key] = t
+    for p, nt in enumerate(nts):
+        nrt = 1 if kind == 0 else (0 if kind == 1 else nt)
+        expect = nt * (nt + 1) // 2 + (nt if kind == 0 else (nt * (nt + 1) // 2 if kind == 2 else 0))
+        assert sum(1 for k in pos if k[0] == p) == expect
+        for (pp, i, j), t in pos.items():
+            if pp != p:
+                continue
+            for dep in _deps(i, j, nt, kind):
+                assert (p, *dep) in pos, (p, i, j, dep)
+                assert pos[(p, *dep)] < t, ("dependency after task", p, (i, j), dep)
+
+
+def test_dag_order_lookahead(native_lib):
+    """The next column's diagonal is handed out before the rest of a column."""
+    tasks = _order(native_lib, [6], 1)
+    seq = [(int(i), int(j)) for _, i, j, _ in tasks]
+    assert seq.index((1, 1)) < seq.index((2, 0))
+    assert seq.index((2, 2)) < seq.index((3, 1))
+    assert seq.index((3, 3)) < seq.index((4, 2))
