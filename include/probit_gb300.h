@@ -56,7 +56,8 @@ extern "C" {
 /* Shape of one GP problem; fixed for the life of a handle. */
 typedef struct pgb_desc {
   int32_t n;              /* training points N (1 .. 2^20)                   */
-  int32_t d;              /* input dimension D (1 .. PGB_MAX_D)              */
+  int32_t d;              /* input dimension D (1 .. PGB_MAX_D; eq_periodic:
+                             1 .. PGB_MAX_D / 2, else PGB_EUNSUPPORTED)     */
   int32_t kernel;         /* PGB_KERNEL_*                                    */
   int32_t n_lengthscales; /* 1 (isotropic) or d (ARD)                        */
   float period;           /* period of EQ.periodic(period)                   */

@@ -78,7 +78,7 @@ struct MvGroup {
   int2* map = nullptr;
 };
 struct TraceGroup {
-  int DM;
+  int DM, periodic;
   std::vector<int4> h;
   int4* tiles = nullptr;
 };
@@ -111,6 +111,7 @@ struct Engine {
   size_t ready_words = 0;
   int* tflags_all = nullptr;
   size_t tflags_words = 0;
+  unsigned char* maps_all = nullptr;       // per problem: tensor maps of L, Linv, Rv, Rz (128 B each)
   // block maps
   std::vector<int2> h_vmap, h_bmap, h_claims;
   std::vector<int4> h_syrk;
@@ -148,21 +149,11 @@ int validate(const pgb_desc* d) {
   if (d->kernel == PGB_KERNEL_EQ_PERIODIC && !(d->period > 0.0f)) return PGB_EINVAL;
   if (!(d->tolerance >= 0.0f) || d->maxiter < 1) return PGB_EINVAL;
   if (d->flags != 0) return PGB_EINVAL;
+  if (feature_count(d) > MAX_D) return PGB_EUNSUPPORTED;   // eq_periodic: 2 features per input dimension
   return PGB_OK;
 }
 
-Shape make_shape(const pgb_desc* d) {
-  Shape s;
-  s.n = d->n;
-  s.D = d->d;
-  s.Dp = (d->d + 3) / 4 * 4;
-  s.kind = d->kernel;
-  s.nl = d->n_lengthscales;
-  s.lik = d->likelihood;
-  s.J = d->likelihood == PGB_LIK_GAUSSIAN ? 0 : d->j;
-  s.inv_p = d->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(1.0 / (double)d->period) : 0.0f;
-  return s;
-}
+Shape make_shape(const pgb_desc* d) { return shape_from_desc(d); }
 
 int theta_size_of(const pgb_desc* d) {
   return theta_len(d->n_lengthscales, d->likelihood, d->likelihood == PGB_LIK_GAUSSIAN ? 0 : d->j);
@@ -239,6 +230,29 @@ int upload(Tp* dst, const std::vector<Tp>& v) {
   return PGB_OK;
 }
 
+enum MapSlot { MAP_L = 0, MAP_LINV = 1, MAP_RV = 2, MAP_RZ = 3, MAPS_PER_PROB = 4 };
+
+const void* map_slot(const Engine& e, int p, int slot) {
+  return e.maps_all + ((size_t)p * MAPS_PER_PROB + slot) * 128;
+}
+
+// Encode the tensor maps of every problem's L, Linv, Rv (and Rz when
+// allocated) and copy them to the arena.
+int upload_maps(Engine& e) {
+  std::vector<unsigned char> h((size_t)e.nprob * MAPS_PER_PROB * 128, 0);
+  for (int p = 0; p < e.nprob; ++p) {
+    const Prob& q = e.hp[p];
+    unsigned char* m = h.data() + (size_t)p * MAPS_PER_PROB * 128;
+    bool ok = make_tile_map(m + MAP_L * 128, q.L, q.n_pad, q.ld, q.ld) &&
+              make_tile_map(m + MAP_LINV * 128, q.Linv, (long long)q.nt * T, T, T) &&
+              make_tile_map(m + MAP_RV * 128, q.Rv, T, q.ld, q.ld);
+    if (ok && q.Rz) ok = make_tile_map(m + MAP_RZ * 128, q.Rz, q.n_pad, q.ld, q.ld);
+    if (!ok) return PGB_ECUDA;
+  }
+  CU_TRY(cudaMemcpy(e.maps_all, h.data(), h.size(), cudaMemcpyHostToDevice));
+  return PGB_OK;
+}
+
 // Assign every device pointer of the engine from `base` (0: sizing pass).
 size_t layout(Engine& e, uintptr_t base) {
   Bump b;
@@ -257,6 +271,7 @@ size_t layout(Engine& e, uintptr_t base) {
   e.any_active = b.take<int>(2);
   e.ready_all = b.take<int>(e.ready_words);
   e.tflags_all = b.take<int>(e.tflags_words);
+  e.maps_all = b.take<unsigned char>((size_t)np * MAPS_PER_PROB * 128);
   e.probs = b.take<Prob>(np);
   e.jobs = b.take<DagJob>((size_t)np * JOB_COUNT);
   e.vmap = b.take<int2>(e.h_vmap.size());
@@ -303,6 +318,7 @@ size_t layout(Engine& e, uintptr_t base) {
     tflags_off += 2 * (size_t)nt;
     q.Rz = nullptr;
     q.Binv = nullptr;
+    q.tm_Rz = map_slot(e, p, MAP_RZ);
     // factorisation jobs of this problem
     for (int k = 0; k < JOB_COUNT; ++k) {
       DagJob& j = e.hjobs[(size_t)p * JOB_COUNT + k];
@@ -320,6 +336,8 @@ size_t layout(Engine& e, uintptr_t base) {
       j.status = q.status;
       j.reuse = q.reuse + 2;
       j.reuse_mode = 0;
+      j.tm_L = map_slot(e, p, MAP_L);
+      j.tm_Linv = map_slot(e, p, MAP_LINV);
     }
     ready_off += 2 * (size_t)nt * nt;
     DagJob* jb = &e.hjobs[(size_t)p * JOB_COUNT];
@@ -330,12 +348,14 @@ size_t layout(Engine& e, uintptr_t base) {
     jb[JOB_VEC].rhs_vec = q.t;
     jb[JOB_VEC].reuse_mode = 2;
     jb[JOB_VEC].active = q.active;
+    jb[JOB_VEC].tm_R = map_slot(e, p, MAP_RV);
     jb[JOB_NONE].rhs_kind = RHS_NONE;
     jb[JOB_NONE].reuse_mode = 1;
     jb[JOB_IDENT].rhs_kind = RHS_IDENT;
     jb[JOB_IDENT].reuse_mode = 1;
     jb[JOB_IDENT].nrt = nt;
     jb[JOB_IDENT].nrhs = (int)npad;
+    jb[JOB_IDENT].tm_R = q.tm_Rz;
     jb[JOB_CROSS].rhs_kind = RHS_CROSS;
   }
   return b.off;
@@ -429,18 +449,21 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   }
   // gradient trace tiles by feature width; B^-1 tiles longest k-range first
   {
-    std::map<int, int> gi;
+    std::map<std::pair<int, int>, int> gi;
     std::vector<std::pair<int, int4>> sy;
     for (int pr = 0; pr < count; ++pr) {
       const int p = order[pr];
       const int DM = dm_of(e.sh[p].Dp);
-      if (!gi.count(DM)) {
-        gi[DM] = (int)e.tr.size();
+      const int per = e.sh[p].kind == PGB_KERNEL_EQ_PERIODIC ? 1 : 0;
+      const auto key = std::make_pair(DM, per);
+      if (!gi.count(key)) {
+        gi[key] = (int)e.tr.size();
         TraceGroup g;
         g.DM = DM;
+        g.periodic = per;
         e.tr.push_back(g);
       }
-      TraceGroup& g = e.tr[gi[DM]];
+      TraceGroup& g = e.tr[gi[key]];
       int ord = 0;
       for (int I = 0; I < e.nt[p]; ++I)
         for (int J = 0; J <= I; ++J) {
@@ -509,6 +532,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
       }
     }
   }
+  PGB_TRY(upload_maps(e));
   PGB_TRY(engine_upload_tables(e));
   CU_TRY(cudaStreamCreateWithFlags(&e.cap_s, cudaStreamNonBlocking));
   CU_TRY(cudaStreamCreateWithFlags(&e.cap_s2, cudaStreamNonBlocking));
@@ -534,6 +558,7 @@ int ensure_grad_buffers(Engine& e) {
     e.hp[p].Binv = b.take<float>(mat);
     e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].R = e.hp[p].Rz;
   }
+  PGB_TRY(upload_maps(e));
   PGB_TRY(engine_upload_tables(e));
   e.grad_ready = 1;
   return PGB_OK;
@@ -591,7 +616,7 @@ void enq_grad(Engine& e, cudaStream_t s) {
   launch_scale_tz(e.probs, e.vmap, e.nvb, s);
   launch_binv_matvec(e.probs, e.bmap, e.nbb, s);
   launch_grad_vec3(e.probs, e.vmap, e.nvb, s);
-  for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, e.probs, g.tiles, (int)g.h.size(), s);
+  for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), s);
   launch_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
 }
 
@@ -706,6 +731,7 @@ struct pgb_gp {
   float* Xq = nullptr;
   float* Xq_in = nullptr;
   int* ready_c = nullptr;
+  void* map_c = nullptr;   // tensor map of Rc (device, 128 B)
   int4* tasks_c = nullptr;
   int ntasks_c = 0;
   long long cap_c = 0;     // predict rows allocated
@@ -761,7 +787,7 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
 int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
   engine_free(gp->e);
-  void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c};
+  void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c, gp->map_c};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete gp;
@@ -918,6 +944,10 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq), sizeof(float) * (size_t)mpad * sh.Dp));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq_in), sizeof(float) * (size_t)mpad * sh.D));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->ready_c), sizeof(int) * (size_t)(nt + mt) * nt));
+    if (!gp->map_c) PGB_TRY(grab(&gp->map_c, 128));
+    alignas(64) unsigned char m[128];
+    if (!make_tile_map(m, gp->Rc, mpad, q.ld, q.ld)) return PGB_ECUDA;
+    CU_TRY(cudaMemcpy(gp->map_c, m, sizeof(m), cudaMemcpyHostToDevice));
     gp->cap_c = mpad;
   }
   if (gp->m_tasks != mt) {
@@ -955,6 +985,7 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
     jb.Xq = gp->Xq;
     jb.rowsq = gp->rowsq;
     jb.ready = gp->ready_c;
+    jb.tm_R = gp->map_c;
     CU_TRY(cudaMemcpyAsync(e.jobs + JOB_CROSS, &jb, sizeof(DagJob), cudaMemcpyHostToDevice, s));
     // L tiles are done: mark them ready; RHS tiles start unready
     CU_TRY(cudaMemsetAsync(gp->ready_c, 1, sizeof(int) * (size_t)nt * nt, s));

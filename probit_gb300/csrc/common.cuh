@@ -80,40 +80,19 @@ __device__ __forceinline__ void raise_status(int* status, int code) {
 
 // ---------------------------------------------------------------- kernels
 // Kernel functions restated from mlkernels' EQ / Matern12 / EQ.periodic(p)
-// with ``stretch``: the inputs are divided by the lengthscale before the
-// distance (features are prepared by prep_features).  For the periodic
-// kernel the stored features are the raw inputs and the distance is
-// q_d = (2 sin(pi (x_d - z_d) / p) / l_d)^2, with sin(pi u) evaluated by sinpif.
-struct KernelParams {
-  int kind;        // PGB_KERNEL_*
-  int D;           // input dims
-  int Dp;          // feature row stride (floats)
-  int nl;          // number of lengthscales (1 or D)
-  float s;         // signal variance
-  float inv_p;     // 1 / period (periodic only)
-  float inv_l[MAX_D];   // 1/l_d (periodic: used after the sine)
-  float l[MAX_D];
-};
-
-__device__ __forceinline__ float sq_dist_dim(const KernelParams& kp, float xi, float xj, int d) {
-  if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-    const float v = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
-    return v * v;
-  }
-  const float v = xi - xj;
-  return v * v;
-}
-
-// k(r) * s from the summed scaled squared distance.
-__device__ __forceinline__ float kernel_from_d2(const KernelParams& kp, float d2) {
-  if (kp.kind == PGB_KERNEL_MATERN12) return kp.s * expf(-sqrtf(d2));
-  return kp.s * expf(-0.5f * d2);
-}
-
-__device__ __forceinline__ float kernel_eval(const KernelParams& kp, const float* xi, const float* xj) {
-  float d2 = 0.0f;
-  for (int d = 0; d < kp.D; ++d) d2 += sq_dist_dim(kp, xi[d], xj[d], d);
-  return kernel_from_d2(kp, d2);
+// with ``stretch`` (the inputs are divided by the lengthscale before the
+// distance).  Every kernel is evaluated on prepared features:
+//   eq, matern12 : f_d = x_d / l_d                         (F = D features)
+//   eq_periodic  : f_2d = sin(2 pi x_d / p) / l_d,
+//                  f_2d+1 = cos(2 pi x_d / p) / l_d          (F = 2D features)
+// (mlkernels' periodic composition maps each input to (sin, cos) and the
+// stretch divides them by l; (sin a - sin b)^2 + (cos a - cos b)^2 =
+// 4 sin^2((a - b) / 2), so the feature distance is the periodic one).
+// Feature rows are zero padded to Dp = 4 ceil(F / 4), so a kernel value is
+// d2 = sum over all Dp features of (f_i - f_j)^2, then
+//   eq, eq_periodic: s exp(-d2 / 2),   matern12: s exp(-sqrt(d2)).
+__device__ __forceinline__ float kernel_of_d2(int matern, float s, float d2) {
+  return s * expf(matern ? -sqrtf(d2) : -0.5f * d2);
 }
 
 // ---------------------------------------------------------------- reductions
@@ -157,30 +136,34 @@ namespace pgb {
 struct Shape {
   int n;          // training points
   int D;          // input dims
-  int Dp;         // feature row stride (floats, multiple of 4)
+  int F;          // kernel features (D, or 2D for eq_periodic)
+  int Dp;         // feature row stride (floats, multiple of 4, <= MAX_D)
   int kind;       // PGB_KERNEL_*
   int nl;         // lengthscales (1 or D)
   int lik;        // PGB_LIK_*
   int J;          // ordinal classes
-  float inv_p;      // 1 / period
+  float inv_p;    // 1 / period
 };
 
-// Build the kernel parameters from the device hyperparameter block.
-__device__ __forceinline__ KernelParams make_kp(const Shape& sh, const float* __restrict__ theta) {
-  KernelParams kp;
-  kp.kind = sh.kind;
-  kp.D = sh.D;
-  kp.Dp = sh.Dp;
-  kp.nl = sh.nl;
-  kp.inv_p = sh.inv_p;
-#pragma unroll 1
-  for (int d = 0; d < sh.nl; ++d) {
-    kp.l[d] = __ldg(theta + d);
-    kp.inv_l[d] = 1.0f / kp.l[d];
-  }
-  kp.s = __ldg(theta + sh.nl);
-  return kp;
+// Shape of a validated descriptor.
+inline Shape shape_from_desc(const pgb_desc* d) {
+  Shape s;
+  s.n = d->n;
+  s.D = d->d;
+  s.F = d->kernel == PGB_KERNEL_EQ_PERIODIC ? 2 * d->d : d->d;
+  s.Dp = (s.F + 3) / 4 * 4;
+  s.kind = d->kernel;
+  s.nl = d->n_lengthscales;
+  s.lik = d->likelihood;
+  s.J = d->likelihood == PGB_LIK_GAUSSIAN ? 0 : d->j;
+  s.inv_p = d->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(1.0 / (double)d->period) : 0.0f;
+  return s;
 }
+
+// Kernel features of a descriptor (F above); the kernels handle F <= MAX_D.
+inline int feature_count(const pgb_desc* d) { return d->kernel == PGB_KERNEL_EQ_PERIODIC ? 2 * d->d : d->d; }
+
+__device__ __forceinline__ float theta_signal(const Shape& sh, const float* theta) { return __ldg(theta + sh.nl); }
 
 __device__ __forceinline__ float theta_sigma(const Shape& sh, const float* theta) {
   return __ldg(theta + sh.nl + 1);

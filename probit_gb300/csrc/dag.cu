@@ -44,98 +44,118 @@ constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 // accumulator layout (row = TMEM lane, 64 columns) and stores -C_init there,
 // so the MMAs accumulate sum_k L_ik L_jk^T - C_init and the tile costs no
 // work after its last dependency arrives.
+//   L tile (i, j):  w_r K(x_r, x_c) w_c (+ 1 on the diagonal; the upper half
+//                   of a diagonal tile is 0; padding rows/columns have w = 0)
+//   RHS_CROSS rows: K(x*_r, x_c) w_c for the query points (row weight 1)
+//   RHS_VEC row 0:  t;   RHS_IDENT: the identity block of row tile ri
+// The entry loop is one uniform formula over the zero-padded features, so
+// its code stays small whatever the kernel family.
 constexpr int SX_STRIDE = 17;   // DM + 1 (<= 16 + 1), breaks bank conflicts
 constexpr int SX_FLOATS = 2 * T * SX_STRIDE + 2 * T;
 
 template <int DM>
-__device__ void stage_features(const DagJob& jb, const KernelParams& kp, int i, int j, float* sX) {
+__device__ void stage_features(const DagJob& jb, int i, int j, float* sX) {
   const int n = jb.n;
   const bool is_rhs = i >= jb.nt;
+  const bool cross = is_rhs && jb.rhs_kind == RHS_CROSS;
   const int ri = i - jb.nt;
+  const int Dp = jb.sh.Dp;
   float* sXr = sX;
   float* sXc = sX + T * SX_STRIDE;
   float* sWr = sXc + T * SX_STRIDE;
   float* sWc = sWr + T;
   for (int e = threadIdx.x; e < T * DM; e += DAG_THREADS) {
-    const int r = e / DM, d = e % DM;
+    const int r = e / DM, f = e % DM;
     const int gj = j * T + r;
-    sXc[r * SX_STRIDE + d] = (gj < n && d < kp.Dp) ? __ldg(jb.Xf + (size_t)gj * kp.Dp + d) : 0.0f;
+    sXc[r * SX_STRIDE + f] = (gj < n && f < Dp) ? __ldg(jb.Xf + (size_t)gj * Dp + f) : 0.0f;
     float xr = 0.0f;
-    if (d < kp.Dp) {
+    if (f < Dp) {
       if (!is_rhs) {
         const int gi = i * T + r;
-        if (gi < n) xr = __ldg(jb.Xf + (size_t)gi * kp.Dp + d);
-      } else if (jb.rhs_kind == RHS_CROSS) {
+        if (gi < n) xr = __ldg(jb.Xf + (size_t)gi * Dp + f);
+      } else if (cross) {
         const int gi = ri * T + r;
-        if (gi < jb.nrhs) xr = __ldg(jb.Xq + (size_t)gi * kp.Dp + d);
+        if (gi < jb.nrhs) xr = __ldg(jb.Xq + (size_t)gi * Dp + f);
       }
     }
-    sXr[r * SX_STRIDE + d] = xr;
+    sXr[r * SX_STRIDE + f] = xr;
   }
   for (int r = threadIdx.x; r < T; r += DAG_THREADS) {
     const int gj = j * T + r, gi = i * T + r;
     sWc[r] = gj < n ? __ldcg(jb.sw + gj) : 0.0f;
-    sWr[r] = (!is_rhs && gi < n) ? __ldcg(jb.sw + gi) : 0.0f;
+    float wr = 0.0f;
+    if (!is_rhs)
+      wr = gi < n ? __ldcg(jb.sw + gi) : 0.0f;
+    else if (cross)
+      wr = (ri * T + r < jb.nrhs) ? 1.0f : 0.0f;
+    sWr[r] = wr;
   }
 }
 
+// -C_init into the TMEM accumulator (all 8 warps; thread: row r, columns
+// cb .. cb + 63).
 template <int DM>
-__device__ __forceinline__ float cinit_entry(const DagJob& jb, const KernelParams& kp, int i, int j, int r, int c,
-                                             const float* sX) {
+__device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, const float* sX) {
   const float* sXr = sX;
   const float* sXc = sX + T * SX_STRIDE;
   const float* sWr = sXc + T * SX_STRIDE;
   const float* sWc = sWr + T;
-  const int n = jb.n;
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int r = (w & 3) * 32 + lane;
+  const int cb = (w >> 2) * 64;
+  const uint32_t taddr = tmem + ((uint32_t)((w & 3) * 32) << 16);
   const bool is_rhs = i >= jb.nt;
   const int ri = i - jb.nt;
-  const int gj = j * T + c;
-  if (!is_rhs) {
-    const int gi = i * T + r;
-    if (i == j && c > r) return 0.0f;
-    if (gi < n && gj < n) {
-      float d2 = 0.0f;
+  if (!is_rhs || jb.rhs_kind == RHS_CROSS) {
+    const int matern = jb.sh.kind == PGB_KERNEL_MATERN12;
+    const float sv = __ldg(jb.theta + jb.sh.nl);
+    const bool diag = !is_rhs && i == j;
+    float xr[DM];
 #pragma unroll
-      for (int d = 0; d < DM; ++d) {
-        if (d < kp.D) {
-          float q;
-          const float xi = sXr[r * SX_STRIDE + d], xj = sXc[c * SX_STRIDE + d];
-          if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
-            q = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
-          else
-            q = xi - xj;
-          d2 += q * q;
+    for (int f = 0; f < DM; ++f) xr[f] = sXr[r * SX_STRIDE + f];
+    const float wr = sWr[r];
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      float v[32];
+#pragma unroll
+      for (int q = 0; q < 32; ++q) {
+        const int c = cb + 32 * h + q;
+        float d2 = 0.0f;
+#pragma unroll
+        for (int f = 0; f < DM; ++f) {
+          const float u = xr[f] - sXc[c * SX_STRIDE + f];
+          d2 = fmaf(u, u, d2);
         }
+        float val = wr * kernel_of_d2(matern, sv, d2) * sWc[c];
+        if (diag) {
+          if (c == r) val += 1.0f;
+          if (c > r) val = 0.0f;
+        }
+        v[q] = -val;
       }
-      float v = sWr[r] * kernel_from_d2(kp, d2) * sWc[c];
-      if (gi == gj) v += 1.0f;
-      return v;
+      tmem_st_32x32(taddr + (uint32_t)(cb + 32 * h), v);
     }
-    return (gi == gj) ? 1.0f : 0.0f;
-  }
-  if (jb.rhs_kind == RHS_VEC) {
-    const int gi = ri * T + r;
-    return (gi == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
-  }
-  if (jb.rhs_kind == RHS_IDENT) return (ri == j && r == c) ? 1.0f : 0.0f;
-  const int gi = ri * T + r;   // RHS_CROSS
-  if (gi < jb.nrhs && gj < n) {
-    float d2 = 0.0f;
+  } else {
+    const int n = jb.n;
+#pragma unroll 1
+    for (int h = 0; h < 2; ++h) {
+      float v[32];
 #pragma unroll
-    for (int d = 0; d < DM; ++d) {
-      if (d < kp.D) {
-        float q;
-        const float xi = sXr[r * SX_STRIDE + d], xj = sXc[c * SX_STRIDE + d];
-        if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
-          q = (2.0f * sinpif((xi - xj) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
+      for (int q = 0; q < 32; ++q) {
+        const int c = cb + 32 * h + q;
+        const int gj = j * T + c;
+        float val;
+        if (jb.rhs_kind == RHS_VEC)
+          val = (ri == 0 && r == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
         else
-          q = xi - xj;
-        d2 += q * q;
+          val = (ri == j && r == c) ? 1.0f : 0.0f;
+        v[q] = -val;
       }
+      tmem_st_32x32(taddr + (uint32_t)(cb + 32 * h), v);
     }
-    return kernel_from_d2(kp, d2) * sWc[c];
   }
-  return 0.0f;
+  tmem_wait_st();
+  tc_fence_before();
 }
 
 constexpr unsigned FULL = 0xffffffffu;
@@ -373,43 +393,108 @@ __device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_
 // Per-block tensor-core state, uniform across the block.
 struct TcCtx {
   uint32_t tmem;       // accumulator: 128 lanes x 128 fp32 columns
-  uint32_t g;          // chunks issued so far by this block (stage = g % NST)
+  uint32_t g;          // chunks loaded so far by this block (stage = g % NST)
   uint32_t ntask;      // accumulator commits waited so far
   uint8_t* stages;     // 1024-aligned stage buffers (unioned with sC, sL)
-  uint64_t* mbar;      // [NST] stage-free barriers, [NST] accumulator barrier
+  uint64_t* full;      // [NST] the stage's tensor loads landed
+  uint64_t* empty;     // [NST] the MMAs that read the stage completed
+  uint64_t* acc;       // every MMA issued so far completed
 };
 
-// Load one 128 x 32 chunk of A (tile rows i) and B (tile rows j) into registers:
-// thread t holds units e = t + 256 q (q < 4) of each, e -> (row e >> 3, unit e & 7).
-__device__ __forceinline__ void load_chunk(const float* __restrict__ A, long long lda, const float* __restrict__ B,
-                                           long long ldb, int kc, float4 (&ra)[4], float4 (&rb)[4]) {
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int e = threadIdx.x + DAG_THREADS * q;
-    const int row = e >> 3, u = e & 7;
-    ra[q] = __ldcg(reinterpret_cast<const float4*>(A + (size_t)row * lda + kc + 4 * u));
-    rb[q] = __ldcg(reinterpret_cast<const float4*>(B + (size_t)row * ldb + kc + 4 * u));
+// Operands of one accumulation acc += sum_{k0 <= k < k1} A_k B_k^T: A_k is
+// the 128 x 128 tile of the `amap` matrix at rows arow.., columns acol +
+// k*T.., B_k likewise.  Chunk c (32 columns) of the loop is k-tile
+// k0 + c / 4, columns (c % 4) * 32.
+struct TcLoad {
+  const void* amap;
+  const void* bmap;
+  int arow, acol, brow, bcol;
+  int k0, nchunks;
+  uint32_t base;       // tc.g when the accumulation started
+  int issued;          // chunks whose loads were issued (thread 0)
+  int ok;              // every dependency wait succeeded (thread 0)
+};
+
+__device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, const void* bmap, int brow, int bcol,
+                                          int k0, int k1, const TcCtx& tc) {
+  TcLoad l;
+  l.amap = amap;
+  l.bmap = bmap;
+  l.arow = arow;
+  l.acol = acol;
+  l.brow = brow;
+  l.bcol = bcol;
+  l.k0 = k0;
+  l.nchunks = (k1 - k0) * (T / 32);
+  l.base = tc.g;
+  l.issued = 0;
+  l.ok = 1;
+  return l;
+}
+
+// Thread 0: issue the loads of chunk `c` into its stage, after the MMAs of
+// the stage's previous chunk completed and, at a k-tile boundary, after the
+// k-tile's dependencies were published (wait_tile).  A dependency wait that
+// gives up still issues the loads (the addresses are valid; the result is
+// discarded), so the stage accounting stays consistent.  False if a
+// pipeline wait timed out.
+template <class WaitTile>
+__device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, WaitTile& wait_tile) {
+  const uint32_t g = l.base + (uint32_t)c;
+  const uint32_t s = g % NST;
+  if (g >= NST && !mbar_wait_bounded(tc.empty + s, ((g / NST) - 1u) & 1u, MMA_WAIT_NS)) return false;
+  if ((c % (T / 32)) == 0) {
+    if (!wait_tile(l.k0 + c / (T / 32))) l.ok = 0;
+    fence_proxy_async_global();
   }
+  const int col = (l.k0 + c / (T / 32)) * T + (c % (T / 32)) * 32;
+  uint8_t* stage = tc.stages + s * STAGE_BYTES;
+  mbar_arrive_expect_tx(tc.full + s, 2 * CHUNK_BYTES);
+  tma_load_2d(stage, l.amap, l.acol + col, l.arow, tc.full + s);
+  tma_load_2d(stage + 2 * CHUNK_BYTES, l.bmap, l.bcol + col, l.brow, tc.full + s);
+  l.issued = c + 1;
+  return true;
 }
 
-__device__ __forceinline__ void store_split(uint8_t* hi, uint8_t* lo, int row, int u, float4 v) {
-  float4 h, l;
-  split_tf32(v.x, h.x, l.x);
-  split_tf32(v.y, h.y, l.y);
-  split_tf32(v.z, h.z, l.z);
-  split_tf32(v.w, h.w, l.w);
-  const uint32_t off = sw128_offset(row, u);
-  *reinterpret_cast<float4*>(hi + off) = h;
-  *reinterpret_cast<float4*>(lo + off) = l;
+// Thread 0: the loads of the first NST - 1 chunks (issued early, e.g.
+// before C_init is evaluated, so they land while other work runs).
+template <class WaitTile>
+__device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& wait_tile) {
+  for (int c = 0; c < min(NST - 1, l.nchunks); ++c)
+    if (!tc_issue(tc, l, c, wait_tile)) return false;
+  return true;
 }
 
-__device__ __forceinline__ void store_chunk(uint8_t* stage, const float4 (&ra)[4], const float4 (&rb)[4]) {
+// Split the fp32 A and B chunks the loads left in a stage into TF32 hi (in
+// place) and lo parts; the 128-byte swizzle is the same for both, so the
+// split is element by element.
+__device__ __forceinline__ void convert_stage(uint8_t* stage) {
+  float4* ah = reinterpret_cast<float4*>(stage);
+  float4* bh = reinterpret_cast<float4*>(stage + 2 * CHUNK_BYTES);
+  constexpr int LO = CHUNK_BYTES / 16;
+  float4 a[4], b[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int e = threadIdx.x + DAG_THREADS * q;
-    const int row = e >> 3, u = e & 7;
-    store_split(stage, stage + CHUNK_BYTES, row, u, ra[q]);
-    store_split(stage + 2 * CHUNK_BYTES, stage + 3 * CHUNK_BYTES, row, u, rb[q]);
+    a[q] = ah[e];
+    b[q] = bh[e];
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int e = threadIdx.x + DAG_THREADS * q;
+    float4 h, o;
+    split_tf32(a[q].x, h.x, o.x);
+    split_tf32(a[q].y, h.y, o.y);
+    split_tf32(a[q].z, h.z, o.z);
+    split_tf32(a[q].w, h.w, o.w);
+    ah[e] = h;
+    ah[e + LO] = o;
+    split_tf32(b[q].x, h.x, o.x);
+    split_tf32(b[q].y, h.y, o.y);
+    split_tf32(b[q].z, h.z, o.z);
+    split_tf32(b[q].w, h.w, o.w);
+    bh[e] = h;
+    bh[e + LO] = o;
   }
 }
 
@@ -431,8 +516,8 @@ __device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stag
 // Wait (bounded) until every MMA this block issued has completed.
 __device__ bool tc_drain(TcCtx& tc, int* status) {
   __syncthreads();
-  if (threadIdx.x == 0) umma_commit(tc.mbar + NST);
-  const bool ok = mbar_wait_bounded(tc.mbar + NST, tc.ntask & 1u, MMA_WAIT_NS);
+  if (threadIdx.x == 0) umma_commit(tc.acc);
+  const bool ok = mbar_wait_bounded(tc.acc, tc.ntask & 1u, MMA_WAIT_NS);
   tc.ntask++;
   if (!ok && threadIdx.x == 0) {
     atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
@@ -443,65 +528,43 @@ __device__ bool tc_drain(TcCtx& tc, int* status) {
   return ok;
 }
 
-// acc (TMEM) = sum_{k0 <= k < k1} A_k B_k^T in 3xTF32, where A_k / B_k are
-// the 128 x 128 tiles at Abase + k*T / Bbase + k*T (row strides lda / ldb).  Thread 0
-// calls wait_tile(k) before tile k is loaded; a false return (a wait gave up)
-// drains the MMAs in flight and returns false.
+// acc (TMEM) += sum_k A_k B_k^T in 3xTF32 (acc starts from zero unless
+// `preloaded`).  Thread 0 must have called tc_start on `l`, and every thread
+// must have fenced its earlier generic writes to the stage buffers
+// (fence_proxy_async_smem) before the barrier that preceded it.  Per chunk:
+// wait for its loads, split it (all threads), thread 0 issues its MMAs and
+// the loads of the chunk NST - 1 ahead.  Every wait is bounded and the loop
+// always runs to the end, so all threads take the same path; false when a
+// dependency wait gave up or a pipeline wait timed out (the problem is then
+// aborted and the accumulator is garbage).
 template <class WaitTile>
-__device__ bool tc_accumulate(const float* Abase, long long lda, const float* Bbase, long long ldb, int k0, int k1,
-                              TcCtx& tc, int* s_ok, int* status, WaitTile wait_tile, bool preloaded = false) {
-  const int nchunks = (k1 - k0) * (T / 32);
-  float4 ra[4], rb[4];
-  if (threadIdx.x == 0) {
-    s_ok[0] = wait_tile(k0);
-    __threadfence();
-  }
-  __syncthreads();
-  if (!s_ok[0]) return false;
-  load_chunk(Abase + (size_t)k0 * T, lda, Bbase + (size_t)k0 * T, ldb, 0, ra, rb);
-  for (int c = 0; c < nchunks; ++c) {
-    const uint32_t g = tc.g;
-    uint8_t* stage = tc.stages + (g % NST) * STAGE_BYTES;
-    if (g >= NST) {
-      if (!mbar_wait_bounded(tc.mbar + (g % NST), ((g / NST) - 1u) & 1u, MMA_WAIT_NS)) {
-        if (threadIdx.x == 0) {
-          atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
-          atomicExch(status + ST_ABORT, 1);
-        }
-        tc_drain(tc, status);
-        return false;
-      }
-    }
-    store_chunk(stage, ra, rb);
+__device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, bool preloaded) {
+  bool bad = false;
+  const int n = l.nchunks;
+  for (int c = 0; c < n; ++c) {
+    const uint32_t g = l.base + (uint32_t)c;
+    const uint32_t s = g % NST;
+    if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
+    uint8_t* stage = tc.stages + s * STAGE_BYTES;
+    convert_stage(stage);
     fence_proxy_async_smem();
-    const int cn = c + 1;
-    const int slot = cn & 1;
-    if (threadIdx.x == 0) {
-      bool ok = true;
-      if (cn < nchunks && (cn % (T / 32)) == 0) {
-        ok = wait_tile(k0 + cn / (T / 32));
-        __threadfence();
-      }
-      s_ok[slot] = ok;
-    }
     __syncthreads();
     if (threadIdx.x == 0) {
       tc_fence_after();
       issue_chunk(tc, stage, c == 0 && !preloaded);
-      umma_commit(tc.mbar + (g % NST));
-    }
-    tc.g = g + 1;
-    if (!s_ok[slot]) {
-      tc_drain(tc, status);
-      return false;
-    }
-    if (cn < nchunks) {
-      const int kt = k0 + cn / (T / 32);
-      const int kc = (cn % (T / 32)) * 32;
-      load_chunk(Abase + (size_t)kt * T, lda, Bbase + (size_t)kt * T, ldb, kc, ra, rb);
+      umma_commit(tc.empty + s);
+      if (c + NST - 1 < n && !tc_issue(tc, l, c + NST - 1, wait_tile)) bad = true;
     }
   }
-  return tc_drain(tc, status);
+  tc.g = l.base + (uint32_t)n;
+  if (threadIdx.x == 0 && !l.ok) bad = true;
+  const bool any_bad = __syncthreads_or(bad) != 0;
+  if (any_bad && threadIdx.x == 0) {
+    atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
+    atomicExch(status + ST_ABORT, 1);
+  }
+  const bool drained = tc_drain(tc, status);
+  return drained && !any_bad;
 }
 
 // Store the TMEM accumulator, multiplied by `sign` (+1 or -1), into the
@@ -534,7 +597,6 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const int ri = i - nt;
   float* rowbase = is_rhs ? jb.R + (size_t)ri * T * ld : jb.L + (size_t)i * T * ld;
   const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
-  const KernelParams kp = make_kp(jb.sh, jb.theta);
   if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
     // the resident L tile (and, on the diagonal, its inverse) is already the
     // factor: publish it and move on
@@ -543,35 +605,30 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     return;
   }
 
-  // -C_init into the accumulator (before any dependency wait)
-  float* sX = reinterpret_cast<float*>(tc.stages + UNION_BYTES);
-  stage_features<DM>(jb, kp, i, j, sX);
-  __syncthreads();
-  {
-    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int r = (w & 3) * 32 + lane;
-    const int cb = (w >> 2) * 64;
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-      float v[32];
-#pragma unroll
-      for (int q = 0; q < 32; ++q) v[q] = -cinit_entry<DM>(jb, kp, i, j, r, cb + 32 * h + q, sX);
-      tmem_st_32x32(tc.tmem + ((uint32_t)((w & 3) * 32) << 16) + (uint32_t)(cb + 32 * h), v);
-    }
-    tmem_wait_st();
-    tc_fence_before();
-  }
-  __syncthreads();
+  // operand loads of the first k-chunks go out first (thread 0 waits for
+  // their dependencies), then -C_init goes into the accumulator
   const bool have_acc = j > k0;
+  const int* ready = jb.ready;
+  int* status = jb.status;
+  auto wait_tile = [=](int k) {
+    return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
+           wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
+  };
+  const void* rows_map = is_rhs ? jb.tm_R : jb.tm_L;
+  const int row0 = (is_rhs ? ri : i) * T;
+  TcLoad acc_load = tc_load(rows_map, row0, 0, jb.tm_L, j * T, 0, k0, j, tc);
+  if (have_acc && threadIdx.x == 0) {
+    fence_tensormap_acquire(rows_map);
+    fence_tensormap_acquire(jb.tm_L);
+    tc_start(tc, acc_load, wait_tile);
+  }
+  float* sX = reinterpret_cast<float*>(tc.stages + UNION_BYTES);
+  if (!is_rhs || jb.rhs_kind == RHS_CROSS) stage_features<DM>(jb, i, j, sX);
+  __syncthreads();
+  cinit_to_tmem<DM>(jb, i, j, tc.tmem, sX);
+  __syncthreads();
   if (have_acc) {
-    const int* ready = jb.ready;
-    int* status = jb.status;
-    auto wait_tile = [=](int k) {
-      return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
-             wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
-    };
-    if (!tc_accumulate(rowbase, ld, jb.L + (size_t)j * T * ld, ld, k0, j, tc, s_ok, jb.status, wait_tile, true))
-      return;
+    if (!tc_run(tc, acc_load, jb.status, wait_tile, true)) return;
   } else {
     tc_fence_after();
   }
@@ -623,9 +680,16 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
     }
+    fence_proxy_async_global();   // dst is read back by the tensor loads
+    fence_proxy_async_smem();     // sC is overwritten by them
     if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 2)) return;
     auto always = [](int) { return true; };
-    if (!tc_accumulate(dst, ld, Linv_j, T, 0, 1, tc, s_ok, jb.status, always)) return;
+    TcLoad trsm_load = tc_load(rows_map, row0, j * T, jb.tm_Linv, j * T, 0, 0, 1, tc);
+    if (threadIdx.x == 0) {
+      fence_tensormap_acquire(jb.tm_Linv);
+      tc_start(tc, trsm_load, always);
+    }
+    if (!tc_run(tc, trsm_load, jb.status, always, false)) return;
     tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
@@ -656,6 +720,39 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   }
 }
 
+// Block set-up of the tensor-core kernels: 1024-aligned stage buffers in the
+// dynamic shared memory, 2 NST + 1 mbarriers, 128 TMEM columns.
+__device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32_t* s_tmem) {
+  TcCtx tc;
+  const uint32_t base = smem_u32(dsmem);
+  const uint32_t aligned = (base + 1023u) & ~1023u;
+  tc.stages = dsmem + (aligned - base);
+  tc.full = bars;
+  tc.empty = bars + NST;
+  tc.acc = bars + 2 * NST;
+  tc.g = 0;
+  tc.ntask = 0;
+  if (threadIdx.x < 32) {
+    tmem_alloc(s_tmem, 128);
+    tmem_relinquish();
+  }
+  if (threadIdx.x == 0) {
+    for (int k = 0; k < 2 * NST + 1; ++k) mbar_init(bars + k, 1);
+    fence_mbar_init();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  tc.tmem = *s_tmem;
+  return tc;
+}
+
+__device__ __forceinline__ void tc_teardown(const TcCtx& tc) {
+  tc_fence_before();
+  __syncthreads();
+  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+}
+
 template <int DM>
 __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob* __restrict__ jobs,
                                                                     const int4* __restrict__ tasks, int ntasks,
@@ -664,90 +761,53 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
   __shared__ int s_task;
   __shared__ int s_ok[4];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
-  TcCtx tc;
-  {
-    const uint32_t base = smem_u32(dsmem);
-    const uint32_t aligned = (base + 1023u) & ~1023u;
-    tc.stages = dsmem + (aligned - base);
-  }
-  tc.mbar = s_mbar;
-  tc.g = 0;
-  tc.ntask = 0;
-  if (threadIdx.x < 32) {
-    tmem_alloc(&s_tmem, 128);
-    tmem_relinquish();
-  }
-  if (threadIdx.x == 0) {
-    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
-    fence_mbar_init();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  tc.tmem = s_tmem;
+  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   while (true) {
+    fence_proxy_async_smem();   // this task's shared-memory writes before the next task's tensor loads
     __syncthreads();
     if (threadIdx.x == 0) {
       int t = atomicAdd(counter, 1);
-      // a raised abort word ends this block's work (uniformly for the block)
-      if (t < ntasks && ld_relaxed(jobs[tasks[t].x].status + ST_ABORT)) t = ntasks;
+      // tasks of a problem whose abort word is raised are skipped
+      if (t < ntasks && ld_relaxed(jobs[tasks[t].x].status + ST_ABORT)) t = -1;
       s_task = t;
     }
     __syncthreads();
     const int t = s_task;
     if (t >= ntasks) break;
+    if (t < 0) continue;
     const int4 tk = tasks[t];
     const DagJob jb = jobs[tk.x];
     if (jb.active && __ldcg(jb.active) == 0) continue;           // problem has stopped
     if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
     dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
   }
-  tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+  tc_teardown(tc);
 }
 
 // Check kernel: C (128 x 128) = A B^T with A, B 128 x K row-major (K a
-// multiple of 128), through the same 3xTF32 pipeline as the factorisation.
-__global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const float* __restrict__ A,
-                                                                       const float* __restrict__ B, int K,
+// multiple of 128, tensor maps amap / bmap), through the same 3xTF32
+// pipeline as the factorisation.
+__global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const void* amap, const void* bmap, int K,
                                                                        float* __restrict__ C, int* __restrict__ status) {
   extern __shared__ uint8_t dsmem[];
-  __shared__ int s_ok[4];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
-  TcCtx tc;
-  {
-    const uint32_t base = smem_u32(dsmem);
-    const uint32_t aligned = (base + 1023u) & ~1023u;
-    tc.stages = dsmem + (aligned - base);
-  }
-  tc.mbar = s_mbar;
-  tc.g = 0;
-  tc.ntask = 0;
-  if (threadIdx.x < 32) {
-    tmem_alloc(&s_tmem, 128);
-    tmem_relinquish();
-  }
-  if (threadIdx.x == 0) {
-    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
-    fence_mbar_init();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  tc.tmem = s_tmem;
+  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   auto always = [](int) { return true; };
-  if (tc_accumulate(A, K, B, K, 0, K / T, tc, s_ok, status, always)) {
+  TcLoad l = tc_load(amap, 0, 0, bmap, 0, 0, 0, K / T, tc);
+  if (threadIdx.x == 0) {
+    fence_tensormap_acquire(amap);
+    fence_tensormap_acquire(bmap);
+    tc_start(tc, l, always);
+  }
+  if (tc_run(tc, l, status, always, false)) {
     tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) C[e] = sC[(e >> 7) * SC_LD + (e & (T - 1))];
   }
-  tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+  tc_teardown(tc);
 }
 
 __global__ void syrk_zzt_kernel(const Prob* __restrict__ probs, const int4* __restrict__ tiles, int ntiles,
@@ -784,32 +844,12 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
                                                                   int* __restrict__ counter) {
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
-  __shared__ int s_ok[4];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_mbar[NST + 1];
-  TcCtx tc;
-  {
-    const uint32_t base = smem_u32(dsmem);
-    const uint32_t aligned = (base + 1023u) & ~1023u;
-    tc.stages = dsmem + (aligned - base);
-  }
-  tc.mbar = s_mbar;
-  tc.g = 0;
-  tc.ntask = 0;
-  if (threadIdx.x < 32) {
-    tmem_alloc(&s_tmem, 128);
-    tmem_relinquish();
-  }
-  if (threadIdx.x == 0) {
-    for (int k = 0; k <= NST; ++k) mbar_init(s_mbar + k, 1);
-    fence_mbar_init();
-  }
-  tc_fence_before();
-  __syncthreads();
-  tc_fence_after();
-  tc.tmem = s_tmem;
+  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   while (true) {
+    fence_proxy_async_smem();
     __syncthreads();
     if (threadIdx.x == 0) {
       int t = atomicAdd(counter, 1);
@@ -825,11 +865,14 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
     const Prob& P = probs[tl.x];
     const int I = tl.y, J = tl.z;
     const long long ld = P.ld;
-    const float* Z = P.Rz;
     float* Binv = P.Binv;
     auto always = [](int) { return true; };
-    if (!tc_accumulate(Z + (size_t)I * T * ld, ld, Z + (size_t)J * T * ld, ld, I, P.nt, tc, s_ok, P.status, always))
-      break;   // the MMA pipeline timed out: this block stops
+    TcLoad l = tc_load(P.tm_Rz, I * T, 0, P.tm_Rz, J * T, 0, I, P.nt, tc);
+    if (threadIdx.x == 0) {
+      fence_tensormap_acquire(P.tm_Rz);
+      tc_start(tc, l, always);
+    }
+    if (!tc_run(tc, l, P.status, always, false)) continue;   // the problem is aborted
     tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
@@ -838,9 +881,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
       if (I != J) Binv[(size_t)(J * T + r) * ld + I * T + c] = sC[c * SC_LD + r];
     }
   }
-  tc_fence_before();
-  __syncthreads();
-  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+  tc_teardown(tc);
 }
 
 void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* counter, int grid, cudaStream_t st) {
@@ -851,10 +892,22 @@ void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* coun
 }  // namespace pgb
 
 // Internal check entry (not part of the public C-ABI): one 128 x 128 tile
-// product through the tensor-core pipeline.
+// product through the tensor-core pipeline (A, B: 128 x K row-major device
+// arrays).
 extern "C" int pgbx_tc_tile_check(const float* A, const float* B, int K, float* C, int* status, void* stream) {
   if (!A || !B || !C || !status || K <= 0 || K % pgb::T) return PGB_EINVAL;
   pgb::dag_set_attributes();
-  pgb::tc_tile_check_kernel<<<1, pgb::DAG_THREADS, pgb::DAG_SMEM, (cudaStream_t)stream>>>(A, B, K, C, status);
-  return cudaGetLastError() == cudaSuccess ? PGB_OK : PGB_ECUDA;
+  alignas(64) unsigned char maps[2][128];
+  if (!pgb::make_tile_map(maps[0], A, pgb::T, K, K) || !pgb::make_tile_map(maps[1], B, pgb::T, K, K))
+    return PGB_ECUDA;
+  void* dmaps = nullptr;
+  if (cudaMalloc(&dmaps, sizeof(maps)) != cudaSuccess) return PGB_ENOMEM;
+  cudaStream_t s = (cudaStream_t)stream;
+  if (cudaMemcpyAsync(dmaps, maps, sizeof(maps), cudaMemcpyHostToDevice, s) != cudaSuccess) return PGB_ECUDA;
+  pgb::tc_tile_check_kernel<<<1, pgb::DAG_THREADS, pgb::DAG_SMEM, s>>>(dmaps, static_cast<unsigned char*>(dmaps) + 128,
+                                                                       K, C, status);
+  const cudaError_t e = cudaGetLastError();
+  cudaStreamSynchronize(s);
+  cudaFree(dmaps);
+  return e == cudaSuccess ? PGB_OK : PGB_ECUDA;
 }

@@ -13,17 +13,24 @@
 namespace pgb {
 
 // ---------------------------------------------------------------- features
-// eq / matern12: x_d / l_d (mlkernels' stretch divides the inputs);
-// eq_periodic: the raw inputs (the lengthscale is applied after the sine).
+// Row i of the features (zero padded to Dp; rows n .. n_pad all zero):
+//   eq / matern12: x_d / l_d
+//   eq_periodic:   sin(2 pi x_d / p) / l_d, cos(2 pi x_d / p) / l_d at 2d, 2d+1
 __device__ __forceinline__ void prep_point(const Shape& sh, const float* __restrict__ X,
                                            const float* __restrict__ theta, float* __restrict__ Xf, int n, int i) {
-  for (int d = 0; d < sh.Dp; ++d) {
-    float v = 0.0f;
-    if (i < n && d < sh.D) {
-      v = X[(size_t)i * sh.D + d];
-      if (sh.kind != PGB_KERNEL_EQ_PERIODIC) v = v / __ldg(theta + (sh.nl == 1 ? 0 : d));
+  float* out = Xf + (size_t)i * sh.Dp;
+  for (int f = 0; f < sh.Dp; ++f) out[f] = 0.0f;
+  if (i >= n) return;
+  for (int d = 0; d < sh.D; ++d) {
+    const float x = X[(size_t)i * sh.D + d];
+    const float l = __ldg(theta + (sh.nl == 1 ? 0 : d));
+    if (sh.kind == PGB_KERNEL_EQ_PERIODIC) {
+      const float u = 2.0f * x * sh.inv_p;
+      out[2 * d] = sinpif(u) / l;
+      out[2 * d + 1] = cospif(u) / l;
+    } else {
+      out[d] = x / l;
     }
-    Xf[(size_t)i * sh.Dp + d] = v;
   }
 }
 
@@ -51,21 +58,15 @@ void launch_prep_features_raw(const Shape& sh, const float* X, const float* thet
   if (n_pad > 0) prep_features_raw_kernel<<<ceil_div(n_pad, VT), VT, 0, st>>>(sh, X, theta, Xf, n, n_pad);
 }
 
-// Summed scaled squared distance with the feature loop unrolled to DM.
+// Squared feature distance with the feature loop unrolled to DM (>= Dp;
+// features beyond Dp are zero on both sides).
 template <int DM>
-__device__ __forceinline__ float d2_t(const KernelParams& kp, const float* xi, const float* xj) {
+__device__ __forceinline__ float d2_t(const float* xi, const float* xj) {
   float d2 = 0.0f;
 #pragma unroll
-  for (int d = 0; d < DM; ++d) {
-    if (d < kp.D) {
-      if (kp.kind == PGB_KERNEL_EQ_PERIODIC) {
-        const float v = (2.0f * sinpif((xi[d] - xj[d]) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
-        d2 += v * v;
-      } else {
-        const float v = xi[d] - xj[d];
-        d2 += v * v;
-      }
-    }
+  for (int f = 0; f < DM; ++f) {
+    const float v = xi[f] - xj[f];
+    d2 = fmaf(v, v, d2);
   }
   return d2;
 }
@@ -74,18 +75,19 @@ __device__ __forceinline__ float d2_t(const KernelParams& kp, const float* xi, c
 template <int DM>
 __global__ void gram_full_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ X1, int n1,
                                  const float* __restrict__ X2, int n2, float* __restrict__ K, long long ldk) {
-  const KernelParams kp = make_kp(sh, theta);
+  const float s = theta_signal(sh, theta);
+  const int matern = sh.kind == PGB_KERNEL_MATERN12;
   const int j = blockIdx.x * 32 + (threadIdx.x & 31);
   const int i0 = blockIdx.y * 32 + (threadIdx.x >> 5);
   if (j >= n2) return;
   float xj[DM];
 #pragma unroll
-  for (int d = 0; d < DM; ++d) xj[d] = d < sh.Dp ? X2[(size_t)j * sh.Dp + d] : 0.0f;
+  for (int f = 0; f < DM; ++f) xj[f] = f < sh.Dp ? X2[(size_t)j * sh.Dp + f] : 0.0f;
   for (int i = i0; i < min(n1, blockIdx.y * 32 + 32); i += 8) {
     float xi[DM];
 #pragma unroll
-    for (int d = 0; d < DM; ++d) xi[d] = d < sh.Dp ? X1[(size_t)i * sh.Dp + d] : 0.0f;
-    K[(size_t)i * ldk + j] = kernel_from_d2(kp, d2_t<DM>(kp, xi, xj));
+    for (int f = 0; f < DM; ++f) xi[f] = f < sh.Dp ? X1[(size_t)i * sh.Dp + f] : 0.0f;
+    K[(size_t)i * ldk + j] = kernel_of_d2(matern, s, d2_t<DM>(xi, xj));
   }
 }
 
@@ -112,26 +114,14 @@ constexpr int MV_THREADS = 256;
 template <int DM>
 constexpr int mv_rows() { return 128 / DM; }
 
-template <int KIND, int DM>
-__device__ __forceinline__ float kval(const float* xi, const float* xj, int D, float s, float inv_p,
-                                      const float* sl) {
-  float d2 = 0.0f;
-#pragma unroll
-  for (int d = 0; d < DM; ++d) {
-    if (d < D) {
-      float q;
-      if (KIND == PGB_KERNEL_EQ_PERIODIC)
-        q = (2.0f * sinpif((xi[d] - xj[d]) * inv_p)) / sl[d];
-      else
-        q = xi[d] - xj[d];
-      d2 += q * q;
-    }
-  }
-  if (KIND == PGB_KERNEL_MATERN12) return s * expf(-sqrtf(d2));
+template <int MATERN, int DM>
+__device__ __forceinline__ float kval(const float* xi, const float* xj, float s) {
+  const float d2 = d2_t<DM>(xi, xj);
+  if (MATERN) return s * expf(-sqrtf(d2));
   return s * expf(-0.5f * d2);
 }
 
-template <int KIND, int DM, bool HAS_M>
+template <int MATERN, int DM, bool HAS_M>
 __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict__ theta,
                                         const float* __restrict__ Xr, int nr, const float* __restrict__ Xc, int nc,
                                         const float* __restrict__ M, long long ldm, const float* __restrict__ v,
@@ -139,14 +129,11 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
   constexpr int MV_ROWS = mv_rows<DM>();
   __shared__ float sx[MV_ROWS][DM];
   __shared__ float sred[MV_THREADS / 32][MV_ROWS];
-  __shared__ float sl[MAX_D];
-  const int D = sh.D, Dp = sh.Dp;
-  const float sv = __ldg(theta + sh.nl);
-  const float inv_p = sh.inv_p;
-  if (threadIdx.x < MAX_D) sl[threadIdx.x] = threadIdx.x < D ? __ldg(theta + (sh.nl == 1 ? 0 : threadIdx.x)) : 1.0f;
+  const int Dp = sh.Dp;
+  const float sv = theta_signal(sh, theta);
   for (int e = threadIdx.x; e < MV_ROWS * DM; e += MV_THREADS) {
-    const int r = e / DM, d = e % DM;
-    sx[r][d] = (r0 + r < nr && d < Dp) ? Xr[(size_t)(r0 + r) * Dp + d] : 0.0f;
+    const int r = e / DM, f = e % DM;
+    sx[r][f] = (r0 + r < nr && f < Dp) ? Xr[(size_t)(r0 + r) * Dp + f] : 0.0f;
   }
   __syncthreads();
   float acc[MV_ROWS];
@@ -156,12 +143,12 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
   for (int c = threadIdx.x; c < nc; c += MV_THREADS) {
     float xc[DM];
 #pragma unroll
-    for (int d = 0; d < DM; ++d) xc[d] = d < Dp ? __ldg(Xc + (size_t)c * Dp + d) : 0.0f;
+    for (int f = 0; f < DM; ++f) xc[f] = f < Dp ? __ldg(Xc + (size_t)c * Dp + f) : 0.0f;
     const float vc = __ldg(v + c);
     if (rmax == MV_ROWS) {
 #pragma unroll
       for (int r = 0; r < MV_ROWS; ++r) {
-        float k = kval<KIND, DM>(sx[r], xc, D, sv, inv_p, sl);
+        float k = kval<MATERN, DM>(sx[r], xc, sv);
         if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
         acc[r] = fmaf(k, vc, acc[r]);
       }
@@ -169,7 +156,7 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
 #pragma unroll
       for (int r = 0; r < MV_ROWS; ++r) {
         if (r < rmax) {
-          float k = kval<KIND, DM>(sx[r], xc, D, sv, inv_p, sl);
+          float k = kval<MATERN, DM>(sx[r], xc, sv);
           if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
           acc[r] = fmaf(k, vc, acc[r]);
         }
@@ -217,66 +204,64 @@ __device__ __forceinline__ float* prob_field(const Prob& P, int f) {
   }
 }
 
-template <int KIND, int DM, bool HAS_M>
+template <int MATERN, int DM, bool HAS_M>
 __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(const Prob* __restrict__ probs,
                                                                  const int2* __restrict__ mvmap, MatvecOp op) {
   const int2 m = mvmap[blockIdx.x];
   const Prob& P = probs[m.x];
   if (op.only_active && *P.active == 0) return;
   const int n = P.sh.n;
-  mv_core<KIND, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
+  mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
                            prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>());
 }
 
-template <int KIND, int DM>
+template <int MATERN, int DM>
 __global__ void __launch_bounds__(MV_THREADS) gram_matvec_raw_kernel(Shape sh, const float* __restrict__ theta,
                                                                      const float* __restrict__ Xr, int nr,
                                                                      const float* __restrict__ Xc, int nc,
                                                                      const float* __restrict__ v,
                                                                      float* __restrict__ y) {
-  mv_core<KIND, DM, false>(sh, theta, Xr, nr, Xc, nc, nullptr, 0, v, nullptr, y, blockIdx.x * mv_rows<DM>());
+  mv_core<MATERN, DM, false>(sh, theta, Xr, nr, Xc, nc, nullptr, 0, v, nullptr, y, blockIdx.x * mv_rows<DM>());
 }
 
-template <int KIND, int DM>
+template <int MATERN, int DM>
 static void mv_launch(const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
   if (op.use_binv)
-    gram_matvec_kernel<KIND, DM, true><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
+    gram_matvec_kernel<MATERN, DM, true><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
   else
-    gram_matvec_kernel<KIND, DM, false><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
+    gram_matvec_kernel<MATERN, DM, false><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
 }
 
-template <int KIND>
+template <int MATERN>
 static void mv_launch_d(int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
   if (DM <= 4)
-    mv_launch<KIND, 4>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 4>(probs, mvmap, nblocks, op, st);
   else if (DM <= 8)
-    mv_launch<KIND, 8>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 8>(probs, mvmap, nblocks, op, st);
   else
-    mv_launch<KIND, 16>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 16>(probs, mvmap, nblocks, op, st);
 }
 
 void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
                         cudaStream_t st) {
   if (nblocks <= 0) return;
   if (kind == PGB_KERNEL_MATERN12)
-    mv_launch_d<PGB_KERNEL_MATERN12>(DM, probs, mvmap, nblocks, op, st);
-  else if (kind == PGB_KERNEL_EQ_PERIODIC)
-    mv_launch_d<PGB_KERNEL_EQ_PERIODIC>(DM, probs, mvmap, nblocks, op, st);
+    mv_launch_d<1>(DM, probs, mvmap, nblocks, op, st);
   else
-    mv_launch_d<PGB_KERNEL_EQ>(DM, probs, mvmap, nblocks, op, st);
+    mv_launch_d<0>(DM, probs, mvmap, nblocks, op, st);
 }
 
-template <int KIND>
+template <int MATERN>
 static void mv_raw_d(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
                      const float* v, float* y, cudaStream_t st) {
   if (sh.Dp <= 4)
-    gram_matvec_raw_kernel<KIND, 4>
+    gram_matvec_raw_kernel<MATERN, 4>
         <<<ceil_div(nr, mv_rows<4>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
   else if (sh.Dp <= 8)
-    gram_matvec_raw_kernel<KIND, 8>
+    gram_matvec_raw_kernel<MATERN, 8>
         <<<ceil_div(nr, mv_rows<8>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
   else
-    gram_matvec_raw_kernel<KIND, 16>
+    gram_matvec_raw_kernel<MATERN, 16>
         <<<ceil_div(nr, mv_rows<16>()), MV_THREADS, 0, st>>>(sh, theta, Xr, nr, Xc, nc, v, y);
 }
 
@@ -284,11 +269,9 @@ void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr
                             const float* v, float* y, cudaStream_t st) {
   if (nr <= 0) return;
   if (sh.kind == PGB_KERNEL_MATERN12)
-    mv_raw_d<PGB_KERNEL_MATERN12>(sh, theta, Xr, nr, Xc, nc, v, y, st);
-  else if (sh.kind == PGB_KERNEL_EQ_PERIODIC)
-    mv_raw_d<PGB_KERNEL_EQ_PERIODIC>(sh, theta, Xr, nr, Xc, nc, v, y, st);
+    mv_raw_d<1>(sh, theta, Xr, nr, Xc, nc, v, y, st);
   else
-    mv_raw_d<PGB_KERNEL_EQ>(sh, theta, Xr, nr, Xc, nc, v, y, st);
+    mv_raw_d<0>(sh, theta, Xr, nr, Xc, nc, v, y, st);
 }
 
 // ---------------------------------------------------------------- B^-1 matvec
@@ -330,17 +313,21 @@ void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaSt
 //   g_k += sum_{i,j} M_ij dK_k(x_i, x_j),  M = 1/2 R + c a^T,  R = sw B^-1 sw
 // folded to the lower triangle: off-diagonal pairs carry R_ij + c_i a_j +
 // c_j a_i, the diagonal 1/2 R_ii + c_i a_i (only dK/ds is nonzero there).
-// dK/dl_d = K q_d / l_d (Matern12: times 1/r, 0 at r = 0), dK/ds = K / s.
+// With q_d the squared feature distance of input dimension d (feature d, or
+// features 2d and 2d+1 for eq_periodic): dK/dl_d = K q_d / l_d (Matern12:
+// times 1/r, 0 at r = 0), dK/ds = K / s.
 // tiles: (problem, I, J, ordinal of the tile within its problem); each block
 // writes its partial sums (double) to tpart[ordinal * (nl + 1) + k].
-template <int DM>
+template <int DM, bool PER>
 __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict__ probs,
                                                          const int4* __restrict__ tiles) {
+  constexpr int ND = PER ? DM / 2 : DM;   // input dimensions covered
   const int4 tl = tiles[blockIdx.x];
   const Prob& P = probs[tl.x];
   const int I = tl.y, J = tl.z, ord = tl.w;
   const Shape sh = P.sh;
-  const KernelParams kp = make_kp(sh, P.theta);
+  const float sv = theta_signal(sh, P.theta);
+  const int matern = sh.kind == PGB_KERNEL_MATERN12;
   const int NP = sh.nl + 1;
   const int n = sh.n;
   const float* __restrict__ Xf = P.Xf;
@@ -351,11 +338,12 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
   const float* __restrict__ avec = P.a;
   __shared__ float sxc[T][DM];
   __shared__ float ssw[T], sc[T], sa[T];
+  __shared__ float sinvl[MAX_D];
   __shared__ double sred[8][MAX_D + 1];
   for (int e = threadIdx.x; e < T * DM; e += 256) {
-    const int c = e / DM, d = e % DM;
+    const int c = e / DM, f = e % DM;
     const int gc = J * T + c;
-    sxc[c][d] = (gc < n && d < sh.Dp) ? Xf[(size_t)gc * sh.Dp + d] : 0.0f;
+    sxc[c][f] = (gc < n && f < sh.Dp) ? Xf[(size_t)gc * sh.Dp + f] : 0.0f;
   }
   for (int c = threadIdx.x; c < T; c += 256) {
     const int gc = J * T + c;
@@ -363,11 +351,12 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
     sc[c] = gc < n ? cvec[gc] : 0.0f;
     sa[c] = gc < n ? avec[gc] : 0.0f;
   }
+  if (threadIdx.x < MAX_D) sinvl[threadIdx.x] = threadIdx.x < sh.nl ? 1.0f / __ldg(P.theta + threadIdx.x) : 0.0f;
   __syncthreads();
-  float acc[DM];
+  float acc[ND];
   float acc_s = 0.0f;
 #pragma unroll
-  for (int k = 0; k < DM; ++k) acc[k] = 0.0f;
+  for (int k = 0; k < ND; ++k) acc[k] = 0.0f;
   const int c = threadIdx.x & (T - 1);
   const int rh = threadIdx.x >> 7;  // 0 or 1
   const int gc = J * T + c;
@@ -376,7 +365,7 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
     if (gr >= n || gc >= n || gc > gr) continue;
     float xr[DM];
 #pragma unroll
-    for (int d = 0; d < DM; ++d) xr[d] = d < sh.Dp ? __ldg(Xf + (size_t)gr * sh.Dp + d) : 0.0f;
+    for (int f = 0; f < DM; ++f) xr[f] = f < sh.Dp ? __ldg(Xf + (size_t)gr * sh.Dp + f) : 0.0f;
     const float swr = __ldg(sw + gr), cr = __ldg(cvec + gr), ar = __ldg(avec + gr);
     const float bij = __ldcg(Binv + (size_t)gr * ld + gc);
     float m;
@@ -384,41 +373,38 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
       m = 0.5f * swr * bij * swr + cr * ar;
     else
       m = swr * bij * ssw[c] + cr * sa[c] + sc[c] * ar;
-    float q[DM];
+    float q[ND];
     float d2 = 0.0f;
 #pragma unroll
-    for (int d = 0; d < DM; ++d) {
-      q[d] = 0.0f;
-      if (d < sh.D) {
-        float v;
-        if (kp.kind == PGB_KERNEL_EQ_PERIODIC)
-          v = (2.0f * sinpif((xr[d] - sxc[c][d]) * kp.inv_p)) / kp.l[kp.nl == 1 ? 0 : d];
-        else
-          v = xr[d] - sxc[c][d];
-        q[d] = v * v;
-        d2 += q[d];
+    for (int d = 0; d < ND; ++d) {
+      if (PER) {
+        const float u = xr[2 * d] - sxc[c][2 * d], w = xr[2 * d + 1] - sxc[c][2 * d + 1];
+        q[d] = fmaf(u, u, w * w);
+      } else {
+        const float u = xr[d] - sxc[c][d];
+        q[d] = u * u;
       }
+      d2 += q[d];
     }
-    const float K = kernel_from_d2(kp, d2);
+    const float K = kernel_of_d2(matern, sv, d2);
     float scale = K * m;
-    if (kp.kind == PGB_KERNEL_MATERN12) {
+    if (matern) {
       const float rr = sqrtf(d2);
       scale = rr > 0.0f ? scale / rr : 0.0f;
     }
-    if (kp.nl == 1) {
-      acc[0] += scale * d2 * kp.inv_l[0];
+    if (sh.nl == 1) {
+      acc[0] += scale * d2 * sinvl[0];
     } else {
 #pragma unroll
-      for (int d = 0; d < DM; ++d)
-        if (d < sh.D) acc[d] += scale * q[d] * kp.inv_l[d];
+      for (int d = 0; d < ND; ++d) acc[d] += scale * q[d] * sinvl[d];
     }
-    acc_s += K * m / kp.s;
+    acc_s += K * m / sv;
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
 #pragma unroll
-  for (int k = 0; k < DM + 1; ++k) {
+  for (int k = 0; k < ND + 1; ++k) {
     if (k < NP) {
-      const float v = (k == NP - 1) ? acc_s : acc[k < DM ? k : 0];
+      const float v = (k == NP - 1) ? acc_s : acc[k < ND ? k : 0];
       const double s = warp_sum_d((double)v);
       if (lane == 0) sred[warp][k] = s;
     }
@@ -431,14 +417,23 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
   }
 }
 
-void launch_grad_trace(int DM, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st) {
+void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st) {
   if (ntiles <= 0) return;
-  if (DM <= 4)
-    grad_trace_kernel<4><<<ntiles, 256, 0, st>>>(probs, tiles);
-  else if (DM <= 8)
-    grad_trace_kernel<8><<<ntiles, 256, 0, st>>>(probs, tiles);
-  else
-    grad_trace_kernel<16><<<ntiles, 256, 0, st>>>(probs, tiles);
+  if (periodic) {
+    if (DM <= 4)
+      grad_trace_kernel<4, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+    else if (DM <= 8)
+      grad_trace_kernel<8, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+    else
+      grad_trace_kernel<16, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+  } else {
+    if (DM <= 4)
+      grad_trace_kernel<4, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+    else if (DM <= 8)
+      grad_trace_kernel<8, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+    else
+      grad_trace_kernel<16, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+  }
 }
 
 }  // namespace pgb

@@ -59,7 +59,8 @@ int scratch_address(float** out) {
 bool desc_ok(const pgb_desc* d) {
   return d && d->n >= 1 && d->d >= 1 && d->d <= PGB_MAX_D && d->kernel >= PGB_KERNEL_EQ &&
          d->kernel <= PGB_KERNEL_EQ_PERIODIC && (d->n_lengthscales == 1 || d->n_lengthscales == d->d) &&
-         (d->kernel != PGB_KERNEL_EQ_PERIODIC || d->period > 0.0f) && d->flags == 0;
+         (d->kernel != PGB_KERNEL_EQ_PERIODIC || d->period > 0.0f) && d->flags == 0 &&
+         pgb::feature_count(d) <= pgb::MAX_D;
 }
 
 }  // namespace
@@ -68,15 +69,7 @@ extern "C" int pgb_gram_noalloc(const pgb_desc* desc, const float* theta, const 
                                 const float* X2, int32_t n2, float* K, int64_t ldk, void* stream) {
   if (!desc_ok(desc) || !theta || !X1 || !X2 || !K || n1 < 0 || n2 < 0 || ldk < n2) return PGB_EINVAL;
   if (n1 == 0 || n2 == 0) return PGB_OK;
-  pgb::Shape sh;
-  sh.n = desc->n;
-  sh.D = desc->d;
-  sh.Dp = (desc->d + 3) / 4 * 4;
-  sh.kind = desc->kernel;
-  sh.nl = desc->n_lengthscales;
-  sh.lik = desc->likelihood;
-  sh.J = 0;
-  sh.inv_p = desc->kernel == PGB_KERNEL_EQ_PERIODIC ? (float)(1.0 / (double)desc->period) : 0.0f;
+  const pgb::Shape sh = pgb::shape_from_desc(desc);
   const size_t need = ((size_t)n1 + (size_t)n2) * (size_t)sh.Dp;
   if (need > kScratchFloats) {
     std::fprintf(stderr,

@@ -43,6 +43,7 @@ struct Prob {
   double* tpart;      // per-tile trace partials (lower tiles x (MAX_D + 1))
   double* lpart;      // per-block likelihood partials (ceil(n / VT) x (MAX_THETA + 2))
   int* tflags;        // 2 nt flags of the two wavefront solves
+  const void* tm_Rz;  // tensor map of Rz (128 x 32 fp32 boxes, 128-byte swizzle)
 };
 
 // One factorisation job of the tile-DAG kernel (dag.cu).
@@ -77,7 +78,17 @@ struct DagJob {
   // C assembled (after the accumulator is applied)
   unsigned long long* trace;
   unsigned long long* ptrace;   // optional: [nt][16] phase times of the diagonal factorisations
+  // tensor maps (128 x 32 fp32 boxes, 128-byte swizzle) of L, of R and of
+  // Linv (nt*T rows of T), for the tensor-core operand loads
+  const void* tm_L;
+  const void* tm_R;
+  const void* tm_Linv;
 };
+
+// Tensor map of a row-major fp32 matrix (rows x cols, row stride ld floats)
+// with 128-row x 32-column boxes and 128-byte swizzle, the layout the
+// tensor-core operand loads expect.  Host code; false if the driver refuses.
+bool make_tile_map(void* map128, const float* base, long long rows, long long cols, long long ld);
 
 // gram.cu ---------------------------------------------------------------------
 // Features of every problem in the map (vmap: block -> (problem, block)).
@@ -109,8 +120,9 @@ void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr
                             const float* v, float* y, cudaStream_t st);
 // y2 = B^-1 tz, 8 rows per block: bmap block -> (problem, row block)
 void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaStream_t st);
-// trace partials over the lower tiles (problem, I, J, -) of one DM group
-void launch_grad_trace(int DM, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st);
+// trace partials over the lower tiles (problem, I, J, ordinal) of one
+// (DM, periodic) group
+void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st);
 
 // vec.cu ----------------------------------------------------------------------
 void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const void* y, int n, float* logp,

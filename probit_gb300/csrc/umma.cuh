@@ -150,6 +150,42 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* mbar, uint32_t parit
   return true;
 }
 
+// One arrive that also announces `bytes` of transaction count (TMA loads
+// complete the phase when their bytes land).
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)), "r"(bytes)
+               : "memory");
+}
+// Plain arrive (count 1).
+__device__ __forceinline__ void mbar_arrive(uint64_t* mbar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+__device__ __forceinline__ void mbar_inval(uint64_t* mbar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(mbar)) : "memory");
+}
+
+// ---------------------------------------------------------------- TMA
+// 2-D tiled load of the box at (x = column, y = row) of the tensor map into
+// shared memory; completes `bytes` of transaction count on `mbar`.  x * 4
+// bytes must be a multiple of 16 (every caller passes a multiple of 32).
+__device__ __forceinline__ void tma_load_2d(void* dst_smem, const void* tmap, int x, int y, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::
+          "r"(smem_u32(dst_smem)),
+      "l"(tmap), "r"(x), "r"(y), "r"(smem_u32(mbar))
+      : "memory");
+}
+// A tensor map written to global memory by ordinary stores (or copied there
+// from the host) is made visible to the tensor-copy unit by this fence.
+__device__ __forceinline__ void fence_tensormap_acquire(const void* tmap) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;" ::"l"(tmap) : "memory");
+}
+// Order this thread's earlier generic-proxy global accesses (and those it
+// acquired from other threads) before its later async-proxy (TMA) accesses.
+__device__ __forceinline__ void fence_proxy_async_global() {
+  asm volatile("fence.proxy.async.global;" ::: "memory");
+}
+
 // ---------------------------------------------------------------- 3xTF32 split
 // Round to the nearest TF32 value (10 explicit mantissa bits, ties away from
 // zero); the result is an fp32 bit pattern whose 13 low mantissa bits are 0.

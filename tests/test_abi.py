@@ -40,6 +40,11 @@ def test_theta_size_and_validation(native_lib):
         assert native_lib.pgb_theta_size(e) == N.PGB_EINVAL, field
     e = N.Desc(100, 1, N.KERNEL_EQ_PERIODIC, 1, 0.0, N.LIK_GAUSSIAN, 0, 1e-5, 100, 0)
     assert native_lib.pgb_theta_size(e) == N.PGB_EINVAL
+    # the periodic kernel uses two features (sin, cos) per input dimension
+    e = N.Desc(100, 9, N.KERNEL_EQ_PERIODIC, 1, 0.5, N.LIK_GAUSSIAN, 0, 1e-5, 100, 0)
+    assert native_lib.pgb_theta_size(e) == N.PGB_EUNSUPPORTED
+    e.d = 8
+    assert native_lib.pgb_theta_size(e) == 3
 
 
 def test_strerror_and_version(native_lib):
