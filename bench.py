@@ -35,6 +35,12 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Laplace evidence+grad solves/s"
+# dram__bytes_read.sum + dram__bytes_write.sum of one N = 8192 factorisation
+# launch (ncu capture summarised in profiles/dag_factor_kernel_gaussian_N8192.md)
+FACTOR_TRAFFIC_N8192 = 73.197312e6 + 114.800384e6
+# nominal dense TF32 tensor rate of a GB300 (TFLOP/s); a 3xTF32 product issues
+# three TF32 MMAs per algorithmic one
+TF32_NOMINAL_TFLOPS = 1100.0
 UNIT = "solves/s"
 TOL = 1.0
 CONFIG_NAME = "gaussian_eq_ard_N8192_D4_evidence_grad"
@@ -49,6 +55,10 @@ def parse():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--predict-m", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=1024,
+                    help="problems of the batched ordinal workload reported beside the headline (0: skip)")
+    ap.add_argument("--batch-tol", type=float, default=1e-3)
+    ap.add_argument("--no-plain", action="store_true", help="skip the plain one-call-per-problem comparison")
     return ap.parse_args()
 
 
@@ -194,6 +204,161 @@ def cpu_baseline(args):
                       f"algorithm, float32, OpenBLAS on all host threads): {dt:.1f} s"}
 
 
+# ---------------------------------------------------------------- batched workload
+def launches_per_solve(iters, trace_groups=1, matvec_groups=1):
+    """Kernels one evidence + gradient solve launches (each covers every problem of a batch)."""
+    newton = matvec_groups + 1 + 2 + 1 + 1 + 2 + 1 + 2      # f = K a .. finalize + loop condition
+    epilogue = 1 + matvec_groups + 1 + 2 + 1 + 1 + 2        # activate, precision, reuse, factor, evidence
+    grad = 1 + matvec_groups + 1 + matvec_groups + 1 + 1 + 1 + trace_groups + 2
+    return 2 + newton * iters + epilogue + grad
+
+
+def run_batched(args, dev):
+    """The batched ordinal workload: B problems of uneven N, D, J and kernel in
+    one batch, against the plain path (one single-GP call per problem)."""
+    import ctypes as C
+
+    import torch
+
+    import probit_gb300 as pg
+    from probit_gb300 import _native as N
+    from probit_gb300 import workloads as Wk
+
+    B = args.batch
+    t0 = time.perf_counter()
+    probs = Wk.batched_c2(B=B, device=dev)
+    gen_s = time.perf_counter() - t0
+    tol = args.batch_tol
+    gps = [pg.LaplaceGP((q.X, q.y), q.prior(), pg.log_probit_likelihood, tolerance=tol) for q in probs]
+    params = [q.params() for q in probs]
+    batch = pg.LaplaceBatch(gps, params)
+    _, theta = batch.pack_theta(params)
+    td = theta.to(dev, torch.float32)
+    stream = torch.cuda.current_stream(dev)
+    for _ in range(max(3, args.warmup)):
+        batch.value_and_grad_flat(td)
+    torch.cuda.synchronize()
+    st = batch.status()
+    iters = np.array([x[1] for x in st])
+    flush = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    reps = max(1, min(args.steps, 5))
+    ms = []
+    for _ in range(reps):
+        flush.zero_()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        batch.value_and_grad_flat(td)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    batched_ms = statistics.median(ms)
+    # end to end through LaplaceBatch: packed host inputs uploaded, values and gradients read back
+    Xp, yp = batch.pack_data([(q.X, q.y) for q in probs])
+    Xh, yh = torch.from_numpy(Xp).pin_memory(), torch.from_numpy(yp).pin_memory()
+    th_h = theta.to(torch.float32).pin_memory()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        batch.set_data(packed=(Xh, yh))
+        v, g = batch.value_and_grad_flat(th_h)
+        v.cpu(), g.cpu()
+    torch.cuda.synchronize()
+    e2e_s = (time.perf_counter() - t0) / reps
+    Ns = np.array([q.N for q in probs], dtype=np.float64)
+    cpu = None if args.no_cpu_baseline else batched_cpu_baseline(probs, tol)
+    out = {
+        "workload": f"ordinal_batch_B{B}_N32-4096", "B": B, "tolerance": tol,
+        "config": "N log-uniform [32,4096], D in {1,2,4,8}, J in 2..7, kernel in {EQ, Matern12, EQ.periodic(0.5)}, "
+                  "l ~ LogU[0.3,3], s ~ LogU[0.5,2], noise std sqrt(0.4), seed 2",
+        "value": B / (batched_ms / 1e3), "unit": UNIT, "ms_per_batch": batched_ms,
+        "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(Xp.nbytes + yp.nbytes + 4 * theta.numel()),
+                "d2h_bytes_per_step": int(4 * (B + theta.numel()))},
+        "newton_iterations": {"mean": float(iters.mean()), "max": int(iters.max()),
+                              "at_maxiter": int((iters >= 100).sum())},
+        "algorithmic_tflop": float((Ns ** 3 / 3).sum() * (iters.mean() + 3) / 1e12),
+        "gpu_launches_per_batch": launches_per_solve(int(iters.max()), *kernel_groups(probs)),
+        "data_generation_s": gen_s,
+    }
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
+    if args.no_plain:
+        return out
+    # plain path: one single-GP value_and_grad per problem (handles and graphs prepared first)
+    lib = N.load()
+    handles, Xs, ys, ths = [], [], [], []
+    for b, q in enumerate(probs):
+        h = C.c_void_p()
+        N.check(lib.pgb_gp_create(batch.descs[b], C.byref(h)), "pgb_gp_create")
+        handles.append(h)
+        Xs.append(torch.from_numpy(q.X).to(dev))
+        ys.append(torch.from_numpy(q.y).to(dev))
+        ths.append(td[int(batch.theta_off[b]):int(batch.theta_off[b + 1])].contiguous())
+    vals = torch.empty(B, dtype=torch.float32, device=dev)
+    grads = torch.empty(int(batch.theta_off[-1]), dtype=torch.float32, device=dev)
+    sh = stream.cuda_stream
+
+    def plain():
+        for b in range(B):
+            N.check(lib.pgb_value_and_grad(handles[b], Xs[b].data_ptr(), ys[b].data_ptr(), ths[b].data_ptr(),
+                                           vals[b:].data_ptr(), grads[int(batch.theta_off[b]):].data_ptr(), sh),
+                    "pgb_value_and_grad")
+
+    plain()
+    torch.cuda.synchronize()
+    same = bool(torch.equal(vals, batch.value_and_grad_flat(td)[0]))
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plain()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    for h in handles:
+        lib.pgb_gp_destroy(h)
+    out["plain"] = {"value": B / (plain_ms / 1e3), "unit": UNIT, "ms_per_batch": plain_ms,
+                    "what": "one pgb_value_and_grad (CUDA graph) per problem, same kernels, no host sync between"}
+    out["batched_over_plain"] = plain_ms / batched_ms
+    out["results_identical_to_plain"] = same
+    return out
+
+
+def batched_cpu_baseline(probs, tol, nsample=12):
+    """The oracle (the reference algorithm in NumPy/SciPy, float32, all host
+    threads) on problems at evenly spaced quantiles of N, extrapolated to the
+    whole batch with a power law t(N) fitted in log-log."""
+    from oracle import laplace as L
+
+    order = np.argsort([q.N for q in probs])
+    pick = [int(order[int(round(k))]) for k in np.linspace(0, len(probs) - 1, nsample)]
+    Ns, ts = [], []
+    t_all = time.perf_counter()
+    for b in pick:
+        q = probs[b]
+        op = L.Problem(q.X, q.y, q.kernel, "probit", 1, q.period, q.J)
+        t0 = time.perf_counter()
+        L.value_and_grad(op, q.theta().astype(np.float32), tol=tol, dtype=np.float32)
+        ts.append(time.perf_counter() - t0)
+        Ns.append(q.N)
+    coef = np.polyfit(np.log(Ns), np.log(ts), 1)
+    total = float(np.exp(np.polyval(coef, np.log([q.N for q in probs]))).sum())
+    return {"value": len(probs) / total, "unit": UNIT, "cores": len(os.sched_getaffinity(0)), "kind": "port",
+            "sample": f"{nsample} problems at N quantiles {sorted(Ns)} timed with the NumPy/SciPy restatement of "
+                      f"the reference algorithm (float32, OpenBLAS on all host threads) in "
+                      f"{time.perf_counter() - t_all:.1f} s; extrapolated to all {len(probs)} problems with "
+                      f"t ~ N^{coef[0]:.2f}"}
+
+
+def kernel_groups(probs):
+    """(gradient-trace launches, Gram-matvec launches) of a batch: one per
+    (feature width class, periodic) and per (kernel, feature width class)."""
+    def dm(q):
+        F = 2 * q.D if q.kernel == "eq_periodic" else q.D
+        Dp = (F + 3) // 4 * 4
+        return 4 if Dp <= 4 else (8 if Dp <= 8 else 16)
+    trace = {(dm(q), q.kernel == "eq_periodic") for q in probs}
+    mv = {(dm(q), q.kernel) for q in probs}
+    return len(trace), len(mv)
+
+
 # ---------------------------------------------------------------- GB300 arm
 def run_gb300(args, ws, rank, local):
     import ctypes as C
@@ -311,7 +476,7 @@ def run_gb300(args, ws, rank, local):
         pf = float(n) * n * args.predict_m
         pred = {"M": args.predict_m, "ms": min(times), "tflops_algorithmic": pf / (min(times) / 1e3) / 1e12}
 
-    launches_per_step = 2 + 7 * iters + 2 + 1 + 2 + 11
+    launches_per_step = launches_per_solve(iters)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -322,7 +487,9 @@ def run_gb300(args, ws, rank, local):
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"kernel": "dag_factor_kernel (Cholesky of B, N^3/3 flop)", "bound": "tensor",
                      "achieved": achieved_tf, "peak": peak_tf, "unit": "TFLOP/s", "frac": achieved_tf / peak_tf,
-                     "peak_kind": f"{pk_kind} bf16 dense", "launch_ms": f_ms, "traffic": None},
+                     "peak_kind": f"{pk_kind} bf16 dense", "launch_ms": f_ms,
+                     "traffic": FACTOR_TRAFFIC_N8192 if n == 8192 else None,
+                     "frac_of_3xtf32_nominal": achieved_tf / (TF32_NOMINAL_TFLOPS / 3.0)},
         "clocks": clocks,
         "gpu_launches": launches_per_step * args.steps,
         "predict": pred,
@@ -330,6 +497,9 @@ def run_gb300(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     lib.pgb_gp_destroy(h)
+    del flush
+    if rank == 0 and ws == 1 and args.batch > 0:
+        line["batched"] = run_batched(args, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

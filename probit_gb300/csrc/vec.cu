@@ -346,36 +346,42 @@ __global__ void grad_lik_kernel(const Prob* __restrict__ probs, const int2* __re
 
 // One block per problem: the theta gradient from the trace partials (nl + 1
 // prior slots, one row per lower tile) and the likelihood partials (1 + J+1
-// slots, one row per vmap block).  Infinite cutpoints get 0.
-__global__ void grad_final_kernel(const Prob* __restrict__ probs) {
+// slots, one row per vmap block), each slot reduced by the whole block in a
+// fixed order.  Infinite cutpoints get 0.
+constexpr int FINAL_THREADS = 256;
+__global__ void __launch_bounds__(FINAL_THREADS) grad_final_kernel(const Prob* __restrict__ probs) {
+  __shared__ double sred[FINAL_THREADS / 32];
   const Prob& P = probs[blockIdx.x];
   const Shape sh = P.sh;
   const int NP = sh.nl + 1;
   const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
   const int ntp = P.nt * (P.nt + 1) / 2;
   const int nlp = ceil_div(P.n_pad, VT);
-  for (int k = threadIdx.x; k < NP + nslots; k += blockDim.x) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int k = 0; k < NP + nslots; ++k) {
+    double s = 0.0;
     if (k < NP) {
-      double s = 0.0;
-      for (int b = 0; b < ntp; ++b) s += P.tpart[(size_t)b * NP + k];
-      P.grad[k] = (float)s;
+      for (int b = threadIdx.x; b < ntp; b += FINAL_THREADS) s += P.tpart[(size_t)b * NP + k];
     } else {
-      const int slot = k - NP;
-      double s = 0.0;
-      for (int b = 0; b < nlp; ++b) s += P.lpart[(size_t)b * nslots + slot];
-      if (slot >= 1) {
-        const float bv = P.theta[sh.nl + 2 + slot - 1];
-        if (!isfinite(bv)) s = 0.0;
-      }
-      P.grad[NP + slot] = (float)s;
+      for (int b = threadIdx.x; b < nlp; b += FINAL_THREADS) s += P.lpart[(size_t)b * nslots + (k - NP)];
     }
+    s = warp_sum_d(s);
+    if (lane == 0) sred[warp] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < FINAL_THREADS / 32; ++w) t += sred[w];
+      if (k >= NP && k - NP >= 1 && !isfinite(P.theta[sh.nl + 2 + (k - NP) - 1])) t = 0.0;
+      P.grad[k] = (float)t;
+    }
+    __syncthreads();
   }
 }
 
 void launch_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
   if (nblocks <= 0) return;
   grad_lik_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-  grad_final_kernel<<<nprob, 64, 0, st>>>(probs);
+  grad_final_kernel<<<nprob, FINAL_THREADS, 0, st>>>(probs);
 }
 
 // ---------------------------------------------------------------- predict

@@ -154,7 +154,16 @@ def draw_latent(rng, kernel, X, ell, s, period=0.5, jitter=1e-6, device=None):
     """
     if X.shape[0] > 1024 and device is not None:
         z = rng.standard_normal(X.shape[0])
-        return _draw_latent_torch(kernel, X, ell, s, period, jitter, z, device)
+        try:
+            return _draw_latent_torch(kernel, X, ell, s, period, jitter, z, device)
+        except RuntimeError:
+            # torch's linear-algebra library can be unavailable (e.g. under a
+            # profiler that changes the library search path): same draw on the host
+            import scipy.linalg as sla
+
+            K = gram64_gemm(kernel, X, ell, s, period)
+            K[np.diag_indices_from(K)] += jitter
+            return sla.cholesky(K, lower=True, check_finite=False) @ z
     if X.shape[0] > 1024:
         import scipy.linalg as sla
 
