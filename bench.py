@@ -59,6 +59,9 @@ def parse():
                     help="problems of the batched ordinal workload reported beside the headline (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-3)
     ap.add_argument("--no-plain", action="store_true", help="skip the plain one-call-per-problem comparison")
+    ap.add_argument("--hyperopt", type=int, default=256,
+                    help="problems of the lockstep L-BFGS hyperparameter workload (0: skip)")
+    ap.add_argument("--hyperopt-steps", type=int, default=50)
     return ap.parse_args()
 
 
@@ -347,6 +350,99 @@ def batched_cpu_baseline(probs, tol, nsample=12):
                       f"t ~ N^{coef[0]:.2f}"}
 
 
+def run_hyperopt(args, dev):
+    """The hyperparameter-optimisation workload: B ordinal GPs (N uniform in
+    [256, 2048], D = 3, J = 5, Matern12) each fitted by lockstep L-BFGS on
+    (log l, log s, log sigma, interior cutpoints); every evaluation round is
+    one batched evidence + gradient call."""
+    import ctypes as C
+
+    import torch
+
+    import probit_gb300 as pg
+    from probit_gb300 import _native as N
+    from probit_gb300 import workloads as Wk
+    from probit_gb300.optimize import LogParams, batch_objective, minimize_lockstep
+
+    B = args.hyperopt
+    probs = Wk.hyperopt_c3(B=B, device=dev)
+    tol = args.batch_tol
+    gps = [pg.LaplaceGP((q.X, q.y), q.prior(), pg.log_probit_likelihood, tolerance=tol) for q in probs]
+    params = [q.params() for q in probs]
+    batch = pg.LaplaceBatch(gps, params)
+    lp = LogParams(nl=1, J=5)
+    rng = np.random.default_rng(30)
+    u0 = np.stack([lp.from_theta(q.theta()[None])[0] for q in probs])
+    u0[:, :3] += rng.normal(0.0, 0.5, size=(B, 3))          # log l, log s, log sigma away from the truth
+    u0[:, 3:] *= rng.uniform(0.7, 1.3, size=(B, 1))          # cutpoints scaled, still ordered
+    fg = batch_objective(batch, lp)
+    for _ in range(max(3, args.warmup)):
+        fg(u0)
+    torch.cuda.synchronize()
+    f0, _ = fg(u0)
+    t0 = time.perf_counter()
+    res = minimize_lockstep(fg, u0, maxiter=args.hyperopt_steps)
+    wall = time.perf_counter() - t0
+    evals = res.evaluations
+    st = batch.status()
+    out = {
+        "workload": f"hyperopt_B{B}_N256-2048_D3_J5_matern12", "B": B, "lbfgs_steps": args.hyperopt_steps,
+        "tolerance": tol, "evaluations": evals, "wall_s": wall,
+        "value": B * evals / wall, "unit": UNIT,
+        "what": "end to end: host L-BFGS (vectorised over problems) + one batched value_and_grad per round, "
+                "theta up and values + gradients down every round",
+        "objective_mean": {"start": float(np.mean(f0)), "end": float(np.mean(res.f))},
+        "accepted_steps_mean": float(res.iterations.mean()),
+        "problems_failed": int(sum(1 for x in st if x[0] != 0)),
+    }
+    # plain path: one single-GP value_and_grad per problem for one round at the final point
+    theta = torch.from_numpy(lp.to_theta(res.x).astype(np.float32).reshape(-1)).to(dev)
+    lib = N.load()
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+    handles, Xs, ys = [], [], []
+    for b, q in enumerate(probs):
+        h = C.c_void_p()
+        N.check(lib.pgb_gp_create(batch.descs[b], C.byref(h)), "pgb_gp_create")
+        handles.append(h)
+        Xs.append(torch.from_numpy(q.X).to(dev))
+        ys.append(torch.from_numpy(q.y).to(dev))
+    vals = torch.empty(B, dtype=torch.float32, device=dev)
+    grads = torch.empty(theta.numel(), dtype=torch.float32, device=dev)
+    off = batch.theta_off
+
+    def plain():
+        for b in range(B):
+            N.check(lib.pgb_value_and_grad(handles[b], Xs[b].data_ptr(), ys[b].data_ptr(),
+                                           theta[int(off[b]):].data_ptr(), vals[b:].data_ptr(),
+                                           grads[int(off[b]):].data_ptr(), sh), "pgb_value_and_grad")
+
+    plain()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    plain()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = e0.elapsed_time(e1)
+    e0.record(stream)
+    batch.value_and_grad_flat(theta)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = e0.elapsed_time(e1)
+    for h in handles:
+        lib.pgb_gp_destroy(h)
+    out["batched_round_ms"] = batched_ms
+    out["plain"] = {"value": B / (plain_ms / 1e3), "unit": UNIT, "round_ms": plain_ms,
+                    "what": "one pgb_value_and_grad per problem per evaluation round (device time)"}
+    out["batched_over_plain"] = plain_ms / batched_ms
+    if not args.no_cpu_baseline:
+        cpu = batched_cpu_baseline(probs, tol, nsample=8)
+        out["cpu_baseline"] = cpu
+        out["e2e_over_cpu"] = out["value"] / cpu["value"]
+    return out
+
+
 def kernel_groups(probs):
     """(gradient-trace launches, Gram-matvec launches) of a batch: one per
     (feature width class, periodic) and per (kernel, feature width class)."""
@@ -500,6 +596,8 @@ def run_gb300(args, ws, rank, local):
     del flush
     if rank == 0 and ws == 1 and args.batch > 0:
         line["batched"] = run_batched(args, dev)
+    if rank == 0 and ws == 1 and args.hyperopt > 0:
+        line["hyperopt"] = run_hyperopt(args, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -216,6 +216,14 @@ int pgb_batch_value_and_grad(pgb_batch* b, const float* X, const void* y,
                              const float* theta, float* values, float* grads,
                              void* stream);
 
+/* Which problems the following evaluations compute (device int32 array of
+ * count entries, 0 = skip; all are enabled after pgb_batch_create).  A
+ * skipped problem's values, gradients and status words keep what its last
+ * evaluation wrote, and it costs (almost) nothing: an optimiser can
+ * re-evaluate only the problems whose line search is still running.  This
+ * entry point has no counterpart in the reference. */
+int pgb_batch_set_enabled(pgb_batch* b, const int32_t* enabled, void* stream);
+
 /* Per-problem status words (host array of count entries); synchronises
  * `stream` first. */
 int pgb_batch_status(pgb_batch* b, pgb_status* out, void* stream);

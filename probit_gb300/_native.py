@@ -95,6 +95,7 @@ _SIGS = {
     "pgb_batch_layout": (C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
     "pgb_batch_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_batch_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_batch_set_enabled": (C.c_int, [_VP, _VP, _VP]),
     "pgb_batch_status": (C.c_int, [_VP, C.POINTER(Status), _VP]),
 }
 

@@ -106,6 +106,18 @@ class LaplaceBatch:
         return thetas, torch.cat([t.detach() for t in thetas])
 
     # -- evaluation ---------------------------------------------------------------
+    def set_enabled(self, mask=None, stream=None):
+        """Evaluate only the problems where `mask` is true (None: all).  The
+        others keep the values and gradients of their last evaluation."""
+        import torch
+
+        m = np.ones(self.B, dtype=np.int32) if mask is None else np.asarray(mask, dtype=bool).astype(np.int32)
+        if m.shape != (self.B,):
+            raise ValueError(f"mask must have {self.B} entries")
+        self._enabled = torch.from_numpy(m).to(self.device)
+        s = stream if stream is not None else stream_handle(self.device)
+        N.check(self.lib.pgb_batch_set_enabled(self.h, self._enabled.data_ptr(), s), "pgb_batch_set_enabled")
+
     def value_and_grad_flat(self, theta_packed, stream=None):
         """(values (B,), grads (packed like theta)) as CUDA tensors; enqueued on the stream."""
         import torch

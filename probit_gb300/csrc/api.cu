@@ -104,6 +104,7 @@ struct Engine {
   float* grad_all = nullptr;
   int* status_all = nullptr;
   int* active_all = nullptr;
+  int* enabled_all = nullptr;
   int* reuse_all = nullptr;
   int* counters = nullptr;
   int* any_active = nullptr;
@@ -266,6 +267,7 @@ size_t layout(Engine& e, uintptr_t base) {
   e.grad_all = b.take<float>(e.th_total);
   e.status_all = b.take<int>((size_t)np * kStatusWords);
   e.active_all = b.take<int>(np);
+  e.enabled_all = b.take<int>(np);
   e.reuse_all = b.take<int>((size_t)np * 4);
   e.counters = b.take<int>(C_COUNT);
   e.any_active = b.take<int>(2);
@@ -313,6 +315,7 @@ size_t layout(Engine& e, uintptr_t base) {
     q.grad = e.grad_all + e.th_off[p];
     q.status = e.status_all + (size_t)p * kStatusWords;
     q.active = e.active_all + p;
+    q.enabled = e.enabled_all + p;
     q.reuse = e.reuse_all + (size_t)p * 4;
     q.tflags = e.tflags_all + tflags_off;
     tflags_off += 2 * (size_t)nt;
@@ -351,8 +354,10 @@ size_t layout(Engine& e, uintptr_t base) {
     jb[JOB_VEC].tm_R = map_slot(e, p, MAP_RV);
     jb[JOB_NONE].rhs_kind = RHS_NONE;
     jb[JOB_NONE].reuse_mode = 1;
+    jb[JOB_NONE].active = q.active;
     jb[JOB_IDENT].rhs_kind = RHS_IDENT;
     jb[JOB_IDENT].reuse_mode = 1;
+    jb[JOB_IDENT].active = q.active;
     jb[JOB_IDENT].nrt = nt;
     jb[JOB_IDENT].nrhs = (int)npad;
     jb[JOB_IDENT].tm_R = q.tm_Rz;
@@ -507,6 +512,10 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   }
   layout(e, reinterpret_cast<uintptr_t>(e.arena));
   CU_TRY(cudaMemset(e.arena, 0, bytes));
+  {
+    const std::vector<int> ones(count, 1);
+    PGB_TRY(upload(e.enabled_all, ones));
+  }
   PGB_TRY(upload(e.vmap, e.h_vmap));
   PGB_TRY(upload(e.bmap, e.h_bmap));
   PGB_TRY(upload(e.claims, e.h_claims));
@@ -600,7 +609,7 @@ void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, in
 }
 
 void enq_precision(Engine& e, cudaStream_t s) {
-  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 0}, s);
+  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);
   launch_lik_full(e.probs, e.vmap, e.nvb, s);
 }
 
@@ -608,10 +617,10 @@ void enq_grad(Engine& e, cudaStream_t s) {
   cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
   launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);
   // rowdot_i = sum_j B^-1_ij K_ij sw_j  ->  diag(Sigma)_i = rowdot_i / sw_i
-  enq_matvec(e, MatvecOp{F_SW, F_NONE, F_ROWDOT, 1, 0}, s);
+  enq_matvec(e, MatvecOp{F_SW, F_NONE, F_ROWDOT, 1, 1}, s);
   launch_grad_vec1(e.probs, e.vmap, e.nvb, s);
   // zbar = K (a - d1 - s)
-  enq_matvec(e, MatvecOp{F_RV, F_NONE, F_ZBAR, 0, 0}, s);
+  enq_matvec(e, MatvecOp{F_RV, F_NONE, F_ZBAR, 0, 1}, s);
   // u = (I + K W)^-1 zbar = W^-1/2 B^-1 W^1/2 zbar
   launch_scale_tz(e.probs, e.vmap, e.nvb, s);
   launch_binv_matvec(e.probs, e.bmap, e.nbb, s);
@@ -627,7 +636,7 @@ void enq_prologue(Engine& e, cudaStream_t s) {
 
 void enq_epilogue(Engine& e, int op, cudaStream_t s) {
   if (op >= OP_POSTERIOR) {
-    launch_set_active(e.probs, e.nprob, 1, s);   // every problem takes part from here on
+    launch_activate_enabled(e.probs, e.nprob, s);   // every enabled problem takes part from here on
     enq_precision(e, s);
     launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
     enq_dag(e, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
@@ -853,6 +862,7 @@ int pgb_precision(pgb_gp* gp, const float* X, const void* y, const float* theta,
   CU_TRY(cudaMemsetAsync(q.a, 0, sizeof(float) * q.n_pad, s));
   CU_TRY(cudaMemcpyAsync(q.a, a, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
   launch_prep_features(e.probs, e.vmap, e.nvb, s);
+  launch_activate_enabled(e.probs, e.nprob, s);
   enq_precision(e, s);
   if (W_out) CU_TRY(cudaMemcpyAsync(W_out, q.W, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
   if (f_out) CU_TRY(cudaMemcpyAsync(f_out, q.f, sizeof(float) * q.sh.n, cudaMemcpyDeviceToDevice, s));
@@ -904,6 +914,7 @@ int pgb_factor(pgb_gp* gp, void* stream) {
   cudaStream_t s = (cudaStream_t)stream;
   Engine& e = gp->e;
   CU_TRY(cudaMemsetAsync(e.hp[0].reuse + 2, 0, sizeof(int), s));   // always a full factorisation
+  launch_activate_enabled(e.probs, e.nprob, s);
   enq_dag(e, JOB_NONE, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
@@ -1053,6 +1064,13 @@ int pgb_batch_value_and_grad(pgb_batch* b, const float* X, const void* y, const 
   PGB_TRY(run_op(e, OP_VG, s));
   CU_TRY(cudaMemcpyAsync(values, e.value_all, sizeof(float) * e.nprob, cudaMemcpyDeviceToDevice, s));
   CU_TRY(cudaMemcpyAsync(grads, e.grad_all, sizeof(float) * e.th_total, cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_batch_set_enabled(pgb_batch* b, const int32_t* enabled, void* stream) {
+  if (!b || !enabled) return PGB_EINVAL;
+  CU_TRY(cudaMemcpyAsync(b->e.enabled_all, enabled, sizeof(int32_t) * b->e.nprob, cudaMemcpyDeviceToDevice,
+                         (cudaStream_t)stream));
   return PGB_OK;
 }
 

@@ -853,8 +853,8 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
     __syncthreads();
     if (threadIdx.x == 0) {
       int t = atomicAdd(counter, 1);
-      // an aborted problem's tiles are skipped (uniformly for the block)
-      if (t < ntiles && ld_relaxed(probs[tiles[t].x].status + ST_ABORT)) t = -1;
+      // tiles of aborted or inactive problems are skipped (uniformly for the block)
+      if (t < ntiles && (ld_relaxed(probs[tiles[t].x].status + ST_ABORT) || *probs[tiles[t].x].active == 0)) t = -1;
       s_task = t;
     }
     __syncthreads();

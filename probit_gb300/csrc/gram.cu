@@ -37,6 +37,7 @@ __device__ __forceinline__ void prep_point(const Shape& sh, const float* __restr
 __global__ void prep_features_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.enabled == 0) return;
   const int i = m.y * VT + threadIdx.x;
   if (i >= P.n_pad) return;
   prep_point(P.sh, P.X, P.theta, P.Xf, P.sh.n, i);
@@ -281,6 +282,7 @@ __global__ void __launch_bounds__(256) binv_matvec_kernel(const Prob* __restrict
                                                           const int2* __restrict__ bmap) {
   const int2 m = bmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int r = m.y * 8 + warp;
   const int n = P.sh.n;
@@ -324,6 +326,7 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
   constexpr int ND = PER ? DM / 2 : DM;   // input dimensions covered
   const int4 tl = tiles[blockIdx.x];
   const Prob& P = probs[tl.x];
+  if (*P.active == 0) return;
   const int I = tl.y, J = tl.z, ord = tl.w;
   const Shape sh = P.sh;
   const float sv = theta_signal(sh, P.theta);

@@ -37,7 +37,9 @@ struct Prob {
   float* value;       // negative log evidence
   float* grad;        // theta-sized gradient
   int* status;        // 8 status words
-  int* active;        // 1 while the Newton loop of this problem runs
+  int* active;        // 1 while this problem takes part in the current phase
+                      // (Newton loop: until it stops; later phases: = *enabled)
+  const int* enabled; // 0: the problem is skipped by every kernel (outputs kept)
   int* reuse;         // [0] factor valid, [1] W differs, [2] reuse decision
   double* part;       // per-block partial sums (ceil(n_pad / VT))
   double* tpart;      // per-tile trace partials (lower tiles x (MAX_D + 1))
@@ -148,10 +150,11 @@ void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st)
 // factor reuse per active problem: differs |= any(sw != sw_prev); decide
 void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st);
-// status words, reuse flags, active = 1 and (zero_a) a = 0
+// enabled problems: status words, reuse flags, active = 1 and (zero_a)
+// a = 0; disabled problems: active = 0, nothing else touched
 void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int zero_a, cudaStream_t st);
-// active = v for every problem
-void launch_set_active(const Prob* probs, int nprob, int v, cudaStream_t st);
+// active = enabled for every problem (the phases after the Newton loop)
+void launch_activate_enabled(const Prob* probs, int nprob, cudaStream_t st);
 
 // dag.cu ----------------------------------------------------------------------
 void dag_set_attributes();

@@ -50,6 +50,10 @@ void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const 
 __global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap, int zero_a) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.enabled == 0) {
+    if (m.y == 0 && threadIdx.x == 0) *P.active = 0;
+    return;
+  }
   const int i = m.y * VT + threadIdx.x;
   if (zero_a && i < P.n_pad) P.a[i] = 0.0f;
   if (m.y == 0) {
@@ -63,14 +67,15 @@ void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int
   if (nblocks > 0) reset_problems_kernel<<<nblocks, VT, 0, st>>>(probs, vmap, zero_a);
 }
 
-// active = v for every problem (the phases after the Newton loop act on all)
-__global__ void set_active_kernel(const Prob* __restrict__ probs, int nprob, int v) {
+// active = enabled for every problem (the phases after the Newton loop act on
+// every enabled problem)
+__global__ void activate_enabled_kernel(const Prob* __restrict__ probs, int nprob) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < nprob) *probs[p].active = v;
+  if (p < nprob) *probs[p].active = *probs[p].enabled != 0 ? 1 : 0;
 }
 
-void launch_set_active(const Prob* probs, int nprob, int v, cudaStream_t st) {
-  set_active_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob, v);
+void launch_activate_enabled(const Prob* probs, int nprob, cudaStream_t st) {
+  activate_enabled_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
 }
 
 // ---------------------------------------------------------------- Newton step
@@ -187,6 +192,7 @@ void launch_newton_finalize(const Prob* probs, int nprob, int* any_active, cudaG
 __global__ void lik_full_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int i = m.y * VT + threadIdx.x;
   if (i >= P.n_pad) return;
   if (i >= P.sh.n) {
@@ -217,6 +223,7 @@ __global__ void evidence_partial_kernel(const Prob* __restrict__ probs, const in
   __shared__ double sred[VT / 32];
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int i = m.y * VT + threadIdx.x;
   float v = 0.0f;
   if (i < P.sh.n) v = -P.logp[i] + 0.5f * P.f[i] * P.a[i] + logf(__ldcg(P.L + (size_t)i * P.ld + i));
@@ -228,6 +235,7 @@ __global__ void evidence_sum_kernel(const Prob* __restrict__ probs, int nprob) {
   const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
   if (w >= nprob) return;
   const Prob& P = probs[w];
+  if (*P.active == 0) return;
   const int nparts = ceil_div(P.n_pad, VT);
   double s = 0.0;
   for (int k = lane; k < nparts; k += 32) s += P.part[k];
@@ -248,6 +256,7 @@ void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob
 __global__ void grad_vec1_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int i = m.y * VT + threadIdx.x;
   if (i >= P.n_pad) return;
   if (i >= P.sh.n) {
@@ -269,6 +278,7 @@ void launch_grad_vec1(const Prob* probs, const int2* vmap, int nblocks, cudaStre
 __global__ void scale_tz_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int i = m.y * VT + threadIdx.x;
   if (i >= P.n_pad) return;
   P.tz[i] = i < P.sh.n ? P.sw[i] * P.zbar[i] : 0.0f;
@@ -283,6 +293,7 @@ void launch_scale_tz(const Prob* probs, const int2* vmap, int nblocks, cudaStrea
 __global__ void grad_vec3_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const int i = m.y * VT + threadIdx.x;
   if (i >= P.n_pad) return;
   if (i >= P.sh.n) {
@@ -305,6 +316,7 @@ __global__ void grad_lik_kernel(const Prob* __restrict__ probs, const int2* __re
   __shared__ double sacc[VT / 32][MAX_LIK_SLOTS];
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
   const Shape sh = P.sh;
   const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
   const int i = m.y * VT + threadIdx.x;
@@ -352,6 +364,7 @@ constexpr int FINAL_THREADS = 256;
 __global__ void __launch_bounds__(FINAL_THREADS) grad_final_kernel(const Prob* __restrict__ probs) {
   __shared__ double sred[FINAL_THREADS / 32];
   const Prob& P = probs[blockIdx.x];
+  if (*P.active == 0) return;
   const Shape sh = P.sh;
   const int NP = sh.nl + 1;
   const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);

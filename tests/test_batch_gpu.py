@@ -115,3 +115,30 @@ def test_batch_result_independent_of_company(batch_run):
     for pos, k in enumerate(order):
         assert abs(v2[pos] - values[k]) <= 1e-6 * max(1.0, abs(values[k])), (k, v2[pos], values[k])
         assert np.allclose(_flat(g2[pos]), _flat(grads[k]), rtol=1e-5, atol=1e-6 * np.abs(_flat(grads[k])).max())
+
+
+@pytest.mark.gpu
+def test_batch_mask_evaluates_only_enabled(batch_run):
+    """Disabled problems keep their last outputs; enabled ones equal a full evaluation."""
+    import torch
+
+    probs, gps, params, batch, values, grads = batch_run
+    _, th1 = batch.pack_theta(params)
+    th2 = th1.clone()
+    off = batch.theta_off
+    for b in range(batch.B):      # scale every signal variance by 1.1
+        th2[int(off[b]) + int(batch.descs[b].n_lengthscales)] *= 1.1
+    batch.set_enabled(None)
+    v1, g1 = (t.clone() for t in batch.value_and_grad_flat(th1))
+    v2, g2 = (t.clone() for t in batch.value_and_grad_flat(th2))
+    mask = np.arange(batch.B) % 2 == 0
+    batch.value_and_grad_flat(th1)                       # back to theta1 everywhere
+    batch.set_enabled(mask)
+    vm, gm = (t.clone() for t in batch.value_and_grad_flat(th2))
+    batch.set_enabled(None)
+    for b in range(batch.B):
+        sl = slice(int(off[b]), int(off[b + 1]))
+        if mask[b]:
+            assert torch.equal(vm[b], v2[b]) and torch.equal(gm[sl], g2[sl]), b
+        else:
+            assert torch.equal(vm[b], v1[b]) and torch.equal(gm[sl], g1[sl]), b

@@ -1,0 +1,95 @@
+"""Hyperparameter fits through the batched objective (probit_gb300.optimize).
+
+Problems shaped like the hyperparameter-optimisation workload (D = 3, J = 5,
+Matern12, ordinal probit), small N.  Checks: the batched gradient in the
+unconstrained coordinates (log l, log s, log sigma, interior cutpoints)
+against central finite differences of the batched objective (h = 1e-3) and
+against the float64 oracle's gradient; a few lockstep L-BFGS steps lower
+every problem's objective, and the final values agree with the oracle's
+objective at the final hyperparameters.
+"""
+
+import math
+
+import numpy as np
+import pytest
+
+import probit_gb300 as pg
+from probit_gb300 import workloads as W
+from probit_gb300.optimize import LogParams, batch_objective, minimize_lockstep
+
+
+def _problems(B=6, seed=33):
+    rng = np.random.default_rng(seed)
+    out = []
+    for b in range(B):
+        N = int(rng.integers(150, 420))
+        out.append(W.ordinal_problem(rng, N, 3, 5, "matern12", 1.0, 1.0, math.sqrt(0.4), list(np.linspace(-1.5, 1.5, 4))))
+    return out
+
+
+@pytest.fixture(scope="module")
+def setup(cuda_device):
+    probs = _problems()
+    gps = [pg.LaplaceGP((p.X, p.y), p.prior(), pg.log_probit_likelihood, tolerance=1e-4) for p in probs]
+    params = [p.params() for p in probs]
+    batch = pg.LaplaceBatch(gps, params)
+    lp = LogParams(nl=1, J=5)
+    u0 = np.stack([lp.from_theta(p.theta()[None])[0] for p in probs])
+    u0[:, 0] += 0.3     # start away from the generating lengthscale
+    u0[:, 1] -= 0.2
+    return probs, batch, lp, u0
+
+
+@pytest.mark.gpu
+def test_gradient_vs_finite_differences(setup):
+    probs, batch, lp, u0 = setup
+    fg = batch_objective(batch, lp)
+    f0, g0 = fg(u0)
+    h = 1e-3
+    fd = np.zeros_like(g0)
+    for k in range(u0.shape[1]):
+        e = np.zeros(u0.shape[1])
+        e[k] = h
+        fp, _ = fg(u0 + e)
+        fm, _ = fg(u0 - e)
+        fd[:, k] = (fp - fm) / (2 * h)
+    # float32 objective: FD noise ~ eps * |f| / h
+    noise = 6e-8 * np.abs(f0)[:, None] / h
+    assert (np.abs(g0 - fd) <= 2e-3 * np.abs(g0).max(axis=1, keepdims=True) + 4 * noise).all(), (g0, fd)
+
+
+@pytest.mark.gpu
+def test_gradient_vs_oracle(setup):
+    from oracle import laplace as L
+
+    probs, batch, lp, u0 = setup
+    fg = batch_objective(batch, lp)
+    f0, g0 = fg(u0)
+    theta = lp.to_theta(u0)
+    for b, p in enumerate(probs):
+        op = L.Problem(p.X.astype(np.float64), p.y, p.kernel, "probit", 1, p.period, p.J)
+        v64, g64, _, _ = L.value_and_grad(op, theta[b], tol=1e-4, dtype=np.float64)
+        gu64 = lp.grad_u(theta[b:b + 1], g64[None])[0]
+        assert abs(f0[b] - v64) <= 1e-4 * abs(v64)
+        assert np.abs(g0[b] - gu64).max() <= 1e-3 * np.abs(gu64).max(), (b, g0[b], gu64)
+
+
+@pytest.mark.gpu
+def test_lockstep_steps_lower_every_objective(setup):
+    from oracle import laplace as L
+
+    probs, batch, lp, u0 = setup
+    fg = batch_objective(batch, lp)
+    f0, _ = fg(u0)
+    res = minimize_lockstep(fg, u0, maxiter=10)
+    assert (res.f < f0 - 1e-3).all(), (f0, res.f)
+    assert (res.iterations >= 5).all()
+    # the end point through the oracle's B form (the reference form's 1/W is
+    # infinite wherever W underflowed, which fitted hyperparameters can reach)
+    theta = lp.to_theta(res.x)
+    for b, p in enumerate(probs):
+        op = L.Problem(p.X.astype(np.float64), p.y, p.kernel, "probit", 1, p.period, p.J)
+        a64, _ = L.newton_weight(op, theta[b], tol=1e-4, dtype=np.float64)
+        v64 = float(L.objective_bform(op, theta[b], a64))
+        assert abs(res.f[b] - v64) <= 1e-4 * abs(v64), (b, res.f[b], v64)
