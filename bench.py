@@ -375,22 +375,31 @@ def run_hyperopt(args, dev):
     u0 = np.stack([lp.from_theta(q.theta()[None])[0] for q in probs])
     u0[:, :3] += rng.normal(0.0, 0.5, size=(B, 3))          # log l, log s, log sigma away from the truth
     u0[:, 3:] *= rng.uniform(0.7, 1.3, size=(B, 1))          # cutpoints scaled, still ordered
-    fg = batch_objective(batch, lp)
+    fg_batch = batch_objective(batch, lp)
+    solved = [0]
+
+    def fg(U, mask=None):
+        solved[0] += B if mask is None else int(np.count_nonzero(mask))
+        return fg_batch(U, mask)
+
     for _ in range(max(3, args.warmup)):
         fg(u0)
     torch.cuda.synchronize()
     f0, _ = fg(u0)
+    solved[0] = 0
     t0 = time.perf_counter()
     res = minimize_lockstep(fg, u0, maxiter=args.hyperopt_steps)
     wall = time.perf_counter() - t0
     evals = res.evaluations
+    batch.set_enabled(None)
     st = batch.status()
     out = {
         "workload": f"hyperopt_B{B}_N256-2048_D3_J5_matern12", "B": B, "lbfgs_steps": args.hyperopt_steps,
-        "tolerance": tol, "evaluations": evals, "wall_s": wall,
-        "value": B * evals / wall, "unit": UNIT,
-        "what": "end to end: host L-BFGS (vectorised over problems) + one batched value_and_grad per round, "
-                "theta up and values + gradients down every round",
+        "tolerance": tol, "evaluation_rounds": evals, "problem_evaluations": solved[0], "wall_s": wall,
+        "value": solved[0] / wall, "unit": UNIT,
+        "what": "end to end: host L-BFGS (vectorised over problems) + one batched value_and_grad per round "
+                "over the problems whose line search runs (the others are masked off), theta up and values + "
+                "gradients down every round; value = problem evaluations / wall time",
         "objective_mean": {"start": float(np.mean(f0)), "end": float(np.mean(res.f))},
         "accepted_steps_mean": float(res.iterations.mean()),
         "problems_failed": int(sum(1 for x in st if x[0] != 0)),

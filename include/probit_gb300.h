@@ -172,6 +172,31 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a,
                 const float* W, const float* Xs, int32_t m, float* mean_out,
                 float* var_out, int32_t reuse_factor, void* stream);
 
+/* pgb_predict followed, in the same launch sequence, by the ordinal
+ * predictive distribution of every test point: dist_out (m x J, row-major)
+ * holds p(y = j) = Phi((b_{j+1} - mean) / s) - Phi((b_j - mean) / s) with
+ * s = sqrt(var + sigma_n^2).  Replaces predict followed by
+ * probit_predictive_distributions (utilities.py:232-249).  Probit
+ * likelihoods only (else PGB_EINVAL); mean_out and var_out may be NULL. */
+int pgb_predict_distributions(pgb_gp* gp, const float* X, const float* theta, const float* a,
+                              const float* W, const float* Xs, int32_t m, float* dist_out,
+                              float* mean_out, float* var_out, int32_t reuse_factor,
+                              void* stream);
+
+/* Ordinal predictive distributions from given predictive means and variances
+ * (device arrays of m; dist_out m x J).  Replaces
+ * probit_predictive_distributions (utilities.py:232-249). */
+int pgb_predictive_distributions(const pgb_desc* desc, const float* theta, const float* mean,
+                                 const float* var, int32_t m, float* dist_out, void* stream);
+
+/* Full predictive covariance K(Xs, Xs) - K_*^T (K + W^-1)^-1 K_* (m x m,
+ * row-major, leading dimension ldc >= m), with the same factor rules as
+ * pgb_predict.  Replaces Approximator.predict_covariance
+ * (approximators.py:182-197). */
+int pgb_predict_covariance(pgb_gp* gp, const float* X, const float* theta, const float* W,
+                           const float* Xs, int32_t m, float* cov_out, int64_t ldc,
+                           int32_t reuse_factor, void* stream);
+
 /* ---------------------------------------------------------------- batches
  * Many independent GP problems, each with its own pgb_desc (n, d, kernel,
  * likelihood, J, tolerance, maxiter), evaluated together: every kernel of

@@ -16,11 +16,12 @@ from .utilities import (
     log_gaussian_likelihood,
     log_probit_likelihood,
     log_probit_likelihood_stable,
+    probit_predictive_distributions,
 )
 
 __all__ = [
     "LaplaceGP", "LaplaceBatch", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
     "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
-    "check_cutpoints",
+    "check_cutpoints", "probit_predictive_distributions",
 ]
 __version__ = "0.1.0"

@@ -90,6 +90,10 @@ _SIGS = {
     "pgb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_factor": (C.c_int, [_VP, _VP]),
     "pgb_predict": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, _VP, C.c_int32, _VP]),
+    "pgb_predict_distributions": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, _VP, _VP, C.c_int32,
+                                             _VP]),
+    "pgb_predictive_distributions": (C.c_int, [C.POINTER(Desc), _VP, _VP, _VP, C.c_int32, _VP, _VP]),
+    "pgb_predict_covariance": (C.c_int, [_VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, C.c_int64, C.c_int32, _VP]),
     "pgb_batch_create": (C.c_int, [C.POINTER(Desc), C.c_int32, C.POINTER(_VP)]),
     "pgb_batch_destroy": (C.c_int, [_VP]),
     "pgb_batch_layout": (C.c_int, [_VP, C.POINTER(C.c_int64), C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),

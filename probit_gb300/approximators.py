@@ -354,8 +354,31 @@ class LaplaceGP:
         return self._out(mean), self._out(var)
 
     def predict_covariance(self, X_test, parameters, weight, precision):
-        """Full predictive covariance; not provided by this build."""
-        raise NotImplementedError("predict_covariance is not implemented by the CUDA library yet")
+        """Full predictive covariance (M, M) at X_test (``Approximator.predict_covariance``,
+        ``approximators.py:182-197``): K(X*, X*) - K_*^T (K + W^-1)^-1 K_*."""
+        import torch
+
+        theta, key = self._theta(parameters)
+        gp = self._handles.get(key) or self._handle(key)
+        X, _ = self._device_data()
+        td = self._theta_dev(theta)
+        Xs = as_device(X_test, torch.float32)
+        if Xs.dim() != 2 or Xs.shape[1] != self.D:
+            raise ValueError(f"X_test must be (M, {self.D})")
+        M = int(Xs.shape[0])
+        reuse = 0
+        last = self._last
+        if (last is not None and weight is last[0] and precision is last[1] and key == last[5]
+                and theta.detach().numpy().tobytes() == last[4] and gp.gen == last[6]):
+            W, reuse = last[3], 1
+        else:
+            gp.gen += 1
+            W = as_device(precision, torch.float32)
+        cov = torch.empty((M, M), dtype=torch.float32, device=td.device)
+        N.check(gp.lib.pgb_predict_covariance(gp.h, X.data_ptr(), td.data_ptr(), W.data_ptr(), Xs.data_ptr(), M,
+                                              cov.data_ptr(), M, reuse, stream_handle(td.device)),
+                "pgb_predict_covariance")
+        return self._out(cov)
 
     def posterior_mean(self, weight, parameters):
         """K weight (the reference's version reads an undefined name, :199-202)."""

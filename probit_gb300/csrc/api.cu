@@ -741,6 +741,7 @@ struct pgb_gp {
   float* Xq_in = nullptr;
   int* ready_c = nullptr;
   void* map_c = nullptr;   // tensor map of Rc (device, 128 B)
+  float* mv_ws = nullptr;  // predictive mean and variance when only distributions are asked
   int4* tasks_c = nullptr;
   int ntasks_c = 0;
   long long cap_c = 0;     // predict rows allocated
@@ -796,7 +797,7 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
 int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
   engine_free(gp->e);
-  void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c, gp->map_c};
+  void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c, gp->map_c, gp->mv_ws};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete gp;
@@ -920,9 +921,22 @@ int pgb_factor(pgb_gp* gp, void* stream) {
   return PGB_OK;
 }
 
-int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, const float* W, const float* Xs,
-                int32_t m, float* mean_out, float* var_out, int32_t reuse_factor, void* stream) {
-  if (!gp || !X || !theta || !a || !Xs || m < 0 || (!mean_out && !var_out)) return PGB_EINVAL;
+}  // extern "C"
+
+namespace {
+
+// Predictive quantities at m test points: mean (needs a), variance, ordinal
+// distribution, full covariance (any subset).  The factor of B is the
+// resident one (reuse_factor) or rebuilt from W; the cross-kernel solve
+// (L^-1 W^1/2 K_*)^T runs when variance, distribution or covariance is asked.
+int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a, const float* W, const float* Xs,
+                 int32_t m, float* mean_out, float* var_out, float* dist_out, float* cov_out, int64_t ldc,
+                 int32_t reuse_factor, void* stream) {
+  if (!gp || !X || !theta || !Xs || m < 0) return PGB_EINVAL;
+  if (!mean_out && !var_out && !dist_out && !cov_out) return PGB_EINVAL;
+  if ((mean_out || dist_out) && !a) return PGB_EINVAL;
+  if (cov_out && ldc < m) return PGB_EINVAL;
+  if (dist_out && gp->e.sh[0].lik == PGB_LIK_GAUSSIAN) return PGB_EINVAL;
   if (m == 0) return PGB_OK;
   if (!reuse_factor && !W) return PGB_EINVAL;
   if (reuse_factor && !gp->factor_valid) return PGB_ESTATE;
@@ -936,10 +950,10 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
   // grow the cross-kernel workspace
   if (mpad > gp->cap_c) {
     CU_TRY(cudaStreamSynchronize(s));
-    void* old[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c};
+    void* old[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->mv_ws};
     for (void* p : old)
       if (p) cudaFree(p);
-    gp->Rc = gp->rowsq = gp->Xq = gp->Xq_in = nullptr;
+    gp->Rc = gp->rowsq = gp->Xq = gp->Xq_in = gp->mv_ws = nullptr;
     gp->ready_c = nullptr;
     gp->cap_c = 0;
     auto grab = [](void** p, size_t bytes) {
@@ -955,6 +969,7 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq), sizeof(float) * (size_t)mpad * sh.Dp));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq_in), sizeof(float) * (size_t)mpad * sh.D));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->ready_c), sizeof(int) * (size_t)(nt + mt) * nt));
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->mv_ws), sizeof(float) * 2 * (size_t)mpad));
     if (!gp->map_c) PGB_TRY(grab(&gp->map_c, 128));
     alignas(64) unsigned char m[128];
     if (!make_tile_map(m, gp->Rc, mpad, q.ld, q.ld)) return PGB_ECUDA;
@@ -987,8 +1002,10 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
   }
   CU_TRY(cudaMemcpyAsync(gp->Xq_in, Xs, sizeof(float) * (size_t)m * sh.D, cudaMemcpyDeviceToDevice, s));
   launch_prep_features_raw(sh, gp->Xq_in, q.theta, gp->Xq, m, (int)mpad, s);
-  if (mean_out) launch_gram_matvec_raw(sh, q.theta, gp->Xq, m, q.Xf, sh.n, a, mean_out, s);
-  if (var_out) {
+  float* mean = mean_out ? mean_out : (dist_out ? gp->mv_ws : nullptr);
+  float* var = var_out ? var_out : (dist_out ? gp->mv_ws + mpad : nullptr);
+  if (mean) launch_gram_matvec_raw(sh, q.theta, gp->Xq, m, q.Xf, sh.n, a, mean, s);
+  if (var || cov_out) {
     DagJob jb = e.hjobs[JOB_CROSS];
     jb.nrt = mt;
     jb.nrhs = m;
@@ -1004,8 +1021,50 @@ int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, 
     CU_TRY(cudaMemsetAsync(e.counters + C_PREDICT, 0, sizeof(int), s));
     launch_dag_factor(e.jobs, gp->tasks_c, gp->ntasks_c, e.counters + C_PREDICT, e.dag_dm,
                       dag_grid(e, gp->ntasks_c), s);
-    launch_predict_var(sh, q.theta, gp->rowsq, nt, m, var_out, s);
+    if (var) launch_predict_var(sh, q.theta, gp->rowsq, nt, m, var, s);
+    if (cov_out) {
+      // K(Xs, Xs), then minus (L^-1 W^1/2 K_*)^T (L^-1 W^1/2 K_*) on the tensor cores
+      launch_gram_full(sh, q.theta, gp->Xq, m, gp->Xq, m, cov_out, ldc, s);
+      CU_TRY(cudaMemsetAsync(e.counters + C_PREDICT, 0, sizeof(int), s));
+      const int ntiles = mt * (mt + 1) / 2;
+      launch_sub_rrt(gp->map_c, m, nt, cov_out, ldc, e.counters + C_PREDICT, e.status_all, dag_grid(e, ntiles), s);
+    }
   }
+  if (dist_out) launch_predictive_dist(sh, q.theta, mean, var, m, dist_out, s);
+  CU_TRY(cudaGetLastError());
+  return PGB_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int pgb_predict(pgb_gp* gp, const float* X, const float* theta, const float* a, const float* W, const float* Xs,
+                int32_t m, float* mean_out, float* var_out, int32_t reuse_factor, void* stream) {
+  if (!gp || !a || (!mean_out && !var_out)) return PGB_EINVAL;
+  return predict_impl(gp, X, theta, a, W, Xs, m, mean_out, var_out, nullptr, nullptr, 0, reuse_factor, stream);
+}
+
+int pgb_predict_distributions(pgb_gp* gp, const float* X, const float* theta, const float* a, const float* W,
+                              const float* Xs, int32_t m, float* dist_out, float* mean_out, float* var_out,
+                              int32_t reuse_factor, void* stream) {
+  if (!gp || !dist_out) return PGB_EINVAL;
+  return predict_impl(gp, X, theta, a, W, Xs, m, mean_out, var_out, dist_out, nullptr, 0, reuse_factor, stream);
+}
+
+int pgb_predict_covariance(pgb_gp* gp, const float* X, const float* theta, const float* W, const float* Xs,
+                           int32_t m, float* cov_out, int64_t ldc, int32_t reuse_factor, void* stream) {
+  if (!gp || !cov_out) return PGB_EINVAL;
+  return predict_impl(gp, X, theta, nullptr, W, Xs, m, nullptr, nullptr, nullptr, cov_out, ldc, reuse_factor,
+                      stream);
+}
+
+int pgb_predictive_distributions(const pgb_desc* desc, const float* theta, const float* mean, const float* var,
+                                 int32_t m, float* dist_out, void* stream) {
+  if (validate(desc) != PGB_OK || desc->likelihood == PGB_LIK_GAUSSIAN || !theta || !mean || !var || !dist_out ||
+      m < 0)
+    return PGB_EINVAL;
+  launch_predictive_dist(make_shape(desc), theta, mean, var, m, dist_out, (cudaStream_t)stream);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
 }

@@ -812,10 +812,13 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const voi
 
 __global__ void syrk_zzt_kernel(const Prob* __restrict__ probs, const int4* __restrict__ tiles, int ntiles,
                                 int* __restrict__ counter);
+__global__ void sub_rrt_kernel(const void* rmap, int m, int nt, float* __restrict__ C, long long ldc,
+                               int* __restrict__ counter, int* __restrict__ status);
 
 void dag_set_attributes() {
   cudaFuncSetAttribute(tc_tile_check_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(syrk_zzt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
+  cudaFuncSetAttribute(sub_rrt_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<8>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
   cudaFuncSetAttribute(dag_factor_kernel<16>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)DAG_SMEM);
@@ -882,6 +885,58 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
     }
   }
   tc_teardown(tc);
+}
+
+// C -= R R^T (predictive covariance: K(Xs, Xs) - V^T V with V^T = R the
+// cross-kernel solve rows).  Task t -> lower tile (I, J) of the ceil(m/128)^2
+// grid; entries beyond m are not written.
+__global__ void __launch_bounds__(DAG_THREADS, 1) sub_rrt_kernel(const void* rmap, int m, int nt,
+                                                                 float* __restrict__ C, long long ldc,
+                                                                 int* __restrict__ counter, int* __restrict__ status) {
+  extern __shared__ uint8_t dsmem[];
+  __shared__ int s_task;
+  __shared__ uint32_t s_tmem;
+  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
+  float* sC = reinterpret_cast<float*>(tc.stages);
+  const int mt = ceil_div(m, T);
+  const int ntiles = mt * (mt + 1) / 2;
+  auto always = [](int) { return true; };
+  while (true) {
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (threadIdx.x == 0) s_task = atomicAdd(counter, 1);
+    __syncthreads();
+    const int t = s_task;
+    if (t >= ntiles) break;
+    int I = (int)((sqrtf(8.0f * t + 1.0f) - 1.0f) * 0.5f);
+    while (I * (I + 1) / 2 > t) --I;
+    while ((I + 1) * (I + 2) / 2 <= t) ++I;
+    const int J = t - I * (I + 1) / 2;
+    TcLoad l = tc_load(rmap, I * T, 0, rmap, J * T, 0, 0, nt, tc);
+    if (threadIdx.x == 0) {
+      fence_tensormap_acquire(rmap);
+      tc_start(tc, l, always);
+    }
+    if (!tc_run(tc, l, status, always, false)) continue;
+    tmem_to_tile(tc, sC, 1.0f);
+    __syncthreads();
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      const int gi = I * T + r, gj = J * T + c;
+      if (gi < m && gj < m && (I != J || c <= r)) {
+        C[(size_t)gi * ldc + gj] -= sC[r * SC_LD + c];
+        if (gi != gj) C[(size_t)gj * ldc + gi] -= sC[r * SC_LD + c];
+      }
+    }
+  }
+  tc_teardown(tc);
+}
+
+void launch_sub_rrt(const void* rmap, int m, int nt, float* C, long long ldc, int* counter, int* status, int grid,
+                    cudaStream_t st) {
+  if (m <= 0) return;
+  sub_rrt_kernel<<<grid, DAG_THREADS, DAG_SMEM, st>>>(rmap, m, nt, C, ldc, counter, status);
 }
 
 void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* counter, int grid, cudaStream_t st) {

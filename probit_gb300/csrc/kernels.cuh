@@ -147,6 +147,9 @@ void launch_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int
 void launch_predict_var(const Shape& sh, const float* theta, const float* rowsq, int nt, int m, float* var,
                         cudaStream_t st);
 void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st);
+// dist (m x J) = ordinal predictive distribution from mean and var
+void launch_predictive_dist(const Shape& sh, const float* theta, const float* mean, const float* var, int m,
+                            float* dist, cudaStream_t st);
 // factor reuse per active problem: differs |= any(sw != sw_prev); decide
 void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st);
@@ -161,6 +164,10 @@ void dag_set_attributes();
 // DM: feature loop bound (4, 8 or 16), at least every job's Dp
 void launch_dag_factor(const DagJob* jobs_dev, const int4* tasks, int ntasks, int* counter, int DM, int grid,
                        cudaStream_t st);
+// C (m x m, ldc) -= R R^T for R = rows 0..m of the matrix behind tensor map
+// `rmap` (k-range: nt tiles of 128 columns); lower tiles computed, mirrored.
+void launch_sub_rrt(const void* rmap, int m, int nt, float* C, long long ldc, int* counter, int* status, int grid,
+                    cudaStream_t st);
 // B^-1 = Z Z^T over the merged lower-tile list (tiles: problem, I, J, -)
 void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* counter, int grid, cudaStream_t st);
 

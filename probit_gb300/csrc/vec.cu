@@ -413,6 +413,32 @@ void launch_predict_var(const Shape& sh, const float* theta, const float* rowsq,
   if (m > 0) predict_var_kernel<<<ceil_div(m, VT), VT, 0, st>>>(sh, theta, rowsq, nt, m, var);
 }
 
+// Ordinal predictive distribution (probit_predictive_distributions,
+// utilities.py:232-249, through the guarded probit of utilities.py:195-229):
+// dist[i, j] = Phi((b_{j+1} - mean_i) / s_i) - Phi((b_j - mean_i) / s_i),
+// s_i = sqrt(var_i + sigma^2); an infinite cutpoint gives Phi = 0 or 1.
+__global__ void predictive_dist_kernel(Shape sh, const float* __restrict__ theta, const float* __restrict__ mean,
+                                       const float* __restrict__ var, int m, float* __restrict__ dist) {
+  const int i = blockIdx.x * VT + threadIdx.x;
+  if (i >= m) return;
+  const float sig = theta_sigma(sh, theta);
+  const float* b = theta_cutpoints(sh, theta);
+  const float mu = mean[i];
+  const float sd = sqrtf(var[i] + sig * sig);
+  float lo = 0.0f;   // b_0 = -inf
+  for (int j = 0; j < sh.J; ++j) {
+    const float bh = __ldg(b + j + 1);
+    const float hi = isinf(bh) ? (bh > 0.0f ? 1.0f : 0.0f) : ndtr_ref((bh - mu) / sd);
+    dist[(size_t)i * sh.J + j] = hi - lo;
+    lo = hi;
+  }
+}
+
+void launch_predictive_dist(const Shape& sh, const float* theta, const float* mean, const float* var, int m,
+                            float* dist, cudaStream_t st) {
+  if (m > 0) predictive_dist_kernel<<<ceil_div(m, VT), VT, 0, st>>>(sh, theta, mean, var, m, dist);
+}
+
 // sw = sqrt(W) for a caller-supplied precision (padding 0)
 __global__ void sqrt_w_kernel(int n, int n_pad, const float* __restrict__ W, float* __restrict__ sw) {
   const int i = blockIdx.x * VT + threadIdx.x;

@@ -29,7 +29,7 @@ from ._device import as_device, like_input, stream_handle
 __all__ = [
     "log_gaussian_likelihood", "log_probit_likelihood", "log_probit_likelihood_stable",
     "grad_log_probit_likelihood", "hessian_log_probit_likelihood", "likelihood_mode",
-    "check_cutpoints", "CutpointValueError",
+    "check_cutpoints", "CutpointValueError", "probit_predictive_distributions",
 ]
 
 
@@ -57,6 +57,31 @@ def _eval(mode, f, y, likelihood_parameters, which):
                                    stream_handle(fd.device)), "pgb_log_likelihood")
     res = [like_input(outs[k], f) for k in which]
     return res[0] if len(res) == 1 else tuple(res)
+
+
+def probit_predictive_distributions(likelihood_parameters, posterior_mean, posterior_variance):
+    """Ordinal predictive distributions (N_test, J) on the GPU
+    (``probit_predictive_distributions``, ``utilities.py:232-249``):
+    p(y = j) = Phi((b_{j+1} - mean) / s) - Phi((b_j - mean) / s),
+    s = sqrt(variance + noise_std^2)."""
+    import torch
+
+    noise_std, cutpoints = likelihood_parameters
+    cut = np.asarray(cutpoints.detach().cpu() if hasattr(cutpoints, "detach") else cutpoints,
+                     dtype=np.float64).reshape(-1)
+    J = cut.size - 1
+    md = as_device(posterior_mean, torch.float32).reshape(-1)
+    vd = as_device(posterior_variance, torch.float32, md.device).reshape(-1)
+    m = md.numel()
+    sigma = float(np.asarray(noise_std, dtype=np.float64))
+    theta = torch.tensor(np.concatenate([[1.0, 1.0, sigma], cut]), dtype=torch.float32, device=md.device)
+    desc = N.Desc(max(m, 1), 1, N.KERNEL_EQ, 1, 1.0, N.LIK_PROBIT, J, 1e-5, 100, 0)
+    out = torch.empty((m, J), dtype=torch.float32, device=md.device)
+    lib = N.load()
+    N.check(lib.pgb_predictive_distributions(desc, theta.data_ptr(), md.data_ptr(), vd.data_ptr(), m,
+                                             out.data_ptr(), stream_handle(md.device)),
+            "pgb_predictive_distributions")
+    return like_input(out, posterior_mean)
 
 
 def log_gaussian_likelihood(f, y, likelihood_parameters):

@@ -187,3 +187,62 @@ def test_eager_mode_matches_graph_mode(cuda_device, monkeypatch):
         v, gr = gp.value_and_grad()(p.params())
         out.append((v, flat(gr), gp.last_status()[1]))
     assert out[0][0] == out[1][0] and np.array_equal(out[0][1], out[1][1]) and out[0][2] == out[1][2]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["ordinal_matern12_n200", "ordinal_periodic_n130", "gauss_eq_ard_n400"])
+def test_predict_covariance_and_distributions(name, cuda_device):
+    """Full predictive covariance and ordinal predictive distributions against
+    the oracle at the fitted posterior (bars: 1e-4 of s for covariance
+    entries, 1e-4 absolute for probabilities)."""
+    import ctypes as C
+
+    import torch
+
+    from oracle import laplace as L
+    from cases import oracle_problem
+
+    g = np.load(GOLD / f"{name}.npz")
+    p, theta, tol = make(name)
+    lik = CASES[name][1]
+    gp = pg.LaplaceGP((g["X"], g["y"]), p.prior(), LIK[lik], tolerance=tol)
+    params = p.params()
+    a, W = gp.approximate_posterior(params)
+    Xs = g["Xtest"]
+    cov = gp.predict_covariance(Xs, params, a, W)
+    mean, var = gp.predict(Xs, params, a, W)
+    op = oracle_problem(p, lik)
+    cov64 = L.predict_covariance(op, theta, Xs.astype(np.float64), np.asarray(a, np.float64),
+                                 np.asarray(W, np.float64))
+    s = p.variance
+    assert cov.shape == (Xs.shape[0], Xs.shape[0])
+    assert np.abs(cov - cov64).max() < 1e-4 * s, np.abs(cov - cov64).max()
+    assert np.abs(np.diag(cov) - var).max() < 1e-5 * s
+    assert np.allclose(cov, cov.T, atol=0)
+    # the same with the factor rebuilt from W
+    cov2 = gp.predict_covariance(Xs, params, np.array(a), np.array(W))
+    assert np.abs(cov2 - cov).max() < 1e-5 * s
+    if lik == "gaussian":
+        return
+    sigma, cut = params[1]
+    d64 = L.predictive_distributions(sigma, cut, np.asarray(mean, np.float64), np.asarray(var, np.float64))
+    dist = pg.probit_predictive_distributions(params[1], mean, var)
+    assert dist.shape == d64.shape
+    assert np.abs(dist - d64).max() < 1e-4
+    assert np.allclose(dist.sum(axis=1), 1.0, atol=1e-5)
+    # fused with predict through the C-ABI
+    h = list(gp._handles.values())[0]
+    dev = cuda_device
+    M = Xs.shape[0]
+    J = len(cut) - 1
+    td = torch.tensor(theta, dtype=torch.float32, device=dev)
+    Xd = torch.tensor(g["X"], dtype=torch.float32, device=dev)
+    ad = torch.tensor(np.asarray(a), dtype=torch.float32, device=dev)
+    Wd = torch.tensor(np.asarray(W), dtype=torch.float32, device=dev)
+    Xsd = torch.tensor(Xs, dtype=torch.float32, device=dev)
+    dd = torch.empty((M, J), dtype=torch.float32, device=dev)
+    N.check(h.lib.pgb_predict_distributions(h.h, Xd.data_ptr(), td.data_ptr(), ad.data_ptr(), Wd.data_ptr(),
+                                            Xsd.data_ptr(), M, dd.data_ptr(), None, None, 0,
+                                            torch.cuda.current_stream().cuda_stream), "pgb_predict_distributions")
+    torch.cuda.synchronize()
+    assert np.abs(dd.cpu().numpy() - d64).max() < 1e-4
