@@ -72,6 +72,22 @@ struct Bump {
 
 int dm_of(int Dp) { return Dp <= 4 ? 4 : (Dp <= 8 ? 8 : 16); }
 
+// Device memory of a handle comes from the stream-ordered allocator on the
+// handle's private stream: freeing it never synchronises the device (a
+// cudaFree would wait for every stream, stalling other requests in a server).
+int ws_alloc(cudaStream_t s, void** p, size_t bytes) {
+  if (cudaMallocAsync(p, std::max<size_t>(bytes, 256), s) != cudaSuccess || cudaStreamSynchronize(s) != cudaSuccess) {
+    cudaGetLastError();
+    *p = nullptr;
+    return PGB_ENOMEM;
+  }
+  return PGB_OK;
+}
+
+void ws_free(cudaStream_t s, void* p) {
+  if (p) cudaFreeAsync(p, s);
+}
+
 struct MvGroup {
   int kind, DM;
   std::vector<int2> h;
@@ -165,6 +181,14 @@ void setup_attributes() {
   std::call_once(g_attr_once, [] {
     dag_set_attributes();
     trsv_set_attributes();
+    // keep freed handle workspaces in this process's pool for the next handle
+    int dev = 0;
+    cudaMemPool_t pool;
+    if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+    cudaGetLastError();
   });
 }
 
@@ -369,10 +393,13 @@ size_t layout(Engine& e, uintptr_t base) {
 void engine_free(Engine& e) {
   for (int k = 0; k < OP_COUNT; ++k)
     if (e.gexec[k]) cudaGraphExecDestroy(e.gexec[k]);
-  if (e.arena) cudaFree(e.arena);
-  if (e.garena) cudaFree(e.garena);
-  if (e.trace) cudaFree(e.trace);
-  if (e.cap_s) cudaStreamDestroy(e.cap_s);
+  if (e.cap_s) {
+    ws_free(e.cap_s, e.arena);
+    ws_free(e.cap_s, e.garena);
+    ws_free(e.cap_s, e.trace);
+    cudaStreamSynchronize(e.cap_s);
+    cudaStreamDestroy(e.cap_s);
+  }
   if (e.cap_s2) cudaStreamDestroy(e.cap_s2);
   e.arena = e.garena = nullptr;
   e.trace = nullptr;
@@ -504,14 +531,13 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     e.nclaims = (int)e.h_claims.size();
   }
   // one arena
+  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s, cudaStreamNonBlocking));
+  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s2, cudaStreamNonBlocking));
   const size_t bytes = layout(e, 0);
-  if (cudaMalloc(&e.arena, bytes) != cudaSuccess) {
-    cudaGetLastError();
-    e.arena = nullptr;
-    return PGB_ENOMEM;
-  }
+  PGB_TRY(ws_alloc(e.cap_s, &e.arena, bytes));
   layout(e, reinterpret_cast<uintptr_t>(e.arena));
-  CU_TRY(cudaMemset(e.arena, 0, bytes));
+  CU_TRY(cudaMemsetAsync(e.arena, 0, bytes, e.cap_s));
+  CU_TRY(cudaStreamSynchronize(e.cap_s));
   {
     const std::vector<int> ones(count, 1);
     PGB_TRY(upload(e.enabled_all, ones));
@@ -530,21 +556,18 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     if (tv && tv[0] == '1') {
       size_t mx = 0;
       for (int k = 0; k < 3; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
-      if (cudaMalloc(&e.trace, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 16)) == cudaSuccess) {
+      void* tp = nullptr;
+      if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 16)) == PGB_OK) {
+        e.trace = static_cast<unsigned long long*>(tp);
         for (DagJob& j : e.hjobs) {
           j.trace = e.trace;
           j.ptrace = e.trace + mx * 8;
         }
-      } else {
-        cudaGetLastError();
-        e.trace = nullptr;
       }
     }
   }
   PGB_TRY(upload_maps(e));
   PGB_TRY(engine_upload_tables(e));
-  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s, cudaStreamNonBlocking));
-  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s2, cudaStreamNonBlocking));
   return PGB_OK;
 }
 
@@ -553,12 +576,9 @@ int ensure_grad_buffers(Engine& e) {
   if (e.grad_ready) return PGB_OK;
   size_t total = 0;
   for (int p = 0; p < e.nprob; ++p) total += 2 * (((size_t)e.hp[p].n_pad * e.hp[p].ld * sizeof(float) + 255) & ~(size_t)255);
-  if (cudaMalloc(&e.garena, total) != cudaSuccess) {
-    cudaGetLastError();
-    e.garena = nullptr;
-    return PGB_ENOMEM;
-  }
-  CU_TRY(cudaMemset(e.garena, 0, total));
+  PGB_TRY(ws_alloc(e.cap_s, &e.garena, total));
+  CU_TRY(cudaMemsetAsync(e.garena, 0, total, e.cap_s));
+  CU_TRY(cudaStreamSynchronize(e.cap_s));
   Bump b;
   b.base = reinterpret_cast<uintptr_t>(e.garena);
   for (int p = 0; p < e.nprob; ++p) {
@@ -796,10 +816,10 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
 
 int pgb_gp_destroy(pgb_gp* gp) {
   if (!gp) return PGB_OK;
-  engine_free(gp->e);
   void* ptrs[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->tasks_c, gp->map_c, gp->mv_ws};
-  for (void* p : ptrs)
-    if (p) cudaFree(p);
+  if (gp->e.cap_s)
+    for (void* p : ptrs) ws_free(gp->e.cap_s, p);
+  engine_free(gp->e);
   delete gp;
   return PGB_OK;
 }
@@ -951,19 +971,11 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
   if (mpad > gp->cap_c) {
     CU_TRY(cudaStreamSynchronize(s));
     void* old[] = {gp->Rc, gp->rowsq, gp->Xq, gp->Xq_in, gp->ready_c, gp->mv_ws};
-    for (void* p : old)
-      if (p) cudaFree(p);
+    for (void* p : old) ws_free(e.cap_s, p);
     gp->Rc = gp->rowsq = gp->Xq = gp->Xq_in = gp->mv_ws = nullptr;
     gp->ready_c = nullptr;
     gp->cap_c = 0;
-    auto grab = [](void** p, size_t bytes) {
-      if (cudaMalloc(p, bytes) != cudaSuccess) {
-        cudaGetLastError();
-        *p = nullptr;
-        return PGB_ENOMEM;
-      }
-      return PGB_OK;
-    };
+    auto grab = [&e](void** p, size_t bytes) { return ws_alloc(e.cap_s, p, bytes); };
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Rc), sizeof(float) * (size_t)mpad * q.ld));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->rowsq), sizeof(float) * (size_t)mpad * nt));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq), sizeof(float) * (size_t)mpad * sh.Dp));
@@ -979,15 +991,11 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
   if (gp->m_tasks != mt) {
     if (gp->tasks_c) {
       CU_TRY(cudaStreamSynchronize(s));
-      cudaFree(gp->tasks_c);
+      ws_free(e.cap_s, gp->tasks_c);
       gp->tasks_c = nullptr;
     }
     std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0});
-    if (cudaMalloc(reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)) != cudaSuccess) {
-      cudaGetLastError();
-      gp->tasks_c = nullptr;
-      return PGB_ENOMEM;
-    }
+    PGB_TRY(ws_alloc(e.cap_s, reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)));
     PGB_TRY(upload(gp->tasks_c, v));
     gp->ntasks_c = (int)v.size();
     gp->m_tasks = mt;

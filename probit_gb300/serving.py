@@ -1,0 +1,385 @@
+"""Serving: fit / evidence+gradient / predict requests with continuous batching.
+
+A :class:`Server` takes requests as they arrive and runs them concurrently on
+one GPU:
+
+* every fitted GP (a *model*) stays resident in HBM as a library handle
+  holding its factor L of B, W, a and the features; a predict request reuses
+  that factor (``pgb_predict`` with ``reuse_factor``), so it costs one
+  cross-kernel solve and no refactorisation;
+* requests are admitted by HBM footprint: a request runs only when its
+  workspace (and, for a fit, its resident model) fits in the memory budget;
+  idle models are evicted least-recently-used when room is needed;
+* admitted requests run on a pool of worker threads, each driving its own
+  CUDA stream, so the kernels of different requests overlap on the device
+  (the tile-DAG launches of small problems use a few SMs each); requests of
+  small problems (n <= ``small_n``) go to higher-priority streams and are
+  taken first;
+* a model is used by one request at a time (a handle is not thread-safe);
+  other requests for it wait in the queue.
+
+Results are what the same call gives alone: every kernel's arithmetic for a
+problem is independent of what else runs on the GPU.
+
+The request semantics follow the reference's methods: a fit is
+``approximate_posterior`` (``approximators.py:204-210``), an evidence+gradient
+request is ``value_and_grad`` (``approximators.py:132-134``), a predict
+request is ``predict`` (``approximators.py:154-180``) at the model's resident
+posterior.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import itertools
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _native as N
+
+_KINDS = {"eq": N.KERNEL_EQ, "matern12": N.KERNEL_MATERN12, "eq_periodic": N.KERNEL_EQ_PERIODIC}
+
+
+def handle_bytes(n, d, kind, grad=True, m=0):
+    """HBM a handle of n points needs (workspace + resident factor), plus the
+    predict workspace for m test points."""
+    npad = -(-n // 128) * 128
+    nt = npad // 128
+    F = 2 * d if kind == "eq_periodic" else d
+    Fp = -(-F // 4) * 4
+    mat = 4 * npad * npad
+    vec = 4 * npad * (22 + Fp)
+    b = mat + 4 * nt * 128 * 128 + 4 * 128 * npad + vec + 8 * npad * 80 + 16 * nt * nt + 4096
+    if grad:
+        b += 2 * mat
+    if m > 0:
+        mpad = -(-m // 128) * 128
+        b += 4 * mpad * (npad + nt + Fp + d + 2) + 4 * (nt + mpad // 128) * nt
+    return b
+
+
+@dataclass
+class Problem:
+    """The data and hyperparameters of one served GP (host arrays)."""
+
+    X: np.ndarray            # (n, d) float32
+    y: np.ndarray            # (n,) int32 labels (ordinal probit) or float32 targets (Gaussian)
+    kind: str                # "eq" | "matern12" | "eq_periodic"
+    theta: np.ndarray        # flat theta: l, s, sigma, cutpoints (J + 1, infinite ends)
+    nl: int = 1
+    J: int = 0               # 0: Gaussian likelihood
+    period: float = 0.5
+    tolerance: float = 1e-3
+    maxiter: int = 100
+
+    @property
+    def n(self):
+        return self.X.shape[0]
+
+    @property
+    def d(self):
+        return self.X.shape[1]
+
+    def desc(self):
+        lik = N.LIK_GAUSSIAN if self.J == 0 else N.LIK_PROBIT
+        return N.Desc(self.n, self.d, _KINDS[self.kind], self.nl, self.period, lik, self.J, self.tolerance,
+                      self.maxiter, 0)
+
+
+@dataclass(order=True)
+class Request:
+    sort_key: tuple = field(init=False, repr=False)
+    arrival: float                     # seconds since the start of the run
+    kind: str = field(compare=False)   # "fit" | "vg" | "predict"
+    model: int = field(compare=False)  # model id (fit: the id it creates)
+    problem: Problem = field(compare=False, default=None)
+    Xs: np.ndarray = field(compare=False, default=None)    # predict: (m, d) float32
+    theta: np.ndarray = field(compare=False, default=None)  # vg: hyperparameters to evaluate
+    # filled in by the server
+    start: float = field(compare=False, default=None)
+    done: float = field(compare=False, default=None)
+    result: tuple = field(compare=False, default=None)
+    error: str = field(compare=False, default=None)
+
+    def __post_init__(self):
+        self.sort_key = (self.arrival,)
+
+    @property
+    def n(self):
+        return self.problem.n
+
+    @property
+    def latency(self):
+        return None if self.done is None else self.done - self.arrival
+
+
+class _Model:
+    def __init__(self, mid, problem):
+        self.id = mid
+        self.problem = problem
+        self.h = None          # handle of the fit and its predicts (resident posterior)
+        self.hvg = None        # handle of evidence + gradient requests (own factor, L^-T, B^-1)
+        self.cap_m = 0         # predict rows the fit handle has workspace for
+        self.bytes = 0         # HBM held by the handles (as accounted)
+        self.busy = False
+        self.fitted = False
+        self.last_used = 0.0
+        self.dev = {}          # device tensors: X, y, theta, a, W
+
+    def footprint(self, fit, vg, cap_m):
+        p = self.problem
+        b = handle_bytes(p.n, p.d, p.kind, grad=False, m=cap_m) if fit else 0
+        if vg:
+            b += handle_bytes(p.n, p.d, p.kind, grad=True)
+        return b
+
+
+class Server:
+    """Continuous-batching request server on the current CUDA device."""
+
+    def __init__(self, workers=12, mem_budget=None, small_n=2048):
+        import torch
+
+        self.torch = torch
+        self.lib = N.load()
+        self.device = torch.device("cuda", torch.cuda.current_device())
+        free, _ = torch.cuda.mem_get_info(self.device)
+        self.budget = int(mem_budget if mem_budget is not None else 0.6 * free)
+        self.used = 0
+        self.small_n = small_n
+        self.models: dict[int, _Model] = {}
+        self.evicted = set()
+        self.lock = threading.Condition()
+        self.queue = []               # [(priority class, arrival, seq, request)]
+        self.seq = itertools.count()
+        self.stop = False
+        self.t0 = time.perf_counter()
+        self.evictions = 0
+        lo, hi = torch.cuda.Stream.priority_range()
+        self.workers = []
+        for w in range(workers):
+            # the first half of the workers run on high-priority streams and take small requests first
+            small_first = w < (workers + 1) // 2
+            stream = torch.cuda.Stream(device=self.device, priority=hi if small_first else lo)
+            t = threading.Thread(target=self._worker, args=(stream, small_first), daemon=True)
+            self.workers.append(t)
+            t.start()
+
+    # -- clock -----------------------------------------------------------------
+    def now(self):
+        return time.perf_counter() - self.t0
+
+    # -- submission -------------------------------------------------------------
+    def submit(self, req: Request):
+        with self.lock:
+            cls = 0 if req.n <= self.small_n else 1
+            self.queue.append((cls, req.arrival, next(self.seq), req))
+            self.lock.notify_all()
+
+    def close(self):
+        with self.lock:
+            self.stop = True
+            self.lock.notify_all()
+        for t in self.workers:
+            t.join()
+        for m in list(self.models.values()):
+            self._destroy(m)
+
+    # -- admission --------------------------------------------------------------
+    def _plan(self, req, m):
+        """(handles after the request: fit, vg, cap_m) for `req` on model `m`."""
+        fit, vg, cap = m.h is not None, m.hvg is not None, m.cap_m
+        if req.kind == "fit":
+            fit = True
+        elif req.kind == "vg":
+            vg = True
+        else:
+            cap = max(cap, -(-req.Xs.shape[0] // 128) * 128)
+        return fit, vg, cap
+
+    def _runnable(self, req):
+        """Called with the lock held: can `req` start now (model state, memory)?"""
+        m = self.models.get(req.model)
+        if req.kind == "predict" and (m is None or not m.fitted):
+            return False
+        if m is not None and m.busy:
+            return False
+        probe = m if m is not None else _Model(req.model, req.problem)
+        need = probe.footprint(*self._plan(req, probe)) - probe.bytes
+        if self.used + need > self.budget:
+            self._evict(self.used + need - self.budget, keep=req.model)
+            if self.used + need > self.budget:
+                return False
+        return True
+
+    def _evict(self, nbytes, keep):
+        idle = sorted((m for m in self.models.values() if not m.busy and m.id != keep), key=lambda m: m.last_used)
+        freed = 0
+        for m in idle:
+            if freed >= nbytes:
+                break
+            freed += m.bytes
+            self._destroy(m)
+            del self.models[m.id]
+            self.evicted.add(m.id)
+            self.evictions += 1
+
+    def _destroy(self, m):
+        for attr in ("h", "hvg"):
+            h = getattr(m, attr)
+            if h:
+                self.lib.pgb_gp_destroy(h)
+                setattr(m, attr, None)
+        self.used -= m.bytes
+        m.bytes = 0
+
+    def _take(self, small_first):
+        """Called with the lock held: the next runnable request, or None."""
+        key = (lambda x: x[:3]) if small_first else (lambda x: x[1:3])
+        for item in sorted(self.queue, key=key):
+            req = item[3]
+            if req.kind == "predict" and req.model in self.evicted and req.model not in self.models:
+                self.queue.remove(item)
+                req.error = "model evicted before the request"
+                req.start = req.done = self.now()
+                self.lock.notify_all()
+                continue
+            if self._runnable(req):
+                self.queue.remove(item)
+                m = self.models.get(req.model)
+                if m is None:
+                    m = _Model(req.model, req.problem)
+                    self.models[req.model] = m
+                m.busy = True
+                fit, vg, cap = self._plan(req, m)
+                grow = m.footprint(fit, vg, cap) - m.bytes
+                self.used += grow
+                m.bytes += grow
+                return req, m
+        return None
+
+    # -- execution ----------------------------------------------------------------
+    def _worker(self, stream, small_first):
+        torch = self.torch
+        torch.cuda.set_device(self.device)
+        while True:
+            with self.lock:
+                while True:
+                    if self.stop and not self.queue:
+                        return
+                    got = self._take(small_first)
+                    if got is not None:
+                        break
+                    self.lock.wait(timeout=0.002)
+            req, m = got
+            req.start = self.now()
+            try:
+                with torch.cuda.stream(stream):
+                    self._run(req, m, stream)
+                stream.synchronize()
+            except Exception as exc:   # reported per request
+                req.error = repr(exc)
+            req.done = self.now()
+            with self.lock:
+                m.busy = False
+                m.last_used = req.done
+                if req.kind == "predict" and req.error is None:
+                    m.cap_m = max(m.cap_m, -(-req.Xs.shape[0] // 128) * 128)
+                self.lock.notify_all()
+
+    def _upload(self, m):
+        torch = self.torch
+        p = m.problem
+        if "X" not in m.dev:
+            ydt = torch.int32 if p.J else torch.float32
+            m.dev["X"] = torch.from_numpy(np.ascontiguousarray(p.X, np.float32)).to(self.device, non_blocking=True)
+            m.dev["y"] = torch.from_numpy(np.ascontiguousarray(p.y)).to(self.device, ydt, non_blocking=True)
+
+    def _run(self, req, m, stream):
+        torch = self.torch
+        lib = self.lib
+        sh = stream.cuda_stream
+        p = req.problem
+        dev = self.device
+        self._upload(m)
+        d = m.dev
+        if req.kind == "fit":
+            if m.h is None:
+                h = C.c_void_p()
+                N.check(lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
+                m.h = h
+                d["a"] = torch.empty(p.n, dtype=torch.float32, device=dev)
+                d["W"] = torch.empty(p.n, dtype=torch.float32, device=dev)
+            d["theta"] = torch.from_numpy(np.asarray(p.theta, np.float32)).to(dev, non_blocking=True)
+            N.check(lib.pgb_approximate_posterior(m.h, d["X"].data_ptr(), d["y"].data_ptr(), d["theta"].data_ptr(),
+                                                  d["a"].data_ptr(), d["W"].data_ptr(), sh), "fit")
+            a = d["a"].to("cpu", non_blocking=True)
+            stream.synchronize()
+            m.fitted = True
+            req.result = (a.numpy(),)
+        elif req.kind == "vg":
+            if m.hvg is None:
+                h = C.c_void_p()
+                N.check(lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
+                m.hvg = h
+            th = req.theta if req.theta is not None else p.theta
+            theta = torch.from_numpy(np.asarray(th, np.float32)).to(dev, non_blocking=True)
+            out = torch.empty(1 + theta.numel(), dtype=torch.float32, device=dev)
+            N.check(lib.pgb_value_and_grad(m.hvg, d["X"].data_ptr(), d["y"].data_ptr(), theta.data_ptr(),
+                                           out.data_ptr(), out[1:].data_ptr(), sh), "value_and_grad")
+            host = out.to("cpu", non_blocking=True)
+            stream.synchronize()
+            req.result = (float(host[0]), host[1:].numpy())
+        else:
+            Xs = torch.from_numpy(np.ascontiguousarray(req.Xs, np.float32)).to(dev, non_blocking=True)
+            M = Xs.shape[0]
+            mean = torch.empty(M, dtype=torch.float32, device=dev)
+            var = torch.empty(M, dtype=torch.float32, device=dev)
+            N.check(lib.pgb_predict(m.h, d["X"].data_ptr(), d["theta"].data_ptr(), d["a"].data_ptr(),
+                                    d["W"].data_ptr(), Xs.data_ptr(), M, mean.data_ptr(), var.data_ptr(), 1, sh),
+                    "predict")
+            mh, vh = mean.to("cpu", non_blocking=True), var.to("cpu", non_blocking=True)
+            stream.synchronize()
+            req.result = (mh.numpy(), vh.numpy())
+
+    # -- open-loop replay --------------------------------------------------------
+    def replay(self, requests, realtime=True):
+        """Submit `requests` at their arrival times (seconds from now) and wait
+        for all of them; returns the requests with start/done times filled."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        self.t0 = time.perf_counter()
+        for r in reqs:
+            if realtime:
+                delay = r.arrival - self.now()
+                if delay > 0:
+                    time.sleep(delay)
+            self.submit(r)
+        while True:
+            with self.lock:
+                if all(r.done is not None for r in reqs):
+                    break
+                self.lock.wait(timeout=0.01)
+        return reqs
+
+
+def latency_summary(reqs, small_n=2048):
+    """p50 / p99 latency (ms) of all requests, per kind, and of n <= small_n."""
+    def pct(xs):
+        if not xs:
+            return None
+        xs = np.sort(np.asarray(xs)) * 1e3
+        return {"p50_ms": float(np.percentile(xs, 50)), "p99_ms": float(np.percentile(xs, 99)),
+                "mean_ms": float(xs.mean()), "count": int(xs.size)}
+
+    ok = [r for r in reqs if r.error is None and r.done is not None]
+    out = {"all": pct([r.latency for r in ok]),
+           f"n<={small_n}": pct([r.latency for r in ok if r.n <= small_n])}
+    for k in ("fit", "vg", "predict"):
+        out[k] = pct([r.latency for r in ok if r.kind == k])
+    span = max(r.done for r in ok) - min(r.arrival for r in reqs) if ok else 0.0
+    out["throughput_req_s"] = len(ok) / span if span > 0 else None
+    out["errors"] = sum(1 for r in reqs if r.error is not None)
+    return out

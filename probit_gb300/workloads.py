@@ -240,3 +240,51 @@ def hyperopt_c3(B=256, seed=3, device=None) -> list[Problem]:
         out.append(ordinal_problem(rng, N, 3, 5, "matern12", 1.0, 1.0, math.sqrt(0.4), _cut_interior(5),
                                    device=device))
     return out
+
+
+def serving_c4(rate=2000.0, duration=60.0, pool=256, seed=4, n_min=32, n_max=8192, device=None):
+    """The serving workload: a pool of `pool` ordinal GPs generated as in
+    ``batched_c2`` (N log-uniform in [n_min, n_max], D in 1..8, J in 2..7,
+    kernel in {EQ, Matern12, EQ.periodic(0.5)}) and Poisson arrivals at
+    `rate` requests/s for `duration` s: 70% predict (M log-uniform in
+    [1, 4096] test points ~ U[-2, 2]^D against a fitted model of the pool),
+    20% fit (refit of a pool model), 10% evidence + gradient (a pool model's
+    data at hyperparameters scaled by U[0.8, 1.25]).
+
+    Returns (problems, requests) with serving.Problem / serving.Request
+    objects; the caller fits every pool model before replaying the requests.
+    """
+    from . import serving as S
+
+    rng = np.random.default_rng(seed)
+    kinds = ["eq", "matern12", "eq_periodic"]
+    problems = []
+    for _ in range(pool):
+        N = int(round(math.exp(rng.uniform(math.log(n_min), math.log(n_max)))))
+        D = int(rng.integers(1, 9))
+        J = int(rng.integers(2, 8))
+        kind = kinds[int(rng.integers(0, 3))]
+        ell = math.exp(rng.uniform(math.log(0.3), math.log(3.0)))
+        s = math.exp(rng.uniform(math.log(0.5), math.log(2.0)))
+        p = ordinal_problem(rng, N, D, J, kind, ell, s, math.sqrt(0.4), _cut_interior(J), device=device)
+        problems.append(S.Problem(p.X, p.y, kind, p.theta().astype(np.float32), 1, J, p.period))
+    requests = []
+    t = 0.0
+    while True:
+        t += rng.exponential(1.0 / rate)
+        if t >= duration:
+            break
+        u = rng.uniform()
+        k = int(rng.integers(0, pool))
+        p = problems[k]
+        if u < 0.7:
+            M = int(round(math.exp(rng.uniform(0.0, math.log(4096)))))
+            Xs = rng.uniform(-2.0, 2.0, size=(M, p.d)).astype(np.float32)
+            requests.append(S.Request(t, "predict", k, p, Xs=Xs))
+        elif u < 0.9:
+            requests.append(S.Request(t, "fit", k, p))
+        else:
+            th = p.theta.copy()
+            th[:3] *= rng.uniform(0.8, 1.25, size=3).astype(np.float32)
+            requests.append(S.Request(t, "vg", k, p, theta=th))
+    return problems, requests
