@@ -249,10 +249,21 @@ std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const s
   return out;
 }
 
-template <class Tp>
-int upload(Tp* dst, const std::vector<Tp>& v) {
-  if (!v.empty()) CU_TRY(cudaMemcpy(dst, v.data(), v.size() * sizeof(Tp), cudaMemcpyHostToDevice));
+// Host -> device upload that has landed when it returns.  A plain cudaMemcpy
+// from pageable memory may return before its DMA reaches the device and is
+// not ordered with non-blocking streams, so work a caller then enqueues on
+// its own stream could read the old contents; the copy runs on `s` and `s` is
+// synchronised instead.
+int h2d(void* dst, const void* src, size_t bytes, cudaStream_t s) {
+  if (bytes == 0) return PGB_OK;
+  CU_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, s));
+  CU_TRY(cudaStreamSynchronize(s));
   return PGB_OK;
+}
+
+template <class Tp>
+int upload(Tp* dst, const std::vector<Tp>& v, cudaStream_t s) {
+  return h2d(dst, v.data(), v.size() * sizeof(Tp), s);
 }
 
 enum MapSlot { MAP_L = 0, MAP_LINV = 1, MAP_RV = 2, MAP_RZ = 3, MAPS_PER_PROB = 4 };
@@ -274,8 +285,7 @@ int upload_maps(Engine& e) {
     if (ok && q.Rz) ok = make_tile_map(m + MAP_RZ * 128, q.Rz, q.n_pad, q.ld, q.ld);
     if (!ok) return PGB_ECUDA;
   }
-  CU_TRY(cudaMemcpy(e.maps_all, h.data(), h.size(), cudaMemcpyHostToDevice));
-  return PGB_OK;
+  return h2d(e.maps_all, h.data(), h.size(), e.cap_s);
 }
 
 // Assign every device pointer of the engine from `base` (0: sizing pass).
@@ -406,9 +416,8 @@ void engine_free(Engine& e) {
 }
 
 int engine_upload_tables(Engine& e) {
-  CU_TRY(cudaMemcpy(e.probs, e.hp.data(), sizeof(Prob) * e.hp.size(), cudaMemcpyHostToDevice));
-  CU_TRY(cudaMemcpy(e.jobs, e.hjobs.data(), sizeof(DagJob) * e.hjobs.size(), cudaMemcpyHostToDevice));
-  return PGB_OK;
+  PGB_TRY(h2d(e.probs, e.hp.data(), sizeof(Prob) * e.hp.size(), e.cap_s));
+  return h2d(e.jobs, e.hjobs.data(), sizeof(DagJob) * e.hjobs.size(), e.cap_s);
 }
 
 // Build the engine of `count` problems: shapes, maps, task lists, one
@@ -540,15 +549,15 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   CU_TRY(cudaStreamSynchronize(e.cap_s));
   {
     const std::vector<int> ones(count, 1);
-    PGB_TRY(upload(e.enabled_all, ones));
+    PGB_TRY(upload(e.enabled_all, ones, e.cap_s));
   }
-  PGB_TRY(upload(e.vmap, e.h_vmap));
-  PGB_TRY(upload(e.bmap, e.h_bmap));
-  PGB_TRY(upload(e.claims, e.h_claims));
-  PGB_TRY(upload(e.syrk_tiles, e.h_syrk));
-  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k]));
-  for (MvGroup& g : e.mv) PGB_TRY(upload(g.map, g.h));
-  for (TraceGroup& g : e.tr) PGB_TRY(upload(g.tiles, g.h));
+  PGB_TRY(upload(e.vmap, e.h_vmap, e.cap_s));
+  PGB_TRY(upload(e.bmap, e.h_bmap, e.cap_s));
+  PGB_TRY(upload(e.claims, e.h_claims, e.cap_s));
+  PGB_TRY(upload(e.syrk_tiles, e.h_syrk, e.cap_s));
+  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
+  for (MvGroup& g : e.mv) PGB_TRY(upload(g.map, g.h, e.cap_s));
+  for (TraceGroup& g : e.tr) PGB_TRY(upload(g.tiles, g.h, e.cap_s));
   {
     const char* ev = std::getenv("PGB_EAGER");
     e.eager = (ev && ev[0] == '1') ? 1 : 0;
@@ -985,7 +994,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
     if (!gp->map_c) PGB_TRY(grab(&gp->map_c, 128));
     alignas(64) unsigned char m[128];
     if (!make_tile_map(m, gp->Rc, mpad, q.ld, q.ld)) return PGB_ECUDA;
-    CU_TRY(cudaMemcpy(gp->map_c, m, sizeof(m), cudaMemcpyHostToDevice));
+    PGB_TRY(h2d(gp->map_c, m, sizeof(m), e.cap_s));
     gp->cap_c = mpad;
   }
   if (gp->m_tasks != mt) {
@@ -996,7 +1005,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
     }
     std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0});
     PGB_TRY(ws_alloc(e.cap_s, reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)));
-    PGB_TRY(upload(gp->tasks_c, v));
+    PGB_TRY(upload(gp->tasks_c, v, e.cap_s));
     gp->ntasks_c = (int)v.size();
     gp->m_tasks = mt;
   }
