@@ -62,6 +62,9 @@ def parse():
     ap.add_argument("--hyperopt", type=int, default=256,
                     help="problems of the lockstep L-BFGS hyperparameter workload (0: skip)")
     ap.add_argument("--hyperopt-steps", type=int, default=50)
+    ap.add_argument("--serve-seconds", type=float, default=3.0,
+                    help="arrival window of the serving workload at 2000 req/s (0: skip)")
+    ap.add_argument("--serve-workers", type=int, default=12)
     return ap.parse_args()
 
 
@@ -452,6 +455,33 @@ def run_hyperopt(args, dev):
     return out
 
 
+def run_serving(args, dev):
+    """The serving workload: Poisson arrivals of fit / evidence+gradient /
+    predict requests against a pool of 256 resident GP models (generated as
+    the batched workload, N 32..8192), served with continuous batching; p50 /
+    p99 latency (arrival to result on the host) and throughput."""
+    from probit_gb300 import serving as S
+    from probit_gb300 import workloads as Wk
+
+    out = {"workers": args.serve_workers, "pool": 256}
+    for tag, rate, dur, seed in (("offered_2000_per_s", 2000.0, args.serve_seconds, 4),
+                                 ("offered_150_per_s", 150.0, max(2.0, args.serve_seconds), 5)):
+        probs, reqs = Wk.serving_c4(rate=rate, duration=dur, pool=256, seed=seed, device=dev)
+        srv = S.Server(workers=args.serve_workers)
+        try:
+            t0 = time.perf_counter()
+            srv.replay([S.Request(0.0, "fit", k, p) for k, p in enumerate(probs)], realtime=False)
+            prefit = time.perf_counter() - t0
+            done = srv.replay(reqs, realtime=True)
+            summ = S.latency_summary(done)
+            summ.update({"rate_req_s": rate, "window_s": dur, "requests": len(reqs), "prefit_s": prefit,
+                         "evictions": srv.evictions})
+        finally:
+            srv.close()
+        out[tag] = summ
+    return out
+
+
 def kernel_groups(probs):
     """(gradient-trace launches, Gram-matvec launches) of a batch: one per
     (feature width class, periodic) and per (kernel, feature width class)."""
@@ -607,6 +637,8 @@ def run_gb300(args, ws, rank, local):
         line["batched"] = run_batched(args, dev)
     if rank == 0 and ws == 1 and args.hyperopt > 0:
         line["hyperopt"] = run_hyperopt(args, dev)
+    if rank == 0 and ws == 1 and args.serve_seconds > 0:
+        line["served"] = run_serving(args, dev)
     if rank == 0:
         print(json.dumps(line), flush=True)
 

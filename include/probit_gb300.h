@@ -97,6 +97,13 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out);
 /* Release a handle and all its device memory (after its work completed). */
 int pgb_gp_destroy(pgb_gp* gp);
 
+/* Cap the persistent blocks of the handle's launches at max_blocks (0: one
+ * per SM, the default).  A server gives large problems a share of the SMs so
+ * that the launches of small requests on other streams run beside them
+ * instead of waiting for them.  This entry point has no counterpart in the
+ * reference. */
+int pgb_gp_set_max_blocks(pgb_gp* gp, int32_t max_blocks);
+
 /* Read the handle's device status word; synchronises `stream` first. */
 int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream);
 

@@ -80,6 +80,7 @@ _SIGS = {
     "pgb_gp_create": (C.c_int, [C.POINTER(Desc), C.POINTER(_VP)]),
     "pgb_gp_destroy": (C.c_int, [_VP]),
     "pgb_gp_status": (C.c_int, [_VP, C.POINTER(Status), _VP]),
+    "pgb_gp_set_max_blocks": (C.c_int, [_VP, C.c_int32]),
     "pgb_gram": (C.c_int, [C.POINTER(Desc), _VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int64, _VP]),
     "pgb_gram_noalloc": (C.c_int, [C.POINTER(Desc), _VP, _VP, C.c_int32, _VP, C.c_int32, _VP, C.c_int64, _VP]),
     "pgb_log_likelihood": (C.c_int, [C.POINTER(Desc), _VP, _VP, _VP, C.c_int32, _VP, _VP, _VP, _VP, _VP]),

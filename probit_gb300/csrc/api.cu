@@ -108,6 +108,7 @@ struct Engine {
   std::vector<size_t> x_off, y_off, th_off;   // offsets (elements) into the packed inputs
   size_t x_total = 0, y_total = 0, th_total = 0;
   int num_sms = 0, device = 0, dag_dm = 4, nt_max = 1;
+  int max_blocks = 0;                      // cap on persistent blocks per launch (0: one per SM)
   std::vector<Prob> hp;                    // host copy of the problem table
   Prob* probs = nullptr;
   void* arena = nullptr;                   // everything but the gradient matrices
@@ -602,8 +603,9 @@ int ensure_grad_buffers(Engine& e) {
   return PGB_OK;
 }
 
-int dag_grid(const Engine& e, int ntasks) { return std::max(1, std::min(e.num_sms, ntasks)); }
-int trsv_grid(const Engine& e) { return std::max(1, std::min(e.nclaims, 4 * e.num_sms)); }
+int block_cap(const Engine& e) { return e.max_blocks > 0 ? std::min(e.max_blocks, e.num_sms) : e.num_sms; }
+int dag_grid(const Engine& e, int ntasks) { return std::max(1, std::min(block_cap(e), ntasks)); }
+int trsv_grid(const Engine& e) { return std::max(1, std::min(e.nclaims, 4 * block_cap(e))); }
 
 // ---------------------------------------------------------------- enqueue helpers
 void enq_matvec(Engine& e, MatvecOp op, cudaStream_t s) {
@@ -830,6 +832,19 @@ int pgb_gp_destroy(pgb_gp* gp) {
     for (void* p : ptrs) ws_free(gp->e.cap_s, p);
   engine_free(gp->e);
   delete gp;
+  return PGB_OK;
+}
+
+int pgb_gp_set_max_blocks(pgb_gp* gp, int32_t max_blocks) {
+  if (!gp || max_blocks < 0) return PGB_EINVAL;
+  Engine& e = gp->e;
+  if (e.max_blocks == max_blocks) return PGB_OK;
+  e.max_blocks = max_blocks;
+  for (int k = 0; k < OP_COUNT; ++k)   // graphs were captured with the old grid sizes
+    if (e.gexec[k]) {
+      cudaGraphExecDestroy(e.gexec[k]);
+      e.gexec[k] = nullptr;
+    }
   return PGB_OK;
 }
 

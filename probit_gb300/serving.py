@@ -31,6 +31,7 @@ posterior.
 from __future__ import annotations
 
 import ctypes as C
+import heapq
 import itertools
 import threading
 import time
@@ -140,7 +141,7 @@ class _Model:
 class Server:
     """Continuous-batching request server on the current CUDA device."""
 
-    def __init__(self, workers=12, mem_budget=None, small_n=2048):
+    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64):
         import torch
 
         self.torch = torch
@@ -150,10 +151,11 @@ class Server:
         self.budget = int(mem_budget if mem_budget is not None else 0.6 * free)
         self.used = 0
         self.small_n = small_n
+        self.large_blocks = large_blocks   # SM share of the launches of a problem with n > small_n
         self.models: dict[int, _Model] = {}
         self.evicted = set()
         self.lock = threading.Condition()
-        self.queue = []               # [(priority class, arrival, seq, request)]
+        self.heaps = ([], [])         # small / large requests: (arrival, seq, request)
         self.seq = itertools.count()
         self.stop = False
         self.t0 = time.perf_counter()
@@ -176,8 +178,11 @@ class Server:
     def submit(self, req: Request):
         with self.lock:
             cls = 0 if req.n <= self.small_n else 1
-            self.queue.append((cls, req.arrival, next(self.seq), req))
+            heapq.heappush(self.heaps[cls], (req.arrival, next(self.seq), req))
             self.lock.notify_all()
+
+    def _pending(self):
+        return bool(self.heaps[0] or self.heaps[1])
 
     def close(self):
         with self.lock:
@@ -236,30 +241,51 @@ class Server:
         self.used -= m.bytes
         m.bytes = 0
 
-    def _take(self, small_first):
-        """Called with the lock held: the next runnable request, or None."""
-        key = (lambda x: x[:3]) if small_first else (lambda x: x[1:3])
-        for item in sorted(self.queue, key=key):
-            req = item[3]
+    def _take(self, small_first, scan=64):
+        """Called with the lock held: the next runnable request, or None.
+
+        Small-first workers look at the small requests first; the others take
+        the earliest arrival of either class.  Up to `scan` requests whose
+        model is busy (or that do not fit in memory yet) are stepped over and
+        put back."""
+        skipped = []
+        found = None
+        for _ in range(scan):
+            heaps = self.heaps
+            if small_first:
+                h = heaps[0] if heaps[0] else heaps[1]
+            elif heaps[0] and heaps[1]:
+                h = heaps[0] if heaps[0][0] < heaps[1][0] else heaps[1]
+            else:
+                h = heaps[0] if heaps[0] else heaps[1]
+            if not h:
+                break
+            item = heapq.heappop(h)
+            req = item[2]
             if req.kind == "predict" and req.model in self.evicted and req.model not in self.models:
-                self.queue.remove(item)
                 req.error = "model evicted before the request"
                 req.start = req.done = self.now()
                 self.lock.notify_all()
                 continue
             if self._runnable(req):
-                self.queue.remove(item)
-                m = self.models.get(req.model)
-                if m is None:
-                    m = _Model(req.model, req.problem)
-                    self.models[req.model] = m
-                m.busy = True
-                fit, vg, cap = self._plan(req, m)
-                grow = m.footprint(fit, vg, cap) - m.bytes
-                self.used += grow
-                m.bytes += grow
-                return req, m
-        return None
+                found = req
+                break
+            skipped.append((h, item))
+        for h, item in skipped:
+            heapq.heappush(h, item)
+        if found is None:
+            return None
+        req = found
+        m = self.models.get(req.model)
+        if m is None:
+            m = _Model(req.model, req.problem)
+            self.models[req.model] = m
+        m.busy = True
+        fit, vg, cap = self._plan(req, m)
+        grow = m.footprint(fit, vg, cap) - m.bytes
+        self.used += grow
+        m.bytes += grow
+        return req, m
 
     # -- execution ----------------------------------------------------------------
     def _worker(self, stream, small_first):
@@ -268,7 +294,7 @@ class Server:
         while True:
             with self.lock:
                 while True:
-                    if self.stop and not self.queue:
+                    if self.stop and not self._pending():
                         return
                     got = self._take(small_first)
                     if got is not None:
@@ -298,6 +324,13 @@ class Server:
             m.dev["X"] = torch.from_numpy(np.ascontiguousarray(p.X, np.float32)).to(self.device, non_blocking=True)
             m.dev["y"] = torch.from_numpy(np.ascontiguousarray(p.y)).to(self.device, ydt, non_blocking=True)
 
+    def _create(self, p):
+        h = C.c_void_p()
+        N.check(self.lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
+        if p.n > self.small_n and self.large_blocks:
+            N.check(self.lib.pgb_gp_set_max_blocks(h, self.large_blocks), "pgb_gp_set_max_blocks")
+        return h
+
     def _run(self, req, m, stream):
         torch = self.torch
         lib = self.lib
@@ -308,9 +341,7 @@ class Server:
         d = m.dev
         if req.kind == "fit":
             if m.h is None:
-                h = C.c_void_p()
-                N.check(lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
-                m.h = h
+                m.h = self._create(p)
                 d["a"] = torch.empty(p.n, dtype=torch.float32, device=dev)
                 d["W"] = torch.empty(p.n, dtype=torch.float32, device=dev)
             d["theta"] = torch.from_numpy(np.asarray(p.theta, np.float32)).to(dev, non_blocking=True)
@@ -322,9 +353,7 @@ class Server:
             req.result = (a.numpy(),)
         elif req.kind == "vg":
             if m.hvg is None:
-                h = C.c_void_p()
-                N.check(lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
-                m.hvg = h
+                m.hvg = self._create(p)
             th = req.theta if req.theta is not None else p.theta
             theta = torch.from_numpy(np.asarray(th, np.float32)).to(dev, non_blocking=True)
             out = torch.empty(1 + theta.numel(), dtype=torch.float32, device=dev)
@@ -376,6 +405,7 @@ def latency_summary(reqs, small_n=2048):
 
     ok = [r for r in reqs if r.error is None and r.done is not None]
     out = {"all": pct([r.latency for r in ok]),
+           "service_all": pct([r.done - r.start for r in ok]),
            f"n<={small_n}": pct([r.latency for r in ok if r.n <= small_n])}
     for k in ("fit", "vg", "predict"):
         out[k] = pct([r.latency for r in ok if r.kind == k])
