@@ -160,31 +160,39 @@ __device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, con
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// 32 x 32 Cholesky in one warp's registers: lane l owns row l (d[m] = A[l][m],
-// m <= l).  Column C: pivot from lane C by shuffle, scale, rank-1 update of
-// the later columns with the pivot column broadcast lane by lane.  The column
-// loop is unrolled by template recursion so every index is a compile-time
-// constant and the row stays in registers.
-template <int C>
-__device__ __forceinline__ void potrf32_col(float (&d)[32], int lane, int& bad) {
-  if constexpr (C < 32) {
-    const float piv = __shfl_sync(FULL, d[C], C);
+// 32 x 32 Cholesky of the lower triangle of the block at A (row stride
+// SC_LD) by one warp: lane l holds row l in registers.  Column C: the pivot
+// from lane C by shuffle, the lanes below scale their entry, then every lane
+// updates its later entries with the scaled column, broadcast lane by lane.
+// After each column the row is shifted left by one register, so the active
+// column is always d[0]: the column loop stays a loop (a fully unrolled
+// version is ~20 KB of straight-line code that runs at instruction-fetch
+// latency inside the factorisation kernel) while every register index is a
+// compile-time constant.  Same operations, same order per element as the
+// unrolled form.  The final L is written back as each column completes;
+// srd[l] = 1 / L[l][l].
+__device__ __forceinline__ void warp_potrf32(float* A, float* srd, int lane, int col0, int* status) {
+  float d[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) d[m] = A[lane * SC_LD + m];
+  int bad = -1;
+#pragma unroll 1
+  for (int C = 0; C < 32; ++C) {
+    const float piv = __shfl_sync(FULL, d[0], C);
     if (!(piv > 0.0f) && bad < 0) bad = C;
     const float lc = sqrtf(piv);
-    const float dc = (lane == C) ? lc : ((lane > C) ? d[C] / lc : d[C]);
-    d[C] = dc;
+    const float dc = (lane == C) ? lc : ((lane > C) ? d[0] / lc : d[0]);
+    if (lane >= C) A[lane * SC_LD + C] = dc;
 #pragma unroll
-    for (int m = C + 1; m < 32; ++m) {
-      const float lmc = __shfl_sync(FULL, dc, m);
-      if (lane >= m) d[m] = fmaf(-dc, lmc, d[m]);
+    for (int m = 1; m < 32; ++m) {
+      const float lm = __shfl_sync(FULL, dc, (C + m) & 31);
+      if (lane >= C + m) d[m] = fmaf(-dc, lm, d[m]);
     }
-    potrf32_col<C + 1>(d, lane, bad);
+#pragma unroll
+    for (int m = 0; m < 31; ++m) d[m] = d[m + 1];
   }
-}
-
-__device__ __forceinline__ void warp_potrf32(float (&d)[32], int lane, int col0, int* status) {
-  int bad = -1;
-  potrf32_col<0>(d, lane, bad);
+  __syncwarp();
+  srd[lane] = __frcp_rn(A[lane * SC_LD + lane]);
   if (lane == 0 && bad >= 0) {
     atomicMin(status + ST_NOTPD_COL, col0 + bad);
     atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
@@ -193,7 +201,9 @@ __device__ __forceinline__ void warp_potrf32(float (&d)[32], int lane, int col0,
 
 // Row substitution x[c] = (x[c] - sum_{m<c} x[m] L[c][m]) / L[c][c] for a
 // 32-wide block, L rows read from shared memory (row stride SC_LD), unrolled
-// by template recursion.
+// by template recursion: it runs on up to 128 threads at once, which share
+// the instruction fetch, and its independent loads give the warps enough
+// instruction-level parallelism (a loop form measured 5-10x slower here).
 template <int C>
 __device__ __forceinline__ void subst32_col(float (&x)[32], const float* Lb, const float* rdiag) {
   if constexpr (C < 32) {
@@ -203,6 +213,15 @@ __device__ __forceinline__ void subst32_col(float (&x)[32], const float* Lb, con
     x[C] = acc * rdiag[C];
     subst32_col<C + 1>(x, Lb, rdiag);
   }
+}
+
+__device__ __forceinline__ void subst32_row(float* xs, const float* Lb, const float* rdiag) {
+  float x[32];
+#pragma unroll
+  for (int m = 0; m < 32; ++m) x[m] = xs[m];
+  subst32_col<0>(x, Lb, rdiag);
+#pragma unroll
+  for (int m = 0; m < 32; ++m) xs[m] = x[m];
 }
 
 // Column `lane` of the inverse of a 32 x 32 lower-triangular block:
@@ -219,37 +238,19 @@ __device__ __forceinline__ void inv32_row(float (&y)[32], const float* Lb, int l
 }
 
 // In-place Cholesky of the lower triangle of the 128 x 128 tile in sC:
-// 32-wide panels; warp 0 factors the diagonal block in registers, one thread
-// per row solves the panel below (row in registers, L rows broadcast from
-// shared memory, reciprocal pivots in srd), 4 x 4 register blocks update the
-// trailing lower triangle.
+// 32-wide panels; warp 0 factors the diagonal block, one thread per row
+// solves the panel below (L rows broadcast from shared memory, reciprocal
+// pivots in srd), 4 x 4 register blocks update the trailing lower triangle.
 __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, unsigned long long* pt = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = 0; jb < T; jb += 32) {
     if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
-    if (warp == 0) {
-      float d[32];
-#pragma unroll
-      for (int m = 0; m < 32; ++m) d[m] = sC[(jb + lane) * SC_LD + jb + m];
-      warp_potrf32(d, lane, col0 + jb, status);
-#pragma unroll
-      for (int m = 0; m < 32; ++m)
-        if (m <= lane) sC[(jb + lane) * SC_LD + jb + m] = d[m];
-      srd[lane] = __frcp_rn(d[lane]);
-    }
+    if (warp == 0) warp_potrf32(sC + jb * SC_LD + jb, srd, lane, col0 + jb, status);
     __syncthreads();
     if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
     const int rem = T - jb - 32;
     if (rem > 0) {
-      if (tid < rem) {
-        const int r = jb + 32 + tid;
-        float x[32];
-#pragma unroll
-        for (int m = 0; m < 32; ++m) x[m] = sC[r * SC_LD + jb + m];
-        subst32_col<0>(x, sC + jb * SC_LD + jb, srd);
-#pragma unroll
-        for (int m = 0; m < 32; ++m) sC[r * SC_LD + jb + m] = x[m];
-      }
+      if (tid < rem) subst32_row(sC + (jb + 32 + tid) * SC_LD + jb, sC + jb * SC_LD + jb, srd);
       __syncthreads();
       if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
       const int nb = rem / 4;
@@ -286,8 +287,7 @@ __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, unsigne
 }
 
 // sL (lower) = inverse of the lower-triangular 128 x 128 L in sC.
-// Diagonal 32 x 32 blocks: warp b solves L_bb y = e_l for column l in lane
-// l's registers.  Off-diagonal blocks by distance:
+// Diagonal 32 x 32 blocks: warp b solves L_bb y = e_l for column l in lane l.  Off-diagonal blocks by distance:
 //   Linv_rc = -Linv_rr * sum_{c <= m < r} L_rm Linv_mc,
 // the partial sum P_rc kept in the (unused) upper block (c, r) of sL.
 __device__ void trinv_tile(const float* sC, float* sL) {
@@ -326,7 +326,7 @@ __device__ void trinv_tile(const float* sC, float* sL) {
 }
 
 // X L^T = C in place for the 128 rows of sC (L lower in sL), by 32-column
-// blocks: one thread per row solves a block with the row in registers, then
+// blocks: one thread per row solves a block of its row, then
 // 4 x 4 register blocks update the remaining columns.  Used on the critical
 // path (the sub-diagonal tile), where waiting for L^-1 would cost more.
 __device__ void trsm_subst(float* sC, const float* sL, float* srd) {
@@ -334,15 +334,7 @@ __device__ void trsm_subst(float* sC, const float* sL, float* srd) {
   if (tid < T) srd[tid] = __frcp_rn(sL[tid * SC_LD + tid]);
   __syncthreads();
   for (int cb = 0; cb < T; cb += 32) {
-    if (tid < T) {
-      const int r = tid;
-      float x[32];
-#pragma unroll
-      for (int m = 0; m < 32; ++m) x[m] = sC[r * SC_LD + cb + m];
-      subst32_col<0>(x, sL + cb * SC_LD + cb, srd + cb);
-#pragma unroll
-      for (int m = 0; m < 32; ++m) sC[r * SC_LD + cb + m] = x[m];
-    }
+    if (tid < T) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
     __syncthreads();
     const int rem = T - cb - 32;
     if (rem > 0) {
