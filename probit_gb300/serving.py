@@ -14,7 +14,8 @@ one GPU:
   CUDA stream, so the kernels of different requests overlap on the device
   (the tile-DAG launches of small problems use a few SMs each); requests of
   small problems (n <= ``small_n``) go to higher-priority streams and are
-  taken first;
+  taken first, some workers take only them, and large problems' launches are
+  capped at ``large_blocks`` persistent blocks so small ones run beside them;
 * a model is used by one request at a time (a handle is not thread-safe);
   other requests for it wait in the queue.
 
@@ -141,7 +142,7 @@ class _Model:
 class Server:
     """Continuous-batching request server on the current CUDA device."""
 
-    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64):
+    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4):
         import torch
 
         self.torch = torch
@@ -161,12 +162,20 @@ class Server:
         self.t0 = time.perf_counter()
         self.evictions = 0
         lo, hi = torch.cuda.Stream.priority_range()
+        small_only = min(small_only, max(0, workers - 2))   # at least two workers take large requests
         self.workers = []
         for w in range(workers):
-            # the first half of the workers run on high-priority streams and take small requests first
-            small_first = w < (workers + 1) // 2
-            stream = torch.cuda.Stream(device=self.device, priority=hi if small_first else lo)
-            t = threading.Thread(target=self._worker, args=(stream, small_first), daemon=True)
+            # roles: the first `small_only` workers take only small requests (so a
+            # small request never waits behind large ones for a worker), then half
+            # the rest prefer small requests; both run on high-priority streams
+            if w < small_only:
+                role = "small"
+            elif w < small_only + (workers - small_only + 1) // 2:
+                role = "small_first"
+            else:
+                role = "any"
+            stream = torch.cuda.Stream(device=self.device, priority=lo if role == "any" else hi)
+            t = threading.Thread(target=self._worker, args=(stream, role), daemon=True)
             self.workers.append(t)
             t.start()
 
@@ -241,18 +250,20 @@ class Server:
         self.used -= m.bytes
         m.bytes = 0
 
-    def _take(self, small_first, scan=64):
+    def _take(self, role, scan=64):
         """Called with the lock held: the next runnable request, or None.
 
-        Small-first workers look at the small requests first; the others take
-        the earliest arrival of either class.  Up to `scan` requests whose
-        model is busy (or that do not fit in memory yet) are stepped over and
-        put back."""
+        "small" workers take only small requests, "small_first" workers look
+        at the small requests first, "any" workers take the earliest arrival
+        of either class.  Up to `scan` requests whose model is busy (or that
+        do not fit in memory yet) are stepped over and put back."""
         skipped = []
         found = None
         for _ in range(scan):
             heaps = self.heaps
-            if small_first:
+            if role == "small":
+                h = heaps[0]
+            elif role == "small_first":
                 h = heaps[0] if heaps[0] else heaps[1]
             elif heaps[0] and heaps[1]:
                 h = heaps[0] if heaps[0][0] < heaps[1][0] else heaps[1]
@@ -288,7 +299,7 @@ class Server:
         return req, m
 
     # -- execution ----------------------------------------------------------------
-    def _worker(self, stream, small_first):
+    def _worker(self, stream, role):
         torch = self.torch
         torch.cuda.set_device(self.device)
         while True:
@@ -296,7 +307,7 @@ class Server:
                 while True:
                     if self.stop and not self._pending():
                         return
-                    got = self._take(small_first)
+                    got = self._take(role)
                     if got is not None:
                         break
                     self.lock.wait(timeout=0.002)
