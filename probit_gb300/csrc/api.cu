@@ -371,13 +371,14 @@ size_t layout(Engine& e, uintptr_t base) {
       j.theta = q.theta;
       j.sh = s;
       j.ready = e.ready_all + ready_off;
+      j.progress = e.ready_all + ready_off + 2 * (size_t)nt * nt;
       j.status = q.status;
       j.reuse = q.reuse + 2;
       j.reuse_mode = 0;
       j.tm_L = map_slot(e, p, MAP_L);
       j.tm_Linv = map_slot(e, p, MAP_LINV);
     }
-    ready_off += 2 * (size_t)nt * nt;
+    ready_off += 2 * (size_t)nt * nt + nt;
     DagJob* jb = &e.hjobs[(size_t)p * JOB_COUNT];
     jb[JOB_VEC].rhs_kind = RHS_VEC;
     jb[JOB_VEC].nrt = 1;
@@ -450,7 +451,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     e.x_total += (size_t)descs[p].n * descs[p].d;
     e.y_total += (size_t)descs[p].n;
     e.th_total += (size_t)e.th[p];
-    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p];
+    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p] + e.nt[p];
     e.tflags_words += 2 * (size_t)e.nt[p];
     e.dag_dm = std::max(e.dag_dm, dm_of(e.sh[p].Dp));
     e.nt_max = std::max(e.nt_max, e.nt[p]);

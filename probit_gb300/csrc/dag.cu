@@ -168,9 +168,10 @@ constexpr unsigned FULL = 0xffffffffu;
 // column is always d[0]: the column loop stays a loop (a fully unrolled
 // version is ~20 KB of straight-line code that runs at instruction-fetch
 // latency inside the factorisation kernel) while every register index is a
-// compile-time constant.  Same operations, same order per element as the
-// unrolled form.  The final L is written back as each column completes;
-// srd[l] = 1 / L[l][l].
+// compile-time constant.  The column is scaled by the correctly rounded
+// reciprocal of its pivot (one rounding more than a division, off the
+// serial chain's slow path).  The final L is written back as each column
+// completes; srd[l] = 1 / L[l][l].
 __device__ __forceinline__ void warp_potrf32(float* A, float* srd, int lane, int col0, int* status) {
   float d[32];
 #pragma unroll
@@ -181,7 +182,8 @@ __device__ __forceinline__ void warp_potrf32(float* A, float* srd, int lane, int
     const float piv = __shfl_sync(FULL, d[0], C);
     if (!(piv > 0.0f) && bad < 0) bad = C;
     const float lc = sqrtf(piv);
-    const float dc = (lane == C) ? lc : ((lane > C) ? d[0] / lc : d[0]);
+    const float rl = __frcp_rn(lc);
+    const float dc = (lane == C) ? lc : ((lane > C) ? d[0] * rl : d[0]);
     if (lane >= C) A[lane * SC_LD + C] = dc;
 #pragma unroll
     for (int m = 1; m < 32; ++m) {
@@ -241,7 +243,25 @@ __device__ __forceinline__ void inv32_row(float (&y)[32], const float* Lb, int l
 // 32-wide panels; warp 0 factors the diagonal block, one thread per row
 // solves the panel below (L rows broadcast from shared memory, reciprocal
 // pivots in srd), 4 x 4 register blocks update the trailing lower triangle.
-__device__ void potrf_tile(float* sC, float* srd, int col0, int* status, unsigned long long* pt = nullptr) {
+// Panel p of the factor (columns 32p .. 32p+31) is final once its diagonal
+// block and the rows below are solved; it is then written to dst (row stride
+// ld; zeros above the diagonal) and `progress` is released to p + 1, so the
+// sub-diagonal tile can start its substitution with it while the later
+// panels are factored.
+__device__ __forceinline__ void publish_panel(const float* sC, float* dst, long long ld, int* progress, int jb) {
+  for (int e = threadIdx.x; e < T * 32; e += DAG_THREADS) {
+    const int r = e >> 5, c = jb + (e & 31);
+    dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    st_release(progress, jb / 32 + 1);
+  }
+}
+
+__device__ void potrf_tile(float* sC, float* srd, int col0, int* status, float* dst, long long ld, int* progress,
+                           unsigned long long* pt = nullptr) {
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = 0; jb < T; jb += 32) {
     if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
@@ -249,9 +269,11 @@ __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, unsigne
     __syncthreads();
     if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
     const int rem = T - jb - 32;
+    if (rem <= 0) publish_panel(sC, dst, ld, progress, jb);
     if (rem > 0) {
       if (tid < rem) subst32_row(sC + (jb + 32 + tid) * SC_LD + jb, sC + jb * SC_LD + jb, srd);
       __syncthreads();
+      publish_panel(sC, dst, ld, progress, jb);
       if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
       const int nb = rem / 4;
       for (int blk = tid; blk < nb * nb; blk += DAG_THREADS) {
@@ -325,47 +347,46 @@ __device__ void trinv_tile(const float* sC, float* sL) {
   }
 }
 
-// X L^T = C in place for the 128 rows of sC (L lower in sL), by 32-column
-// blocks: one thread per row solves a block of its row, then
-// 4 x 4 register blocks update the remaining columns.  Used on the critical
-// path (the sub-diagonal tile), where waiting for L^-1 would cost more.
-__device__ void trsm_subst(float* sC, const float* sL, float* srd) {
+// X L^T = C in place for the 128 rows of sC, by 32-column blocks: block cb
+// needs panel cb of L (rows cb.., columns cb .. cb+31) in sL; one thread per
+// row solves the block of its row, then 4 x 4 register blocks update the
+// remaining columns.  Used on the critical path (the sub-diagonal tile),
+// panel by panel as the diagonal tile publishes them.
+__device__ void trsm_subst_block(float* sC, const float* sL, float* srd, int cb) {
   const int tid = threadIdx.x;
-  if (tid < T) srd[tid] = __frcp_rn(sL[tid * SC_LD + tid]);
+  if (tid < 32) srd[cb + tid] = __frcp_rn(sL[(cb + tid) * SC_LD + cb + tid]);
   __syncthreads();
-  for (int cb = 0; cb < T; cb += 32) {
-    if (tid < T) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
-    __syncthreads();
-    const int rem = T - cb - 32;
-    if (rem > 0) {
-      const int nbc = rem / 4;   // 4-column groups
-      for (int blk = tid; blk < (T / 4) * nbc; blk += DAG_THREADS) {
-        const int r0 = (blk / nbc) * 4, c0 = cb + 32 + (blk % nbc) * 4;
-        float acc[4][4];
+  if (tid < T) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
+  __syncthreads();
+  const int rem = T - cb - 32;
+  if (rem > 0) {
+    const int nbc = rem / 4;   // 4-column groups
+    for (int blk = tid; blk < (T / 4) * nbc; blk += DAG_THREADS) {
+      const int r0 = (blk / nbc) * 4, c0 = cb + 32 + (blk % nbc) * 4;
+      float acc[4][4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q)
+      for (int q = 0; q < 4; ++q)
 #pragma unroll
-          for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
+        for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
 #pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-          float a[4], b[4];
+      for (int m = 0; m < 32; ++m) {
+        float a[4], b[4];
 #pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            a[q] = sC[(r0 + q) * SC_LD + cb + m];
-            b[q] = sL[(c0 + q) * SC_LD + cb + m];
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
+        for (int q = 0; q < 4; ++q) {
+          a[q] = sC[(r0 + q) * SC_LD + cb + m];
+          b[q] = sL[(c0 + q) * SC_LD + cb + m];
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
-          for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
+          for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
       }
-      __syncthreads();
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
     }
+    __syncthreads();
   }
 }
 
@@ -635,12 +656,8 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   if (!is_rhs && i == j) {
     // L_jj = chol(C), published (flag 1) before its inverse (flag 2), so the
     // sub-diagonal tile can start while the inverse is computed
-    potrf_tile(sC, sX, j * T, jb.status, jb.ptrace ? jb.ptrace + (size_t)j * 16 : nullptr);
-    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
-      const int r = e >> 7, c = e & (T - 1);
-      dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
-    }
-    __syncthreads();
+    potrf_tile(sC, sX, j * T, jb.status, dst, ld, jb.progress + j,
+               jb.ptrace ? jb.ptrace + (size_t)j * 16 : nullptr);
     if (jb.ptrace && threadIdx.x == 0) jb.ptrace[(size_t)j * 16 + 12] = global_ns();
     if (threadIdx.x == 0) {
       if (tr) tr[5] = global_ns();
@@ -653,15 +670,17 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       Linv_j[(size_t)r * T + c] = c <= r ? sL[r * SC_LD + c] : 0.0f;
     }
   } else if (!is_rhs && i == j + 1) {
-    // critical path: substitution with L_jj as soon as it is published
-    if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 1)) return;
+    // critical path: substitution with each panel of L_jj as soon as it is published
     const float* Ljj = jb.L + (size_t)j * T * ld + (size_t)j * T;
-    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
-      const int r = e >> 7, c = e & (T - 1);
-      sL[r * SC_LD + c] = c <= r ? __ldcg(Ljj + (size_t)r * ld + c) : 0.0f;
+    for (int cb = 0; cb < T; cb += 32) {
+      if (!block_wait(jb.progress + j, jb.status, s_ok + 2, cb / 32 + 1)) return;
+      for (int e = threadIdx.x; e < (T - cb) * 32; e += DAG_THREADS) {
+        const int r = cb + (e >> 5), c = cb + (e & 31);
+        sL[r * SC_LD + c] = __ldcg(Ljj + (size_t)r * ld + c);
+      }
+      __syncthreads();
+      trsm_subst_block(sC, sL, sX, cb);
     }
-    __syncthreads();
-    trsm_subst(sC, sL, sX);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
