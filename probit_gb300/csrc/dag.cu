@@ -162,36 +162,50 @@ constexpr unsigned FULL = 0xffffffffu;
 
 // 32 x 32 Cholesky of the lower triangle of the block at A (row stride
 // SC_LD) by one warp: lane l holds row l in registers.  Column C: the pivot
-// from lane C by shuffle, the lanes below scale their entry, then every lane
-// updates its later entries with the scaled column, broadcast lane by lane.
-// After each column the row is shifted left by one register, so the active
-// column is always d[0]: the column loop stays a loop (a fully unrolled
-// version is ~20 KB of straight-line code that runs at instruction-fetch
-// latency inside the factorisation kernel) while every register index is a
-// compile-time constant.  The column is scaled by the correctly rounded
-// reciprocal of its pivot (one rounding more than a division, off the
-// serial chain's slow path).  The final L is written back as each column
-// completes; srd[l] = 1 / L[l][l].
-__device__ __forceinline__ void warp_potrf32(float* A, float* srd, int lane, int col0, int* status) {
+// from lane C by shuffle; every lane scales its entry by the pivot's
+// reciprocal square root and puts it in a 32-float line of shared memory at
+// position (l - C) mod 32, so that the later columns' multipliers sit at
+// fixed positions 1..31 and come back as eight 16-byte broadcast loads; then
+// every lane updates its later entries.  Entries above the diagonal are
+// updated too (no per-entry predicate) and never written back.  The line is
+// double-buffered by column parity, so one __syncwarp per column orders the
+// store before the loads.  Every 4 columns the row is shifted left by 4
+// registers: the column loop stays a small loop (a fully unrolled version is
+// ~20 KB of straight-line code that runs at instruction-fetch latency inside
+// the factorisation kernel) while every register index is a compile-time
+// constant.  The final L is written back as each column completes;
+// srd[l] = 1 / L[l][l].  sbuf: 64 floats, 16-byte aligned.
+__device__ __forceinline__ void warp_potrf32(float* A, float* srd, float* sbuf, int lane, int col0, int* status) {
   float d[32];
 #pragma unroll
   for (int m = 0; m < 32; ++m) d[m] = A[lane * SC_LD + m];
   int bad = -1;
 #pragma unroll 1
-  for (int C = 0; C < 32; ++C) {
-    const float piv = __shfl_sync(FULL, d[0], C);
-    if (!(piv > 0.0f) && bad < 0) bad = C;
-    const float lc = sqrtf(piv);
-    const float rl = __frcp_rn(lc);
-    const float dc = (lane == C) ? lc : ((lane > C) ? d[0] * rl : d[0]);
-    if (lane >= C) A[lane * SC_LD + C] = dc;
+  for (int C0 = 0; C0 < 32; C0 += 4) {
 #pragma unroll
-    for (int m = 1; m < 32; ++m) {
-      const float lm = __shfl_sync(FULL, dc, (C + m) & 31);
-      if (lane >= C + m) d[m] = fmaf(-dc, lm, d[m]);
+    for (int k = 0; k < 4; ++k) {
+      const int C = C0 + k;
+      float* line = sbuf + 32 * (k & 1);
+      const float piv = __shfl_sync(FULL, d[k], C);
+      if (!(piv > 0.0f) && bad < 0) bad = C;
+      const float rl = rsqrtf(piv);
+      const float dc = (lane == C) ? piv * rl : d[k] * rl;
+      if (lane >= C) A[lane * SC_LD + C] = dc;
+      line[(lane - C) & 31] = dc;
+      __syncwarp();
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const float4 v = reinterpret_cast<const float4*>(line)[q];
+        const float lv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const int m = 4 * q + e;
+          if (m >= 1 && k + m < 32) d[k + m] = fmaf(-dc, lv[e], d[k + m]);
+        }
+      }
     }
 #pragma unroll
-    for (int m = 0; m < 31; ++m) d[m] = d[m + 1];
+    for (int m = 0; m < 28; ++m) d[m] = d[m + 4];
   }
   __syncwarp();
   srd[lane] = __frcp_rn(A[lane * SC_LD + lane]);
@@ -265,7 +279,7 @@ __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, float* 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   for (int jb = 0; jb < T; jb += 32) {
     if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
-    if (warp == 0) warp_potrf32(sC + jb * SC_LD + jb, srd, lane, col0 + jb, status);
+    if (warp == 0) warp_potrf32(sC + jb * SC_LD + jb, srd, srd + T, lane, col0 + jb, status);
     __syncthreads();
     if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
     const int rem = T - jb - 32;
