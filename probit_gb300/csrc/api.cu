@@ -339,7 +339,7 @@ size_t layout(Engine& e, uintptr_t base) {
     q.Linv = b.take<float>((size_t)nt * T * T);
     q.Rv = b.take<float>((size_t)T * ld);
     float** vecs[] = {&q.a,    &q.f,    &q.d1, &q.W,    &q.sw, &q.r,  &q.t, &q.x, &q.logp, &q.d3,
-                      &q.dsig, &q.svec, &q.rv, &q.zbar, &q.tz, &q.y2, &q.u, &q.c, &q.rowdot, &q.sw_prev};
+                      &q.dsig, &q.svec, &q.rv, &q.zbar, &q.tz, &q.y2, &q.u, &q.c, &q.rowdot, &q.sw_prev, &q.da};
     for (float** v : vecs) *v = b.take<float>(npad);
     const size_t nvb = (size_t)ceil_div((int)npad, VT);
     q.part = b.take<double>(nvb + 8);
@@ -568,7 +568,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
       size_t mx = 0;
       for (int k = 0; k < 3; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
       void* tp = nullptr;
-      if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 16)) == PGB_OK) {
+      if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 32)) == PGB_OK) {
         e.trace = static_cast<unsigned long long*>(tp);
         for (DagJob& j : e.hjobs) {
           j.trace = e.trace;
@@ -621,8 +621,10 @@ void enq_dag(Engine& e, int slot, cudaStream_t s) {
 }
 
 void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
-  // f = K a
-  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);
+  // f += K da: f follows a by the updates (f = 0, da = a at the start), so
+  // the rounding of f shrinks with the step instead of staying at the float32
+  // error of a full K a, which would otherwise set a floor under ||da||
+  enq_matvec(e, MatvecOp{F_DA, F_NONE, F_F, 0, 1, 1}, s);
   // d1, W, sqrt W, r = d1 - a, t = r / sqrt W
   launch_newton_lik(e.probs, e.vmap, e.nvb, s);
   // bitwise-unchanged W keeps the resident factor

@@ -126,7 +126,8 @@ template <int MATERN, int DM, bool HAS_M>
 __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict__ theta,
                                         const float* __restrict__ Xr, int nr, const float* __restrict__ Xc, int nc,
                                         const float* __restrict__ M, long long ldm, const float* __restrict__ v,
-                                        const float* __restrict__ row_scale, float* __restrict__ y, int r0) {
+                                        const float* __restrict__ row_scale, float* __restrict__ y, int r0,
+                                        bool accumulate = false) {
   constexpr int MV_ROWS = mv_rows<DM>();
   __shared__ float sx[MV_ROWS][DM];
   __shared__ float sred[MV_THREADS / 32][MV_ROWS];
@@ -176,7 +177,7 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
 #pragma unroll
     for (int w = 0; w < MV_THREADS / 32; ++w) t += sred[w][threadIdx.x];
     if (row_scale) t *= row_scale[r0 + threadIdx.x];
-    y[r0 + threadIdx.x] = t;
+    y[r0 + threadIdx.x] = accumulate ? y[r0 + threadIdx.x] + t : t;
   }
 }
 
@@ -201,6 +202,7 @@ __device__ __forceinline__ float* prob_field(const Prob& P, int f) {
     case F_U: return P.u;
     case F_C: return P.c;
     case F_ROWDOT: return P.rowdot;
+    case F_DA: return P.da;
     default: return nullptr;
   }
 }
@@ -213,7 +215,7 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(const Prob* __r
   if (op.only_active && *P.active == 0) return;
   const int n = P.sh.n;
   mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
-                           prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>());
+                           prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>(), op.accumulate != 0);
 }
 
 template <int MATERN, int DM>

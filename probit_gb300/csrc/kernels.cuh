@@ -33,6 +33,7 @@ struct Prob {
   float* Binv;        // B^-1 (n_pad x ld), gradient only
   // vectors (n_pad each)
   float *a, *f, *d1, *W, *sw, *r, *t, *x, *logp, *d3, *dsig, *svec, *rv, *zbar, *tz, *y2, *u, *c, *rowdot, *sw_prev;
+  float* da;             // the last Newton update of a (f follows a by f += K da)
   float* err;         // last ||a_k - a_{k-1}||_2
   float* value;       // negative log evidence
   float* grad;        // theta-sized gradient
@@ -80,7 +81,7 @@ struct DagJob {
   // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
   // C assembled (after the accumulator is applied)
   unsigned long long* trace;
-  unsigned long long* ptrace;   // optional: [nt][16] phase times of the diagonal factorisations
+  unsigned long long* ptrace;   // optional: [2 nt][16] phase times of the diagonal factorisations, then of the sub-diagonal substitutions
   // tensor maps (128 x 32 fp32 boxes, 128-byte swizzle) of L, of R and of
   // Linv (nt*T rows of T), for the tensor-core operand loads
   const void* tm_L;
@@ -105,7 +106,7 @@ void launch_gram_full(const Shape& sh, const float* theta, const float* X1f, int
 // Vector operands of the batched Gram matvec, named by Prob field.
 enum VecField {
   F_A, F_F, F_D1, F_W, F_SW, F_R, F_T, F_X, F_LOGP, F_D3, F_DSIG, F_SVEC, F_RV, F_ZBAR, F_TZ, F_Y2, F_U, F_C,
-  F_ROWDOT, F_NONE
+  F_ROWDOT, F_DA, F_NONE
 };
 struct MatvecOp {
   int v;            // VecField of the vector
@@ -113,8 +114,9 @@ struct MatvecOp {
   int y;            // VecField of the output
   int use_binv;     // multiply K by B^-1 elementwise
   int only_active;  // skip problems whose Newton loop has stopped
+  int accumulate;   // y += result instead of y = result
 };
-// y = row_scale * ((K [o B^-1]) v) for every problem of one (kind, DM)
+// y (+)= row_scale * ((K [o B^-1]) v) for every problem of one (kind, DM)
 // group; mvmap: block -> (problem, row block of 128 / DM rows).
 void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
                         cudaStream_t st);

@@ -45,8 +45,9 @@ void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const 
 
 // ---------------------------------------------------------------- reset
 // Per problem: status words (no error, no iterations, no bad column), reuse
-// flags cleared (new theta: no resident factor), active = 1; a = 0 over the
-// padded length when zero_a.
+// flags cleared (new theta: no resident factor), active = 1; when zero_a,
+// a = 0 over the padded length and with it f = K a = 0 and the last update
+// da = 0 (the Newton loop keeps f by f += K da).
 __global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap, int zero_a) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
@@ -55,7 +56,11 @@ __global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2
     return;
   }
   const int i = m.y * VT + threadIdx.x;
-  if (zero_a && i < P.n_pad) P.a[i] = 0.0f;
+  if (zero_a && i < P.n_pad) {   // a = 0, f = K a = 0, no update yet
+    P.a[i] = 0.0f;
+    P.f[i] = 0.0f;
+    P.da[i] = 0.0f;
+  }
   if (m.y == 0) {
     if (threadIdx.x < 8) P.status[threadIdx.x] = threadIdx.x == ST_NOTPD_COL ? INT_MAX : 0;
     if (threadIdx.x < 4) P.reuse[threadIdx.x] = 0;
@@ -135,6 +140,9 @@ __global__ void newton_update_kernel(const Prob* __restrict__ probs, const int2*
     const float dlt = an - ai;
     e = dlt * dlt;
     P.a[i] = an;
+    P.da[i] = dlt;
+  } else if (i < P.n_pad) {
+    P.da[i] = 0.0f;
   }
   const double s = block_sum_d<VT>(e, sred);
   if (threadIdx.x == 0) P.part[m.y] = s;
