@@ -279,7 +279,11 @@ def run_batched(args, dev):
         "e2e": {"value": B / e2e_s, "unit": UNIT, "h2d_bytes_per_step": int(Xp.nbytes + yp.nbytes + 4 * theta.numel()),
                 "d2h_bytes_per_step": int(4 * (B + theta.numel()))},
         "newton_iterations": {"mean": float(iters.mean()), "max": int(iters.max()),
-                              "at_maxiter": int((iters >= 100).sum())},
+                              "at_maxiter": int((iters >= 100).sum()),
+                              "at_maxiter_problems": [
+                                  {"index": int(k), "N": int(probs[k].X.shape[0]), "D": int(probs[k].X.shape[1]),
+                                   "J": int(probs[k].J), "kernel": probs[k].kernel}
+                                  for k in np.nonzero(iters >= 100)[0][:8]]},
         "algorithmic_tflop": float((Ns ** 3 / 3).sum() * (iters.mean() + 3) / 1e12),
         "gpu_launches_per_batch": launches_per_solve(int(iters.max()), *kernel_groups(probs)),
         "data_generation_s": gen_s,

@@ -212,18 +212,19 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
 
 // Lookahead stage of tile task (i, j) of a problem with nt tile rows
 // (i >= nt: right-hand-side rows):
-//   diagonal (j, j) -> 2j,  sub-diagonal (j+1, j) -> 2j+1,
+//   diagonal (j, j) -> 2j,  the two tiles below it (j+1, j), (j+2, j) -> 2j+1,
 //   other tiles of column j and right-hand-side tiles -> 2j+3,
-// so the diagonal and sub-diagonal of column j+1 (the critical path) are
-// handed out before the rest of column j, whose tiles need the inverse of
-// the diagonal tile L_jj; by the time they are taken that inverse is
-// usually published, and their blocks do not sit waiting for it.  Sorting
-// by (stage, j, i) keeps every task after all tasks it waits for: a task
-// (i, j) waits for (i, k), (j, k) with k < j (stages <= 2j+1, and at stage
-// 2j+1 only column j-1 < j) and for (j, j) (stage 2j).
+// so the diagonal of column j+1 and the tiles below it (the critical path:
+// they solve with the panels of L_jj as they are published) are handed out
+// before the rest of column j, whose tiles need the inverse of the diagonal
+// tile L_jj; by the time they are taken that inverse is usually published,
+// and their blocks do not sit waiting for it.  Sorting by (stage, j, i)
+// keeps every task after all tasks it waits for: a task (i, j) waits for
+// (i, k), (j, k) with k < j (stages <= 2j+1, and at stage 2j+1 only column
+// j-1 < j) and for (j, j) (stage 2j).
 int dag_stage(int i, int j, int nt) {
   if (i < nt && i == j) return 2 * j;
-  if (i < nt && i == j + 1) return 2 * j + 1;
+  if (i < nt && i <= j + 2) return 2 * j + 1;
   return 2 * j + 3;
 }
 
@@ -378,7 +379,7 @@ size_t layout(Engine& e, uintptr_t base) {
       j.tm_L = map_slot(e, p, MAP_L);
       j.tm_Linv = map_slot(e, p, MAP_LINV);
     }
-    ready_off += 2 * (size_t)nt * nt + nt;
+    ready_off += 2 * (size_t)nt * nt + 2 * nt;
     DagJob* jb = &e.hjobs[(size_t)p * JOB_COUNT];
     jb[JOB_VEC].rhs_kind = RHS_VEC;
     jb[JOB_VEC].nrt = 1;
@@ -451,7 +452,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     e.x_total += (size_t)descs[p].n * descs[p].d;
     e.y_total += (size_t)descs[p].n;
     e.th_total += (size_t)e.th[p];
-    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p] + e.nt[p];
+    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p] + 2 * e.nt[p];
     e.tflags_words += 2 * (size_t)e.nt[p];
     e.dag_dm = std::max(e.dag_dm, dm_of(e.sh[p].Dp));
     e.nt_max = std::max(e.nt_max, e.nt[p]);

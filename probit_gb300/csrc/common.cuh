@@ -57,21 +57,29 @@ __device__ __forceinline__ uint64_t global_ns() {
 // so every other waiter of this launch returns promptly.  Returns true when
 // the flag was seen.
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;   // 4 s
-__device__ __forceinline__ bool wait_flag_geq(const int* flag, int target, int* status) {
-  if (ld_acquire(flag) >= target) return true;
+// wait_flag_value: the same wait for a target >= 1, returning the value
+// seen (>= target), or 0 when it gave up.
+__device__ __forceinline__ int wait_flag_value(const int* flag, int target, int* status) {
+  int v = ld_acquire(flag);
+  if (v >= target) return v;
   const uint64_t t0 = global_ns();
   unsigned ns = 32;
   while (true) {
-    if (ld_acquire(flag) >= target) return true;
-    if (ld_relaxed(status + ST_ABORT)) return false;
+    v = ld_acquire(flag);
+    if (v >= target) return v;
+    if (ld_relaxed(status + ST_ABORT)) return 0;
     if (global_ns() - t0 > WAIT_LIMIT_NS) {
       atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
       atomicExch(status + ST_ABORT, 1);
-      return false;
+      return 0;
     }
     __nanosleep(ns);
     if (ns < 256) ns <<= 1;
   }
+}
+
+__device__ __forceinline__ bool wait_flag_geq(const int* flag, int target, int* status) {
+  return target <= 0 || wait_flag_value(flag, target, status) >= target;
 }
 
 __device__ __forceinline__ void raise_status(int* status, int code) {

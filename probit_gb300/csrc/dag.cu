@@ -240,19 +240,6 @@ __device__ __forceinline__ void subst32_row(float* xs, const float* Lb, const fl
   for (int m = 0; m < 32; ++m) xs[m] = x[m];
 }
 
-// Column `lane` of the inverse of a 32 x 32 lower-triangular block:
-// y[r] = (delta_{r,lane} - sum_{m<r} L[r][m] y[m]) / L[r][r].
-template <int R>
-__device__ __forceinline__ void inv32_row(float (&y)[32], const float* Lb, int lane) {
-  if constexpr (R < 32) {
-    float acc = (R == lane) ? 1.0f : 0.0f;
-#pragma unroll
-    for (int m = 0; m < R; ++m) acc = fmaf(-Lb[R * SC_LD + m], y[m], acc);
-    y[R] = acc * __frcp_rn(Lb[R * SC_LD + R]);
-    inv32_row<R + 1>(y, Lb, lane);
-  }
-}
-
 // In-place Cholesky of the lower triangle of the 128 x 128 tile in sC:
 // 32-wide panels; warp 0 factors the diagonal block, one thread per row
 // solves the panel below (L rows broadcast from shared memory, reciprocal
@@ -260,18 +247,16 @@ __device__ __forceinline__ void inv32_row(float (&y)[32], const float* Lb, int l
 // Panel p of the factor (columns 32p .. 32p+31) is final once its diagonal
 // block and the rows below are solved; it is then written to dst (row stride
 // ld; zeros above the diagonal) and `progress` is released to p + 1, so the
-// sub-diagonal tile can start its substitution with it while the later
-// panels are factored.
+// tiles below can start their substitution with it while the later panels
+// are factored.  The block's writes precede thread 0's release store through
+// the barrier, and the release orders them for whoever acquires the count.
 __device__ __forceinline__ void publish_panel(const float* sC, float* dst, long long ld, int* progress, int jb) {
   for (int e = threadIdx.x; e < T * 32; e += DAG_THREADS) {
     const int r = e >> 5, c = jb + (e & 31);
     dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    st_release(progress, jb / 32 + 1);
-  }
+  if (threadIdx.x == 0) st_release(progress, jb / 32 + 1);
 }
 
 __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, float* dst, long long ld, int* progress,
@@ -322,60 +307,26 @@ __device__ void potrf_tile(float* sC, float* srd, int col0, int* status, float* 
   }
 }
 
-// sL (lower) = inverse of the lower-triangular 128 x 128 L in sC.
-// Diagonal 32 x 32 blocks: warp b solves L_bb y = e_l for column l in lane l.  Off-diagonal blocks by distance:
-//   Linv_rc = -Linv_rr * sum_{c <= m < r} L_rm Linv_mc,
-// the partial sum P_rc kept in the (unused) upper block (c, r) of sL.
-__device__ void trinv_tile(const float* sC, float* sL) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  if (warp < 4) {
-    const int b0 = warp * 32;
-    float y[32];
-    inv32_row<0>(y, sC + b0 * SC_LD + b0, lane);
-#pragma unroll
-    for (int r = 0; r < 32; ++r) sL[(b0 + r) * SC_LD + b0 + lane] = y[r];
-  }
-  __syncthreads();
-  for (int dl = 1; dl < 4; ++dl) {
-    const int nblk = 4 - dl;
-    // P_rc = sum_{m=c}^{r-1} L_rm Linv_mc  (block indices), stored at block (c, r)
-    for (int e = tid; e < nblk * 1024; e += DAG_THREADS) {
-      const int bi = e >> 10, rr = (e >> 5) & 31, cc = e & 31;
-      const int bc = bi, br = bi + dl;
-      float acc = 0.0f;
-      for (int m = bc * 32; m < br * 32; ++m)
-        acc = fmaf(sC[(br * 32 + rr) * SC_LD + m], sL[m * SC_LD + bc * 32 + cc], acc);
-      sL[(bc * 32 + cc) * SC_LD + br * 32 + rr] = acc;   // transposed into the upper block
-    }
-    __syncthreads();
-    // Linv_rc = -Linv_rr P_rc
-    for (int e = tid; e < nblk * 1024; e += DAG_THREADS) {
-      const int bi = e >> 10, rr = (e >> 5) & 31, cc = e & 31;
-      const int bc = bi, br = bi + dl;
-      float acc = 0.0f;
-      for (int m = 0; m <= rr; ++m)
-        acc = fmaf(sL[(br * 32 + rr) * SC_LD + br * 32 + m], sL[(bc * 32 + cc) * SC_LD + br * 32 + m], acc);
-      sL[(br * 32 + rr) * SC_LD + bc * 32 + cc] = -acc;
-    }
-    __syncthreads();
-  }
-}
-
-// X L^T = C in place for the 128 rows of sC, by 32-column blocks: block cb
-// needs panel cb of L (rows cb.., columns cb .. cb+31) in sL; one thread per
-// row solves the block of its row, then 4 x 4 register blocks update the
-// remaining columns.  Used on the critical path (the sub-diagonal tile),
-// panel by panel as the diagonal tile publishes them.
-__device__ void trsm_subst_block(float* sC, const float* sL, float* srd, int cb) {
+// X L^T = C in place for the first `rows` rows of sC (a multiple of 4), by
+// 32-column blocks: block cb needs panel cb of L (rows cb.., columns
+// cb .. cb+31) in sL; one thread per row solves the block of its row, then
+// 4 x 4 register blocks update the remaining columns.  Used on the critical
+// path (the tiles just below the diagonal), panel by panel as the diagonal
+// tile publishes them, and for the inverse of the diagonal tile.
+__device__ void trsm_subst_panel(float* sC, const float* sL, float* srd, int cb, int rows) {
   const int tid = threadIdx.x;
   if (tid < 32) srd[cb + tid] = __frcp_rn(sL[(cb + tid) * SC_LD + cb + tid]);
   __syncthreads();
-  if (tid < T) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
+  if (tid < rows) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
   __syncthreads();
+}
+
+__device__ void trsm_trail_panel(float* sC, const float* sL, int cb, int rows) {
+  const int tid = threadIdx.x;
   const int rem = T - cb - 32;
   if (rem > 0) {
     const int nbc = rem / 4;   // 4-column groups
-    for (int blk = tid; blk < (T / 4) * nbc; blk += DAG_THREADS) {
+    for (int blk = tid; blk < (rows / 4) * nbc; blk += DAG_THREADS) {
       const int r0 = (blk / nbc) * 4, c0 = cb + 32 + (blk % nbc) * 4;
       float acc[4][4];
 #pragma unroll
@@ -404,17 +355,24 @@ __device__ void trsm_subst_block(float* sC, const float* sL, float* srd, int cb)
   }
 }
 
-// Thread 0 waits, everyone learns the outcome.
+__device__ void trsm_subst_block(float* sC, const float* sL, float* srd, int cb, int rows) {
+  trsm_subst_panel(sC, sL, srd, cb, rows);
+  trsm_trail_panel(sC, sL, cb, rows);
+}
+
+// Thread 0 waits (an acquire load; the barrier then orders the rest of the
+// block after it), everyone learns the value seen (>= target), or 0 when
+// the wait gave up.
+__device__ __forceinline__ int block_wait_value(const int* flag, int* status, int* s_ok, int target) {
+  if (threadIdx.x == 0) *s_ok = wait_flag_value(flag, target, status);
+  __syncthreads();
+  const int v = *s_ok;
+  __syncthreads();
+  return v;
+}
+
 __device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_ok, int target = 1) {
-  if (threadIdx.x == 0) {
-    const bool ok = wait_flag_geq(flag, target, status);
-    __threadfence();
-    *s_ok = ok ? 1 : 0;
-  }
-  __syncthreads();
-  const bool ok = *s_ok != 0;
-  __syncthreads();
-  return ok;
+  return block_wait_value(flag, status, s_ok, target) >= target;
 }
 
 // Per-block tensor-core state, uniform across the block.
@@ -440,6 +398,7 @@ struct TcLoad {
   uint32_t base;       // tc.g when the accumulation started
   int issued;          // chunks whose loads were issued (thread 0)
   int ok;              // every dependency wait succeeded (thread 0)
+  int kfine;           // k-tile whose dependencies are waited for chunk by chunk (-1: none)
 };
 
 __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, const void* bmap, int brow, int bcol,
@@ -456,12 +415,14 @@ __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, 
   l.base = tc.g;
   l.issued = 0;
   l.ok = 1;
+  l.kfine = -1;
   return l;
 }
 
 // Thread 0: issue the loads of chunk `c` into its stage, after the MMAs of
-// the stage's previous chunk completed and, at a k-tile boundary, after the
-// k-tile's dependencies were published (wait_tile).  A dependency wait that
+// the stage's previous chunk completed and, at a k-tile boundary (every chunk
+// of the k-tile l.kfine), after the dependencies were published
+// (wait_tile(k-tile, chunk within it)).  A dependency wait that
 // gives up still issues the loads (the addresses are valid; the result is
 // discarded), so the stage accounting stays consistent.  False if a
 // pipeline wait timed out.
@@ -470,8 +431,9 @@ __device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, Wait
   const uint32_t g = l.base + (uint32_t)c;
   const uint32_t s = g % NST;
   if (g >= NST && !mbar_wait_bounded(tc.empty + s, ((g / NST) - 1u) & 1u, MMA_WAIT_NS)) return false;
-  if ((c % (T / 32)) == 0) {
-    if (!wait_tile(l.k0 + c / (T / 32))) l.ok = 0;
+  const int kt = l.k0 + c / (T / 32), q = c % (T / 32);
+  if (q == 0 || kt == l.kfine) {
+    if (!wait_tile(kt, q)) l.ok = 0;
     fence_proxy_async_global();
   }
   const int col = (l.k0 + c / (T / 32)) * T + (c % (T / 32)) * 32;
@@ -637,13 +599,19 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const bool have_acc = j > k0;
   const int* ready = jb.ready;
   int* status = jb.status;
-  auto wait_tile = [=](int k) {
+  // the diagonal tile takes its last k-tile, the tile just below the
+  // previous diagonal, 32 columns at a time as that tile publishes them
+  const int kfine = (!is_rhs && i == j && j > 0) ? j - 1 : -1;
+  const int* xprog = jb.progress + nt;
+  auto wait_tile = [=](int k, int q) {
+    if (k == kfine) return wait_flag_geq(xprog + k, q + 1, status);
     return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
            wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
   };
   const void* rows_map = is_rhs ? jb.tm_R : jb.tm_L;
   const int row0 = (is_rhs ? ri : i) * T;
   TcLoad acc_load = tc_load(rows_map, row0, 0, jb.tm_L, j * T, 0, k0, j, tc);
+  acc_load.kfine = kfine;
   if (have_acc && threadIdx.x == 0) {
     fence_tensormap_acquire(rows_map);
     fence_tensormap_acquire(jb.tm_L);
@@ -678,26 +646,60 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       __threadfence();
       st_release(jb.ready + (size_t)i * nt + j, 1);
     }
-    trinv_tile(sC, sL);
+    // L^-1 = X^T with X L^T = I: X = L^-T is upper triangular, so in column
+    // block cb only its rows < cb + 32 are nonzero and solved
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      Linv_j[(size_t)r * T + c] = c <= r ? sL[r * SC_LD + c] : 0.0f;
+      const float l = sC[r * SC_LD + c];
+      sL[r * SC_LD + c] = c <= r ? l : 0.0f;
+      sC[r * SC_LD + c] = r == c ? 1.0f : 0.0f;
     }
-  } else if (!is_rhs && i == j + 1) {
-    // critical path: substitution with each panel of L_jj as soon as it is published
+    __syncthreads();
+    for (int cb = 0; cb < T; cb += 32) trsm_subst_block(sC, sL, sX, cb, cb + 32);
+    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+      const int r = e >> 7, c = e & (T - 1);
+      Linv_j[(size_t)r * T + c] = c <= r ? sC[c * SC_LD + r] : 0.0f;
+    }
+  } else if (!is_rhs && i <= j + 2) {
+    // the two tiles below the diagonal feed the next column's critical
+    // path: substitution with each panel of L_jj as soon as it is
+    // published, instead of waiting for L_jj^-1.  The tile just below
+    // publishes its own panels as they are solved (progress[nt + j]), for
+    // the next diagonal tile's last k-step.
     const float* Ljj = jb.L + (size_t)j * T * ld + (size_t)j * T;
+    const bool sub = i == j + 1;
+    unsigned long long* sp = (jb.ptrace && threadIdx.x == 0 && sub) ? jb.ptrace + (size_t)(nt + j) * 16 : nullptr;
+    int have = 0;   // panels of L_jj known to be published
     for (int cb = 0; cb < T; cb += 32) {
-      if (!block_wait(jb.progress + j, jb.status, s_ok + 2, cb / 32 + 1)) return;
+      if (have < cb / 32 + 1) {
+        have = block_wait_value(jb.progress + j, jb.status, s_ok + 2, cb / 32 + 1);
+        if (have == 0) return;
+      }
+      if (sp) sp[cb / 8] = global_ns();
       for (int e = threadIdx.x; e < (T - cb) * 32; e += DAG_THREADS) {
         const int r = cb + (e >> 5), c = cb + (e & 31);
         sL[r * SC_LD + c] = __ldcg(Ljj + (size_t)r * ld + c);
       }
       __syncthreads();
-      trsm_subst_block(sC, sL, sX, cb);
+      if (sp) sp[cb / 8 + 1] = global_ns();
+      trsm_subst_panel(sC, sL, sX, cb, T);
+      if (sub) {
+        for (int e = threadIdx.x; e < T * 32; e += DAG_THREADS) {
+          const int r = e >> 5, c = cb + (e & 31);
+          dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) st_release(jb.progress + nt + j, cb / 32 + 1);
+      }
+      if (sp) sp[cb / 8 + 2] = global_ns();
+      trsm_trail_panel(sC, sL, cb, T);
+      if (sp) sp[cb / 8 + 3] = global_ns();
     }
-    for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
-      const int r = e >> 7, c = e & (T - 1);
-      dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+    if (!sub) {
+      for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
+        const int r = e >> 7, c = e & (T - 1);
+        dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+      }
     }
   } else {
     // X = C L_jj^-T = C Linv_jj^T on the tensor cores (C staged through dst)
@@ -708,7 +710,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     fence_proxy_async_global();   // dst is read back by the tensor loads
     fence_proxy_async_smem();     // sC is overwritten by them
     if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 2)) return;
-    auto always = [](int) { return true; };
+    auto always = [](int, int) { return true; };
     TcLoad trsm_load = tc_load(rows_map, row0, j * T, jb.tm_Linv, j * T, 0, 0, 1, tc);
     if (threadIdx.x == 0) {
       fence_tensormap_acquire(jb.tm_Linv);
@@ -820,7 +822,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const voi
   __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
-  auto always = [](int) { return true; };
+  auto always = [](int, int) { return true; };
   TcLoad l = tc_load(amap, 0, 0, bmap, 0, 0, 0, K / T, tc);
   if (threadIdx.x == 0) {
     fence_tensormap_acquire(amap);
@@ -894,7 +896,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
     const int I = tl.y, J = tl.z;
     const long long ld = P.ld;
     float* Binv = P.Binv;
-    auto always = [](int) { return true; };
+    auto always = [](int, int) { return true; };
     TcLoad l = tc_load(P.tm_Rz, I * T, 0, P.tm_Rz, J * T, 0, I, P.nt, tc);
     if (threadIdx.x == 0) {
       fence_tensormap_acquire(P.tm_Rz);
@@ -926,7 +928,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) sub_rrt_kernel(const void* rma
   float* sC = reinterpret_cast<float*>(tc.stages);
   const int mt = ceil_div(m, T);
   const int ntiles = mt * (mt + 1) / 2;
-  auto always = [](int) { return true; };
+  auto always = [](int, int) { return true; };
   while (true) {
     fence_proxy_async_smem();
     __syncthreads();

@@ -68,7 +68,8 @@ struct DagJob {
   const float* theta;
   Shape sh;
   int* ready;            // (nt + nrt) x nt tile flags, zeroed before the launch
-  int* progress;         // nt: panels of each diagonal tile published (0..4), zeroed with ready
+  int* progress;         // 2 nt: panels published (0..4) of each diagonal tile, then of the tile
+                         // just below it; zeroed with ready
   int* status;
   // factor reuse: when *reuse is 1 the resident L is already the factor of
   // this B (bitwise equal W, same theta).  reuse_mode 1: skip the L tiles and

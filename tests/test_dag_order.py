@@ -62,9 +62,12 @@ def test_dag_order_topological(native_lib, nts, kind):
 
 
 def test_dag_order_lookahead(native_lib):
-    """The next column's diagonal is handed out before the rest of a column."""
+    """The next column's diagonal is handed out before the rest of a column,
+    the two tiles below a diagonal before the next diagonal."""
     tasks = _order(native_lib, [6], 1)
     seq = [(int(i), int(j)) for _, i, j, _ in tasks]
-    assert seq.index((1, 1)) < seq.index((2, 0))
-    assert seq.index((2, 2)) < seq.index((3, 1))
-    assert seq.index((3, 3)) < seq.index((4, 2))
+    assert seq.index((1, 1)) < seq.index((3, 0))
+    assert seq.index((2, 2)) < seq.index((4, 1))
+    assert seq.index((3, 3)) < seq.index((5, 2))
+    assert seq.index((2, 0)) < seq.index((1, 1))
+    assert seq.index((3, 1)) < seq.index((2, 2))
