@@ -212,7 +212,7 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
 
 // Lookahead stage of tile task (i, j) of a problem with nt tile rows
 // (i >= nt: right-hand-side rows):
-//   diagonal (j, j) -> 2j,  the two tiles below it (j+1, j), (j+2, j) -> 2j+1,
+//   diagonal (j, j) -> 2j,  the near_depth(nt) tiles below it -> 2j+1,
 //   other tiles of column j and right-hand-side tiles -> 2j+3,
 // so the diagonal of column j+1 and the tiles below it (the critical path:
 // they solve with the panels of L_jj as they are published) are handed out
@@ -224,7 +224,7 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
 // j-1 < j) and for (j, j) (stage 2j).
 int dag_stage(int i, int j, int nt) {
   if (i < nt && i == j) return 2 * j;
-  if (i < nt && i <= j + 2) return 2 * j + 1;
+  if (i < nt && i <= j + near_depth(nt)) return 2 * j + 1;
   return 2 * j + 3;
 }
 
@@ -569,7 +569,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
       size_t mx = 0;
       for (int k = 0; k < 3; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
       void* tp = nullptr;
-      if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 32)) == PGB_OK) {
+      if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 48)) == PGB_OK) {
         e.trace = static_cast<unsigned long long*>(tp);
         for (DagJob& j : e.hjobs) {
           j.trace = e.trace;

@@ -27,9 +27,16 @@ enum StatusSlot {
   ST_ABORT = 3,       // set by any kernel that gave up waiting
   ST_CONVERGED = 4,   // 1 once the fixed point test passed
   ST_SPARE0 = 5,
-  ST_SPARE1 = 6,
-  ST_SPARE2 = 7,
+  ST_STALL = 6,       // consecutive Newton steps that did not halve ||delta||
+  ST_PREV_ERR = 7,    // float bits of the previous step's ||delta||
 };
+// A Newton loop that has stopped contracting (kStallSteps steps in a row
+// without halving ||delta||, at ||delta|| <= max(kStallTol * tol,
+// kStallAbs)) is at the float32 floor of its fixed point; its remaining
+// steps reuse the resident factor.
+constexpr int kStallSteps = 2;
+constexpr float kStallTol = 16.0f;
+constexpr float kStallAbs = 1e-2f;
 
 // ---------------------------------------------------------------- memory order
 __device__ __forceinline__ int ld_acquire(const int* p) {
@@ -135,6 +142,13 @@ __device__ __forceinline__ double block_sum_d(float v, double* smem_red) {
 }
 
 __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
+
+// Tiles (i, j) with j < i <= j + near_depth(nt) of an nt-tile factor are
+// solved by substitution with the panels of L_jj as they are published (the
+// next columns' critical path); the tiles further down wait for L_jj^-1 and
+// use the tensor cores.  A deeper band keeps the inverse off the critical
+// path of long factorisations; short ones save the substitution work.
+__host__ __device__ inline int near_depth(int nt) { return nt >= 16 ? 3 : 2; }
 
 }  // namespace pgb
 

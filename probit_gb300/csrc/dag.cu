@@ -399,6 +399,7 @@ struct TcLoad {
   int issued;          // chunks whose loads were issued (thread 0)
   int ok;              // every dependency wait succeeded (thread 0)
   int kfine;           // k-tile whose dependencies are waited for chunk by chunk (-1: none)
+  unsigned long long* kt;   // optional timestamps (thread 0): last k-tile's dependency seen, its 4 chunks landed, drained
 };
 
 __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, const void* bmap, int brow, int bcol,
@@ -416,6 +417,7 @@ __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, 
   l.issued = 0;
   l.ok = 1;
   l.kfine = -1;
+  l.kt = nullptr;
   return l;
 }
 
@@ -435,6 +437,7 @@ __device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, Wait
   if (q == 0 || kt == l.kfine) {
     if (!wait_tile(kt, q)) l.ok = 0;
     fence_proxy_async_global();
+    if (l.kt && c == l.nchunks - (T / 32)) l.kt[0] = global_ns();
   }
   const int col = (l.k0 + c / (T / 32)) * T + (c % (T / 32)) * 32;
   uint8_t* stage = tc.stages + s * STAGE_BYTES;
@@ -534,6 +537,7 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
     const uint32_t g = l.base + (uint32_t)c;
     const uint32_t s = g % NST;
     if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
+    if (l.kt && threadIdx.x == 0 && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
     uint8_t* stage = tc.stages + s * STAGE_BYTES;
     convert_stage(stage);
     fence_proxy_async_smem();
@@ -553,6 +557,7 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
     atomicExch(status + ST_ABORT, 1);
   }
   const bool drained = tc_drain(tc, status);
+  if (l.kt && threadIdx.x == 0) l.kt[5] = global_ns();
   return drained && !any_bad;
 }
 
@@ -612,6 +617,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const int row0 = (is_rhs ? ri : i) * T;
   TcLoad acc_load = tc_load(rows_map, row0, 0, jb.tm_L, j * T, 0, k0, j, tc);
   acc_load.kfine = kfine;
+  if (jb.ptrace && threadIdx.x == 0 && !is_rhs && i <= j + 1) acc_load.kt = jb.ptrace + (size_t)32 * nt + (size_t)(2 * j + (i - j)) * 8;
   if (have_acc && threadIdx.x == 0) {
     fence_tensormap_acquire(rows_map);
     fence_tensormap_acquire(jb.tm_L);
@@ -660,8 +666,8 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       const int r = e >> 7, c = e & (T - 1);
       Linv_j[(size_t)r * T + c] = c <= r ? sC[c * SC_LD + r] : 0.0f;
     }
-  } else if (!is_rhs && i <= j + 2) {
-    // the two tiles below the diagonal feed the next column's critical
+  } else if (!is_rhs && i <= j + near_depth(nt)) {
+    // the tiles just below the diagonal feed the next columns' critical
     // path: substitution with each panel of L_jj as soon as it is
     // published, instead of waiting for L_jj^-1.  The tile just below
     // publishes its own panels as they are solved (progress[nt + j]), for

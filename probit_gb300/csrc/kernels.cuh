@@ -82,7 +82,8 @@ struct DagJob {
   // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
   // C assembled (after the accumulator is applied)
   unsigned long long* trace;
-  unsigned long long* ptrace;   // optional: [2 nt][16] phase times of the diagonal factorisations, then of the sub-diagonal substitutions
+  unsigned long long* ptrace;   // optional: [2 nt][16] phase times of the diagonal factorisations, then of the
+                                // sub-diagonal substitutions; then [nt][2][8] last k-step times of (j, j), (j+1, j)
   // tensor maps (128 x 32 fp32 boxes, 128-byte swizzle) of L, of R and of
   // Linv (nt*T rows of T), for the tensor-core operand loads
   const void* tm_L;

@@ -76,7 +76,12 @@ void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int
 // every enabled problem)
 __global__ void activate_enabled_kernel(const Prob* __restrict__ probs, int nprob) {
   const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p < nprob) *probs[p].active = *probs[p].enabled != 0 ? 1 : 0;
+  if (p < nprob && *probs[p].enabled != 0) {
+    *probs[p].active = 1;
+    probs[p].status[ST_STALL] = 0;   // the factor of the final W is compared bitwise again
+  } else if (p < nprob) {
+    *probs[p].active = 0;
+  }
 }
 
 void launch_activate_enabled(const Prob* probs, int nprob, cudaStream_t st) {
@@ -171,6 +176,10 @@ __global__ void newton_finalize_kernel(const Prob* __restrict__ probs, int nprob
     const int it = status[ST_ITERS] + 1;
     status[ST_ITERS] = it;
     *P.err = err;
+    const float prev = __int_as_float(status[ST_PREV_ERR]);
+    const bool flat = it > 1 && err > 0.5f * prev && err <= fmaxf(kStallTol * P.tol, kStallAbs);
+    status[ST_STALL] = flat ? status[ST_STALL] + 1 : 0;
+    status[ST_PREV_ERR] = __float_as_int(err);
     if (!(err > P.tol)) status[ST_CONVERGED] = 1;
     if (err != err) atomicCAS(status + ST_CODE, 0, PGB_ENAN);
     const bool again = (err > P.tol) && (it < P.maxiter) && (status[ST_ABORT] == 0);
@@ -461,11 +470,14 @@ void launch_sqrt_w(int n, int n_pad, const float* W, float* sw, cudaStream_t st)
 // ---------------------------------------------------------------- factor reuse
 // Per active problem: reuse[1] |= any(sw != sw_prev) (bitwise; NaN always
 // differs); sw_prev <- sw.  Then per problem: reuse[2] = valid && !differs,
-// differs <- 0.
+// differs <- 0.  A Newton loop at its float32 floor (ST_STALL) skips the
+// comparison and keeps the resident factor of sw_prev: its steps are then
+// Newton steps with a Jacobian a few rounding errors old.
 __global__ void reuse_check_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
   const int2 m = vmap[blockIdx.x];
   const Prob& P = probs[m.x];
   if (*P.active == 0) return;   // uniform per block
+  if (P.status[ST_STALL] >= kStallSteps) return;
   const int i = m.y * VT + threadIdx.x;
   bool diff = false;
   if (i < P.sh.n) {
