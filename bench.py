@@ -469,7 +469,7 @@ def run_serving(args, dev):
 
     out = {"workers": args.serve_workers, "pool": 256}
     for tag, rate, dur, seed in (("offered_2000_per_s", 2000.0, args.serve_seconds, 4),
-                                 ("offered_150_per_s", 150.0, max(2.0, args.serve_seconds), 5)):
+                                 ("offered_150_per_s", 150.0, max(5.0, args.serve_seconds), 5)):
         probs, reqs = Wk.serving_c4(rate=rate, duration=dur, pool=256, seed=seed, device=dev)
         srv = S.Server(workers=args.serve_workers)
         try:

@@ -51,7 +51,6 @@ constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 // The entry loop is one uniform formula over the zero-padded features, so
 // its code stays small whatever the kernel family.
 constexpr int SX_STRIDE = 17;   // DM + 1 (<= 16 + 1), breaks bank conflicts
-constexpr int SX_FLOATS = 2 * T * SX_STRIDE + 2 * T;
 
 template <int DM>
 __device__ void stage_features(const DagJob& jb, int i, int j, float* sX) {

@@ -14,40 +14,50 @@ namespace pgb {
 
 constexpr int TS_THREADS = 256;
 
-// acc[r] (+)= sign * sum_c A[r, c] v[c] for a 128 x 128 tile A (row stride
-// lda): thread t owns row t >> 1 and columns (t & 1) * 64 .. +63; its 16
-// float4 loads are issued before any use.
-__device__ __forceinline__ void tile_mv_rows(const float* __restrict__ A, long long lda, const float* sv,
-                                             float* sacc, bool assign) {
-  const int t = threadIdx.x;
-  const int r = t >> 1, h = t & 1;
-  const float* a = A + (size_t)r * lda + h * 64;
-  float4 v[16];
-#pragma unroll
-  for (int q = 0; q < 16; ++q) v[q] = __ldcg(reinterpret_cast<const float4*>(a) + q);
-  float s = 0.0f;
-#pragma unroll
-  for (int q = 0; q < 16; ++q) {
-    const float* x = sv + h * 64 + 4 * q;
-    s = fmaf(v[q].x, x[0], s);
-    s = fmaf(v[q].y, x[1], s);
-    s = fmaf(v[q].z, x[2], s);
-    s = fmaf(v[q].w, x[3], s);
-  }
-  s += __shfl_xor_sync(0xffffffffu, s, 1);
-  if (h == 0) sacc[r] = assign ? s : sacc[r] - s;
-}
-
-// acc[c] (+)= sign * sum_r A[r, c] v[r]: thread t owns columns 4 (t & 31) ..
-// +3 and rows (t >> 5) * 16 .. +15; partial sums combined in spart.
-__device__ __forceinline__ void tile_mv_cols(const float* __restrict__ A, long long lda, const float* sv,
-                                             float* sacc, float (*spart)[T], bool assign) {
+// A 128 x 128 tile A (row stride lda) in registers: thread t holds rows
+// 16 (t >> 5) .. +15, columns 4 (t & 31) .. +3, so every load instruction
+// of a warp reads one 512-byte row segment.  The loads are issued before the
+// block waits for the vector they multiply.
+__device__ __forceinline__ void tile_load(const float* __restrict__ A, long long lda, float4 (&v)[16]) {
   const int t = threadIdx.x;
   const int cq = t & 31, g = t >> 5;
-  float4 v[16];
 #pragma unroll
-  for (int q = 0; q < 16; ++q)
-    v[q] = __ldcg(reinterpret_cast<const float4*>(A + (size_t)(g * 16 + q) * lda + 4 * cq));
+  for (int q = 0; q < 16; ++q) v[q] = __ldcg(reinterpret_cast<const float4*>(A + (size_t)(g * 16 + q) * lda + 4 * cq));
+}
+
+// acc[r] (+)= sign * sum_c A[r, c] x[c], A in registers (tile_load layout):
+// each thread's 16 row partials are summed over the warp's 32 lanes by a
+// halving butterfly (16 shuffles), after which lanes 2m and 2m + 1 hold row m.
+__device__ __forceinline__ void tile_mv_rows(const float4 (&v)[16], const float* sv, float* sacc, bool assign) {
+  const int t = threadIdx.x;
+  const int lane = t & 31, g = t >> 5;
+  const float4 x = reinterpret_cast<const float4*>(sv)[lane];
+  float p[16];
+#pragma unroll
+  for (int q = 0; q < 16; ++q) p[q] = fmaf(v[q].x, x.x, fmaf(v[q].y, x.y, fmaf(v[q].z, x.z, v[q].w * x.w)));
+#pragma unroll
+  for (int w = 8; w >= 1; w >>= 1) {   // keep w values: the upper or lower half by lane bit
+    const bool up = (lane & (2 * w)) != 0;
+#pragma unroll
+    for (int q = 0; q < w; ++q) {
+      const float send = up ? p[q] : p[q + w];
+      const float keep = up ? p[q + w] : p[q];
+      p[q] = keep + __shfl_xor_sync(0xffffffffu, send, 2 * w);
+    }
+  }
+  const float s = p[0] + __shfl_xor_sync(0xffffffffu, p[0], 1);
+  if ((lane & 1) == 0) {
+    const int r = g * 16 + (lane >> 1);
+    sacc[r] = assign ? s : sacc[r] - s;
+  }
+}
+
+// acc[c] (+)= sign * sum_r A[r, c] x[r], A in registers (tile_load layout);
+// the 8 warps' partial column sums are combined in spart.
+__device__ __forceinline__ void tile_mv_cols(const float4 (&v)[16], const float* sv, float* sacc, float (*spart)[T],
+                                             bool assign) {
+  const int t = threadIdx.x;
+  const int cq = t & 31, g = t >> 5;
   float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll
   for (int q = 0; q < 16; ++q) {
@@ -82,7 +92,7 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(const Prob* __restr
                                                              int* __restrict__ counter, int run_on_reuse,
                                                              int only_active) {
   __shared__ float sacc[T];
-  __shared__ float sx[T];
+  __shared__ __align__(16) float sx[T];
   __shared__ float spart[8][T];
   __shared__ int s_q, s_ok;
   const int tid = threadIdx.x;
@@ -111,20 +121,24 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(const Prob* __restr
     int* flags = P.tflags + (trans ? 0 : nt);
     int* status = P.status;
     const int i = trans ? nt - 1 - cl.y : cl.y;
+    // the inverse of the diagonal tile, needed last, is loaded first
+    float4 dv[16];
+    tile_load(P.Linv + (size_t)i * T * T, T, dv);
     if (tid < T) {
       const int gi = i * T + tid;
       sacc[tid] = gi < n ? __ldcg(b + gi) : 0.0f;
     }
     // dependencies oldest first (the order they were solved in), so a block
-    // accumulates everything already available while the newest is pending
+    // accumulates everything already available while the newest is pending;
+    // each tile of L is loaded before its vector is waited for
     const int ndep = trans ? nt - 1 - i : i;
     bool ok = true;
     for (int kk = 0; kk < ndep; ++kk) {
       const int k = trans ? nt - 1 - kk : kk;
-      if (tid == 0) {
-        s_ok = wait_flag_geq(flags + k, 1, status) ? 1 : 0;
-        __threadfence();
-      }
+      float4 v[16];
+      tile_load(trans ? L + (size_t)(k * T) * ld + i * T : L + (size_t)(i * T) * ld + k * T, ld, v);
+      // thread 0's acquire load, then the barrier, order the block's reads of x_k
+      if (tid == 0) s_ok = wait_flag_geq(flags + k, 1, status) ? 1 : 0;
       __syncthreads();
       if (!s_ok) {
         ok = false;
@@ -133,27 +147,23 @@ __global__ void __launch_bounds__(TS_THREADS, 1) trsv_kernel(const Prob* __restr
       if (tid < T) sx[tid] = __ldcg(x + (size_t)k * T + tid);
       __syncthreads();
       if (!trans)
-        tile_mv_rows(L + (size_t)(i * T) * ld + k * T, ld, sx, sacc, false);   // sacc -= L_ik x_k
+        tile_mv_rows(v, sx, sacc, false);          // sacc -= L_ik x_k
       else
-        tile_mv_cols(L + (size_t)(k * T) * ld + i * T, ld, sx, sacc, spart, false);   // sacc -= L_ki^T x_k
+        tile_mv_cols(v, sx, sacc, spart, false);   // sacc -= L_ki^T x_k
       __syncthreads();
     }
     if (!ok) continue;
     // diagonal tile: x_i = Linv_ii acc (lower) or Linv_ii^T acc (trans)
-    const float* Li = P.Linv + (size_t)i * T * T;
     if (tid < T) sx[tid] = sacc[tid];
     __syncthreads();
     if (!trans)
-      tile_mv_rows(Li, T, sx, sacc, true);
+      tile_mv_rows(dv, sx, sacc, true);
     else
-      tile_mv_cols(Li, T, sx, sacc, spart, true);
+      tile_mv_cols(dv, sx, sacc, spart, true);
     __syncthreads();
     if (tid < T) x[(size_t)i * T + tid] = sacc[tid];
     __syncthreads();
-    if (tid == 0) {
-      __threadfence();
-      st_release(flags + i, 1);
-    }
+    if (tid == 0) st_release(flags + i, 1);   // orders the block's stores of x_i (barrier above)
   }
 }
 
