@@ -382,6 +382,7 @@ struct TcCtx {
   uint8_t* stages;     // 1024-aligned stage buffers (unioned with sC, sL)
   uint64_t* full;      // [NST] the stage's tensor loads landed
   uint64_t* empty;     // [NST] the MMAs that read the stage completed
+  uint64_t* split;     // [NST] the stage's chunk is split (one arrival per splitting warp)
   uint64_t* acc;       // every MMA issued so far completed
 };
 
@@ -458,21 +459,28 @@ __device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& w
 
 // Split the fp32 A and B chunks the loads left in a stage into TF32 hi (in
 // place) and lo parts; the 128-byte swizzle is the same for both, so the
-// split is element by element.
-__device__ __forceinline__ void convert_stage(uint8_t* stage) {
+// split is element by element.  Done by the SPLIT_THREADS threads of warps
+// 2..7 (thread index t - 64), 5 or 6 float4 of A and of B each.
+constexpr int SPLIT_WARPS = DAG_THREADS / 32 - 2;
+constexpr int SPLIT_THREADS = 32 * SPLIT_WARPS;
+__device__ __forceinline__ void convert_stage(uint8_t* stage, int t) {
   float4* ah = reinterpret_cast<float4*>(stage);
   float4* bh = reinterpret_cast<float4*>(stage + 2 * CHUNK_BYTES);
   constexpr int LO = CHUNK_BYTES / 16;
-  float4 a[4], b[4];
+  constexpr int NQ = (LO + SPLIT_THREADS - 1) / SPLIT_THREADS;
+  float4 a[NQ], b[NQ];
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int e = threadIdx.x + DAG_THREADS * q;
-    a[q] = ah[e];
-    b[q] = bh[e];
+  for (int q = 0; q < NQ; ++q) {
+    const int e = t + SPLIT_THREADS * q;
+    if (e < LO) {
+      a[q] = ah[e];
+      b[q] = bh[e];
+    }
   }
 #pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int e = threadIdx.x + DAG_THREADS * q;
+  for (int q = 0; q < NQ; ++q) {
+    const int e = t + SPLIT_THREADS * q;
+    if (e >= LO) break;
     float4 h, o;
     split_tf32(a[q].x, h.x, o.x);
     split_tf32(a[q].y, h.y, o.y);
@@ -522,30 +530,48 @@ __device__ bool tc_drain(TcCtx& tc, int* status) {
 // acc (TMEM) += sum_k A_k B_k^T in 3xTF32 (acc starts from zero unless
 // `preloaded`).  Thread 0 must have called tc_start on `l`, and every thread
 // must have fenced its earlier generic writes to the stage buffers
-// (fence_proxy_async_smem) before the barrier that preceded it.  Per chunk:
-// wait for its loads, split it (all threads), thread 0 issues its MMAs and
-// the loads of the chunk NST - 1 ahead.  Every wait is bounded and the loop
-// always runs to the end, so all threads take the same path; false when a
-// dependency wait gave up or a pipeline wait timed out (the problem is then
-// aborted and the accumulator is garbage).
+// (fence_proxy_async_smem) before the barrier that preceded it.  Three
+// roles: thread 32 issues the loads of each chunk as soon as the MMAs that
+// read its stage have completed (and its dependencies are published); warps
+// 2..7 split each chunk as soon as its loads land and signal the stage's
+// split barrier; thread 0 waits for that signal and issues the chunk's MMAs.
+// So loads, splits and MMAs of consecutive chunks overlap.  Every wait is bounded and every
+// loop runs to the end, so each warp takes the same number of steps; false
+// when a dependency wait gave up or a pipeline wait timed out (the problem
+// is then aborted and the accumulator is garbage).
 template <class WaitTile>
 __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, bool preloaded) {
   bool bad = false;
   const int n = l.nchunks;
-  for (int c = 0; c < n; ++c) {
-    const uint32_t g = l.base + (uint32_t)c;
-    const uint32_t s = g % NST;
-    if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
-    if (l.kt && threadIdx.x == 0 && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
-    uint8_t* stage = tc.stages + s * STAGE_BYTES;
-    convert_stage(stage);
-    fence_proxy_async_smem();
-    __syncthreads();
-    if (threadIdx.x == 0) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    // the MMAs of each chunk once its split is signalled
+    for (int c = 0; c < n; ++c) {
+      const uint32_t g = l.base + (uint32_t)c;
+      const uint32_t s = g % NST;
+      if (!mbar_wait_bounded(tc.split + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
+      if (l.kt && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
       tc_fence_after();
-      issue_chunk(tc, stage, c == 0 && !preloaded);
+      issue_chunk(tc, tc.stages + s * STAGE_BYTES, c == 0 && !preloaded);
       umma_commit(tc.empty + s);
-      if (c + NST - 1 < n && !tc_issue(tc, l, c + NST - 1, wait_tile)) bad = true;
+    }
+  } else if (threadIdx.x == 32) {
+    // the loads of the chunks after the first NST - 1 (issued by tc_start),
+    // each as soon as the MMAs that read its stage have completed
+    l.issued = min(NST - 1, n);
+    for (int c = l.issued; c < n; ++c)
+      if (!tc_issue(tc, l, c, wait_tile)) bad = true;
+    if (!l.ok) bad = true;
+  } else if (warp >= 2) {
+    // warps 2..7: split each chunk as soon as its loads land, ahead of the MMAs
+    for (int c = 0; c < n; ++c) {
+      const uint32_t g = l.base + (uint32_t)c;
+      const uint32_t s = g % NST;
+      if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
+      convert_stage(tc.stages + s * STAGE_BYTES, threadIdx.x - 64);
+      fence_proxy_async_smem();   // the split is read by the tensor cores
+      __syncwarp();
+      if (lane == 0) mbar_arrive(tc.split + s);
     }
   }
   tc.g = l.base + (uint32_t)n;
@@ -616,7 +642,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const int row0 = (is_rhs ? ri : i) * T;
   TcLoad acc_load = tc_load(rows_map, row0, 0, jb.tm_L, j * T, 0, k0, j, tc);
   acc_load.kfine = kfine;
-  if (jb.ptrace && threadIdx.x == 0 && !is_rhs && i <= j + 1) acc_load.kt = jb.ptrace + (size_t)32 * nt + (size_t)(2 * j + (i - j)) * 8;
+  if (jb.ptrace && (threadIdx.x == 0 || threadIdx.x == 32) && !is_rhs && i <= j + 1) acc_load.kt = jb.ptrace + (size_t)32 * nt + (size_t)(2 * j + (i - j)) * 8;
   if (have_acc && threadIdx.x == 0) {
     fence_tensormap_acquire(rows_map);
     fence_tensormap_acquire(jb.tm_L);
@@ -753,7 +779,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
 }
 
 // Block set-up of the tensor-core kernels: 1024-aligned stage buffers in the
-// dynamic shared memory, 2 NST + 1 mbarriers, 128 TMEM columns.
+// dynamic shared memory, 3 NST + 1 mbarriers, 128 TMEM columns.
 __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32_t* s_tmem) {
   TcCtx tc;
   const uint32_t base = smem_u32(dsmem);
@@ -761,7 +787,8 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
   tc.stages = dsmem + (aligned - base);
   tc.full = bars;
   tc.empty = bars + NST;
-  tc.acc = bars + 2 * NST;
+  tc.split = bars + 2 * NST;
+  tc.acc = bars + 3 * NST;
   tc.g = 0;
   tc.ntask = 0;
   if (threadIdx.x < 32) {
@@ -769,7 +796,7 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 2 * NST + 1; ++k) mbar_init(bars + k, 1);
+    for (int k = 0; k < 3 * NST + 1; ++k) mbar_init(bars + k, (k >= 2 * NST && k < 3 * NST) ? SPLIT_WARPS : 1);
     fence_mbar_init();
   }
   tc_fence_before();
@@ -793,7 +820,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
   __shared__ int s_task;
   __shared__ int s_ok[4];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   while (true) {
     fence_proxy_async_smem();   // this task's shared-memory writes before the next task's tensor loads
@@ -824,7 +851,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const voi
                                                                        float* __restrict__ C, int* __restrict__ status) {
   extern __shared__ uint8_t dsmem[];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   auto always = [](int, int) { return true; };
@@ -880,7 +907,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   while (true) {
@@ -928,7 +955,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) sub_rrt_kernel(const void* rma
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[2 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   const int mt = ceil_div(m, T);
