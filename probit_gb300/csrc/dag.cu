@@ -27,12 +27,19 @@ namespace pgb {
 
 constexpr int DAG_THREADS = 256;
 constexpr int SC_LD = T + 1;
-// tensor-core pipeline: NST stages of (A_hi, A_lo, B_hi, B_lo) 128 x 32 fp32
-// chunks (16 KB each), unioned with the epilogue tiles sC, sL.
-constexpr int NST = 3;
+// tensor-core pipeline, unioned with the epilogue tiles sC, sL: NST stages
+// of (A, B) 128 x 32 fp32 chunks (16 KB each) that the tensor loads fill
+// and the split turns into their TF32 hi parts in place, and NLO slots of
+// the (A_lo, B_lo) parts.  A stage is reloaded once the MMAs of its chunk
+// completed, a lo slot rewritten once the MMAs of the chunk NLO before.
+constexpr int NST = 4;
+constexpr int NLO = 2;
 constexpr int CHUNK_BYTES = T * 128;             // 128 rows x 32 fp32
-constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;     // A_hi, A_lo, B_hi, B_lo
-constexpr int UNION_BYTES = NST * STAGE_BYTES;   // >= 2 * T * SC_LD * 4
+constexpr int STAGE_BYTES = 2 * CHUNK_BYTES;     // A(hi), B(hi)
+constexpr int LO_BYTES = 2 * CHUNK_BYTES;        // A_lo, B_lo
+constexpr int LO_OFF = NST * STAGE_BYTES;
+constexpr int UNION_BYTES = LO_OFF + NLO * LO_BYTES;   // >= 2 * T * SC_LD * 4
+constexpr int NBARS = 3 * NST + NLO + 1;         // full, empty, split [NST], lofree [NLO], acc
 constexpr size_t DAG_SMEM = UNION_BYTES + (2 * T * 17 + 2 * T) * 4 + 1024 + 64;
 static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
 constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
@@ -377,12 +384,13 @@ __device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_
 // Per-block tensor-core state, uniform across the block.
 struct TcCtx {
   uint32_t tmem;       // accumulator: 128 lanes x 128 fp32 columns
-  uint32_t g;          // chunks loaded so far by this block (stage = g % NST)
+  uint32_t g;          // chunks loaded so far by this block (stage g % NST, lo slot g % NLO)
   uint32_t ntask;      // accumulator commits waited so far
   uint8_t* stages;     // 1024-aligned stage buffers (unioned with sC, sL)
   uint64_t* full;      // [NST] the stage's tensor loads landed
   uint64_t* empty;     // [NST] the MMAs that read the stage completed
   uint64_t* split;     // [NST] the stage's chunk is split (one arrival per splitting warp)
+  uint64_t* lofree;    // [NLO] the MMAs that read the lo slot completed
   uint64_t* acc;       // every MMA issued so far completed
 };
 
@@ -443,7 +451,7 @@ __device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, Wait
   uint8_t* stage = tc.stages + s * STAGE_BYTES;
   mbar_arrive_expect_tx(tc.full + s, 2 * CHUNK_BYTES);
   tma_load_2d(stage, l.amap, l.acol + col, l.arow, tc.full + s);
-  tma_load_2d(stage + 2 * CHUNK_BYTES, l.bmap, l.bcol + col, l.brow, tc.full + s);
+  tma_load_2d(stage + CHUNK_BYTES, l.bmap, l.bcol + col, l.brow, tc.full + s);
   l.issued = c + 1;
   return true;
 }
@@ -463,9 +471,11 @@ __device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& w
 // 2..7 (thread index t - 64), 5 or 6 float4 of A and of B each.
 constexpr int SPLIT_WARPS = DAG_THREADS / 32 - 2;
 constexpr int SPLIT_THREADS = 32 * SPLIT_WARPS;
-__device__ __forceinline__ void convert_stage(uint8_t* stage, int t) {
+__device__ __forceinline__ void convert_stage(uint8_t* stage, uint8_t* lo, int t) {
   float4* ah = reinterpret_cast<float4*>(stage);
-  float4* bh = reinterpret_cast<float4*>(stage + 2 * CHUNK_BYTES);
+  float4* bh = reinterpret_cast<float4*>(stage + CHUNK_BYTES);
+  float4* al = reinterpret_cast<float4*>(lo);
+  float4* bl = reinterpret_cast<float4*>(lo + CHUNK_BYTES);
   constexpr int LO = CHUNK_BYTES / 16;
   constexpr int NQ = (LO + SPLIT_THREADS - 1) / SPLIT_THREADS;
   float4 a[NQ], b[NQ];
@@ -487,22 +497,22 @@ __device__ __forceinline__ void convert_stage(uint8_t* stage, int t) {
     split_tf32(a[q].z, h.z, o.z);
     split_tf32(a[q].w, h.w, o.w);
     ah[e] = h;
-    ah[e + LO] = o;
+    al[e] = o;
     split_tf32(b[q].x, h.x, o.x);
     split_tf32(b[q].y, h.y, o.y);
     split_tf32(b[q].z, h.z, o.z);
     split_tf32(b[q].w, h.w, o.w);
     bh[e] = h;
-    bh[e + LO] = o;
+    bl[e] = o;
   }
 }
 
 // Thread 0: the 12 MMAs of one 32-wide k-chunk, 4 k-steps x (hi lo, lo hi,
 // hi hi), the small terms first so they are not lost against the large one
 // (a fourth product lo lo changed no measured error).
-__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, bool first) {
-  const uint32_t a_hi = smem_u32(stage), a_lo = a_hi + CHUNK_BYTES;
-  const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, const uint8_t* lo, bool first) {
+  const uint32_t a_hi = smem_u32(stage), b_hi = a_hi + CHUNK_BYTES;
+  const uint32_t a_lo = smem_u32(lo), b_lo = a_lo + CHUNK_BYTES;
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {
     const uint32_t o = ks * 32;
@@ -552,8 +562,9 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       if (!mbar_wait_bounded(tc.split + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
       if (l.kt && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
       tc_fence_after();
-      issue_chunk(tc, tc.stages + s * STAGE_BYTES, c == 0 && !preloaded);
+      issue_chunk(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + (g % NLO) * LO_BYTES, c == 0 && !preloaded);
       umma_commit(tc.empty + s);
+      umma_commit(tc.lofree + g % NLO);
     }
   } else if (threadIdx.x == 32) {
     // the loads of the chunks after the first NST - 1 (issued by tc_start),
@@ -568,7 +579,9 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       const uint32_t g = l.base + (uint32_t)c;
       const uint32_t s = g % NST;
       if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
-      convert_stage(tc.stages + s * STAGE_BYTES, threadIdx.x - 64);
+      const uint32_t ls = g % NLO;
+      if (g >= NLO && !mbar_wait_bounded(tc.lofree + ls, ((g / NLO) - 1u) & 1u, MMA_WAIT_NS)) bad = true;
+      convert_stage(tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + ls * LO_BYTES, threadIdx.x - 64);
       fence_proxy_async_smem();   // the split is read by the tensor cores
       __syncwarp();
       if (lane == 0) mbar_arrive(tc.split + s);
@@ -779,7 +792,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
 }
 
 // Block set-up of the tensor-core kernels: 1024-aligned stage buffers in the
-// dynamic shared memory, 3 NST + 1 mbarriers, 128 TMEM columns.
+// dynamic shared memory, NBARS mbarriers, 128 TMEM columns.
 __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32_t* s_tmem) {
   TcCtx tc;
   const uint32_t base = smem_u32(dsmem);
@@ -788,7 +801,8 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
   tc.full = bars;
   tc.empty = bars + NST;
   tc.split = bars + 2 * NST;
-  tc.acc = bars + 3 * NST;
+  tc.lofree = bars + 3 * NST;
+  tc.acc = bars + 3 * NST + NLO;
   tc.g = 0;
   tc.ntask = 0;
   if (threadIdx.x < 32) {
@@ -796,7 +810,7 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < 3 * NST + 1; ++k) mbar_init(bars + k, (k >= 2 * NST && k < 3 * NST) ? SPLIT_WARPS : 1);
+    for (int k = 0; k < NBARS; ++k) mbar_init(bars + k, (k >= 2 * NST && k < 3 * NST) ? SPLIT_WARPS : 1);
     fence_mbar_init();
   }
   tc_fence_before();
@@ -820,7 +834,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
   __shared__ int s_task;
   __shared__ int s_ok[4];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[NBARS];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   while (true) {
     fence_proxy_async_smem();   // this task's shared-memory writes before the next task's tensor loads
@@ -851,7 +865,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) tc_tile_check_kernel(const voi
                                                                        float* __restrict__ C, int* __restrict__ status) {
   extern __shared__ uint8_t dsmem[];
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[NBARS];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   auto always = [](int, int) { return true; };
@@ -907,7 +921,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) syrk_zzt_kernel(const Prob* __
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[NBARS];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   while (true) {
@@ -955,7 +969,7 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) sub_rrt_kernel(const void* rma
   extern __shared__ uint8_t dsmem[];
   __shared__ int s_task;
   __shared__ uint32_t s_tmem;
-  __shared__ __align__(8) uint64_t s_bars[3 * NST + 1];
+  __shared__ __align__(8) uint64_t s_bars[NBARS];
   TcCtx tc = tc_setup(dsmem, s_bars, &s_tmem);
   float* sC = reinterpret_cast<float*>(tc.stages);
   const int mt = ceil_div(m, T);
