@@ -40,6 +40,10 @@ constexpr int LO_BYTES = 2 * CHUNK_BYTES;        // A_lo, B_lo
 constexpr int LO_OFF = NST * STAGE_BYTES;
 constexpr int UNION_BYTES = LO_OFF + NLO * LO_BYTES;   // >= 2 * T * SC_LD * 4
 constexpr int NBARS = 3 * NST + NLO + 1;         // full, empty, split [NST], lofree [NLO], acc
+// tensor memory: the 128 x 128 fp32 accumulator in columns 0..127, then NLO
+// slots of the A operand's (hi, lo) parts, 64 columns each
+constexpr uint32_t A_COL = 128;
+constexpr uint32_t TMEM_COLS = 256;
 constexpr size_t DAG_SMEM = UNION_BYTES + (2 * T * 17 + 2 * T) * 4 + 1024 + 64;
 static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
 constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
@@ -465,60 +469,96 @@ __device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& w
   return true;
 }
 
-// Split the fp32 A and B chunks the loads left in a stage into TF32 hi (in
-// place) and lo parts; the 128-byte swizzle is the same for both, so the
-// split is element by element.  Done by the SPLIT_THREADS threads of warps
-// 2..7 (thread index t - 64), 5 or 6 float4 of A and of B each.
+// Split the fp32 A and B chunks the loads left in a stage into their TF32
+// hi and lo parts (round to nearest), by warps 2..7.  A goes to tensor
+// memory (the MMAs read it from there: `a_col` = hi in columns a_col ..
+// a_col + 31, lo in a_col + 32 .. +63, lane = row), so it costs no shared
+// memory traffic beyond one read; warp w may only write lanes 32 (w % 4) ..
+// +31, so warps 4, 5 take all 32 columns of their rows and warps 2, 6 and
+// 3, 7 half each.  B: hi in place, lo to the lo slot; a quarter of it on
+// each of the four SM sub-partitions (warp w runs on sub-partition w % 4):
+// warps 4 and 5 a quarter each, warps 2, 6, 3, 7 an eighth each, so the
+// shared-memory work of every sub-partition is the same.  The 128-byte
+// swizzle is the same for every part, so the split is element by element.
 constexpr int SPLIT_WARPS = DAG_THREADS / 32 - 2;
-constexpr int SPLIT_THREADS = 32 * SPLIT_WARPS;
-__device__ __forceinline__ void convert_stage(uint8_t* stage, uint8_t* lo, int t) {
-  float4* ah = reinterpret_cast<float4*>(stage);
-  float4* bh = reinterpret_cast<float4*>(stage + CHUNK_BYTES);
-  float4* al = reinterpret_cast<float4*>(lo);
-  float4* bl = reinterpret_cast<float4*>(lo + CHUNK_BYTES);
-  constexpr int LO = CHUNK_BYTES / 16;
-  constexpr int NQ = (LO + SPLIT_THREADS - 1) / SPLIT_THREADS;
-  float4 a[NQ], b[NQ];
+__device__ __forceinline__ void split_a_cols(const uint8_t* stage, int r, int u0, int nu, float (&h)[32],
+                                             float (&o)[32]) {
+  // row r of the swizzled chunk: 16-byte unit u at position u ^ (r % 8)
+  const uint8_t* rowp = stage + r * 128;
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    const int e = t + SPLIT_THREADS * q;
-    if (e < LO) {
-      a[q] = ah[e];
-      b[q] = bh[e];
+  for (int u = 0; u < 8; ++u) {
+    if (u < nu) {
+      const float4 x = *reinterpret_cast<const float4*>(rowp + (((u0 + u) ^ (r & 7)) << 4));
+      split_tf32(x.x, h[4 * u + 0], o[4 * u + 0]);
+      split_tf32(x.y, h[4 * u + 1], o[4 * u + 1]);
+      split_tf32(x.z, h[4 * u + 2], o[4 * u + 2]);
+      split_tf32(x.w, h[4 * u + 3], o[4 * u + 3]);
     }
   }
+}
+
+__device__ __forceinline__ void convert_stage(const TcCtx& tc, uint8_t* stage, uint8_t* lo, uint32_t a_col) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int qd = warp & 3;
+  const int r = 32 * qd + lane;
+  const uint32_t lanes = (uint32_t)(32 * qd) << 16;
+  float h[32], o[32];
+  int b0, nb;   // this warp's float4 of B: b0 + lane + 32 q, q < nb
+  if (warp == 4 || warp == 5) {
+    split_a_cols(stage, r, 0, 8, h, o);
+    tmem_st_32x32(tc.tmem + lanes + a_col, h);
+    tmem_st_32x32(tc.tmem + lanes + a_col + 32, o);
+    b0 = (warp - 4) * 256;
+    nb = 8;
+  } else {
+    const int half = warp >= 6 ? 1 : 0;
+    split_a_cols(stage, r, 4 * half, 4, h, o);
+    float h16[16], o16[16];
 #pragma unroll
-  for (int q = 0; q < NQ; ++q) {
-    const int e = t + SPLIT_THREADS * q;
-    if (e >= LO) break;
-    float4 h, o;
-    split_tf32(a[q].x, h.x, o.x);
-    split_tf32(a[q].y, h.y, o.y);
-    split_tf32(a[q].z, h.z, o.z);
-    split_tf32(a[q].w, h.w, o.w);
-    ah[e] = h;
-    al[e] = o;
-    split_tf32(b[q].x, h.x, o.x);
-    split_tf32(b[q].y, h.y, o.y);
-    split_tf32(b[q].z, h.z, o.z);
-    split_tf32(b[q].w, h.w, o.w);
-    bh[e] = h;
-    bl[e] = o;
+    for (int k = 0; k < 16; ++k) {
+      h16[k] = h[k];
+      o16[k] = o[k];
+    }
+    tmem_st_32x32_x16(tc.tmem + lanes + a_col + 16 * half, h16);
+    tmem_st_32x32_x16(tc.tmem + lanes + a_col + 32 + 16 * half, o16);
+    b0 = 512 + (2 * (warp & 1) + half) * 128;
+    nb = 4;
   }
+  float4* bh = reinterpret_cast<float4*>(stage + CHUNK_BYTES);
+  float4* bl = reinterpret_cast<float4*>(lo + CHUNK_BYTES);
+  float4 b[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+    if (q < nb) b[q] = bh[b0 + lane + 32 * q];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    if (q < nb) {
+      float4 hh, oo;
+      split_tf32(b[q].x, hh.x, oo.x);
+      split_tf32(b[q].y, hh.y, oo.y);
+      split_tf32(b[q].z, hh.z, oo.z);
+      split_tf32(b[q].w, hh.w, oo.w);
+      bh[b0 + lane + 32 * q] = hh;
+      bl[b0 + lane + 32 * q] = oo;
+    }
+  }
+  tmem_wait_st();
 }
 
 // Thread 0: the 12 MMAs of one 32-wide k-chunk, 4 k-steps x (hi lo, lo hi,
 // hi hi), the small terms first so they are not lost against the large one
 // (a fourth product lo lo changed no measured error).
-__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, const uint8_t* lo, bool first) {
-  const uint32_t a_hi = smem_u32(stage), b_hi = a_hi + CHUNK_BYTES;
-  const uint32_t a_lo = smem_u32(lo), b_lo = a_lo + CHUNK_BYTES;
+__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, const uint8_t* lo, uint32_t a_col,
+                                            bool first) {
+  const uint32_t b_hi = smem_u32(stage) + CHUNK_BYTES, b_lo = smem_u32(lo) + CHUNK_BYTES;
+  const uint32_t a_hi = tc.tmem + a_col, a_lo = a_hi + 32;
 #pragma unroll
   for (int ks = 0; ks < 4; ++ks) {
-    const uint32_t o = ks * 32;
-    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
-    umma_tf32(tc.tmem, sdesc_sw128(a_lo + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
-    umma_tf32(tc.tmem, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+    const uint32_t o = ks * 32;   // bytes into the swizzled B rows
+    const uint32_t ka = ks * 8;   // tensor-memory columns of A
+    umma_tf32_ts(tc.tmem, a_hi + ka, sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
+    umma_tf32_ts(tc.tmem, a_lo + ka, sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+    umma_tf32_ts(tc.tmem, a_hi + ka, sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
   }
 }
 
@@ -562,7 +602,8 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       if (!mbar_wait_bounded(tc.split + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
       if (l.kt && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
       tc_fence_after();
-      issue_chunk(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + (g % NLO) * LO_BYTES, c == 0 && !preloaded);
+      issue_chunk(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + (g % NLO) * LO_BYTES, A_COL + 64 * (g % NLO),
+                  c == 0 && !preloaded);
       umma_commit(tc.empty + s);
       umma_commit(tc.lofree + g % NLO);
     }
@@ -581,8 +622,9 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
       const uint32_t ls = g % NLO;
       if (g >= NLO && !mbar_wait_bounded(tc.lofree + ls, ((g / NLO) - 1u) & 1u, MMA_WAIT_NS)) bad = true;
-      convert_stage(tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + ls * LO_BYTES, threadIdx.x - 64);
+      convert_stage(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + ls * LO_BYTES, A_COL + 64 * ls);
       fence_proxy_async_smem();   // the split is read by the tensor cores
+      tc_fence_before();
       __syncwarp();
       if (lane == 0) mbar_arrive(tc.split + s);
     }
@@ -792,7 +834,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
 }
 
 // Block set-up of the tensor-core kernels: 1024-aligned stage buffers in the
-// dynamic shared memory, NBARS mbarriers, 128 TMEM columns.
+// dynamic shared memory, NBARS mbarriers, TMEM_COLS tensor-memory columns.
 __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32_t* s_tmem) {
   TcCtx tc;
   const uint32_t base = smem_u32(dsmem);
@@ -806,7 +848,7 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
   tc.g = 0;
   tc.ntask = 0;
   if (threadIdx.x < 32) {
-    tmem_alloc(s_tmem, 128);
+    tmem_alloc(s_tmem, TMEM_COLS);
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
@@ -823,7 +865,7 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
 __device__ __forceinline__ void tc_teardown(const TcCtx& tc) {
   tc_fence_before();
   __syncthreads();
-  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, 128);
+  if (threadIdx.x < 32) tmem_dealloc(tc.tmem, TMEM_COLS);
 }
 
 template <int DM>
