@@ -37,7 +37,7 @@ sys.path.insert(0, str(ROOT))
 METRIC = "Laplace evidence+grad solves/s"
 # dram__bytes_read.sum + dram__bytes_write.sum of one N = 8192 factorisation
 # launch (ncu capture summarised in profiles/dag_factor_kernel_gaussian_N8192.md)
-FACTOR_TRAFFIC_N8192 = 83.221760e6 + 116.572928e6
+FACTOR_TRAFFIC_N8192 = 85.472512e6 + 116.641792e6
 # nominal dense TF32 tensor rate of a GB300 (TFLOP/s); a 3xTF32 product issues
 # three TF32 MMAs per algorithmic one
 TF32_NOMINAL_TFLOPS = 1100.0

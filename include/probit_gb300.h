@@ -164,6 +164,23 @@ int pgb_objective(pgb_gp* gp, const float* X, const void* y, const float* theta,
 int pgb_value_and_grad(pgb_gp* gp, const float* X, const void* y, const float* theta,
                        float* value_out, float* grad_out, void* stream);
 
+/* Variational-Bayes fixed point w* from w = 0: w <- (sigma^2 I + K)^-1
+ * (K w + sigma d log p(K w)), stopped like pgb_weight (the handle's tolerance
+ * and maxiter).  Replaces VBGP.weight (approximators.py:332-334) with fwd_solver
+ * (implicit/solvers.py:7-15) over f_VB (implicit/VB.py:4-17).  The posterior
+ * precision of VBGP.precision (approximators.py:336-339) is 1 / sigma^2 at
+ * every point and its mean K w* (pgb_precision's f_out).  Leaves the factor
+ * of I + K / sigma^2 resident (not a Laplace posterior for pgb_predict's
+ * reuse_factor). */
+int pgb_vb_weight(pgb_gp* gp, const float* X, const void* y, const float* theta,
+                  float* w_out, void* stream);
+
+/* The VB objective at the fixed point (one float written to value_out).
+ * Replaces VBGP.objective (approximators.py:317-330) -> objective_VB
+ * (implicit/VB.py:20-40).  Its gradient is not provided. */
+int pgb_vb_objective(pgb_gp* gp, const float* X, const void* y, const float* theta,
+                     float* value_out, void* stream);
+
 /* Factor B = I + W^1/2 K W^1/2 at the handle's resident precision W (from
  * its last fit) into the resident L, without any right-hand side.  This is
  * the Cholesky of objective_LA (implicit/Laplace.py:24) on its own, for

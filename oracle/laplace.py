@@ -26,6 +26,7 @@ __all__ = [
     "scaled_sq_dists", "gram", "gram_diag", "lik_terms", "newton_weight",
     "precision", "objective", "value_and_grad", "predict", "predict_covariance",
     "predictive_distributions", "objective_bform", "newton_weight_bform",
+    "vb_map", "vb_weight", "vb_objective", "vb_objective_bform",
 ]
 
 KERNELS = ("eq", "matern12", "eq_periodic")
@@ -533,3 +534,86 @@ def objective_bform(prob: Problem, theta, a, dtype=np.float64):
     sw = np.sqrt(-t["d2"])
     L = np.linalg.cholesky(np.eye(K.shape[0], dtype=dt) + sw[:, None] * K * sw[None, :])
     return dt(-np.sum(t["logp"]) + 0.5 * f @ a + np.sum(np.log(np.diag(L))))
+
+
+# ---------------------------------------------------------------- Variational Bayes
+
+def vb_map(prob: Problem, theta, w, dtype=np.float64, K=None, L_cov=None):
+    """``f_VB`` (``implicit/VB.py:4-17``): (sigma^2 I + K)^-1 (K w + sigma d log p(K w)),
+    the Cholesky of sigma^2 I + K solved twice (``B.cholesky_solve``)."""
+    dt = np.dtype(dtype).type
+    if K is None:
+        K = _K(prob, theta, dt)
+    _, _, sig, cut = prob.split(theta)
+    N = K.shape[0]
+    if L_cov is None:
+        L_cov = np.linalg.cholesky(dt(sig) ** 2 * np.eye(N, dtype=dt) + K)
+    m = K @ np.asarray(w, dtype=dt)
+    t = lik_terms(prob.likelihood, m, prob.y, sig, cut, dt)
+    rhs = m + dt(sig) * t["d1"]
+    return sla.cho_solve((L_cov, True), rhs, check_finite=False).astype(dt)
+
+
+def vb_weight(prob: Problem, theta, tol=1e-5, maxiter=100, dtype=np.float64, K=None):
+    """``VBGP.weight`` (``approximators.py:332-334``): ``fwd_solver``
+    (``implicit/solvers.py:7-15``, jaxopt ``FixedPointIteration``) over ``f_VB``
+    from w = 0; stop once ||w_k - w_{k-1}|| <= tol or after maxiter updates.
+    sigma^2 I + K does not depend on w, so it is factored once.  Returns (w, iterations)."""
+    dt = np.dtype(dtype).type
+    if K is None:
+        K = _K(prob, theta, dt)
+    _, _, sig, _ = prob.split(theta)
+    N = K.shape[0]
+    L_cov = np.linalg.cholesky(dt(sig) ** 2 * np.eye(N, dtype=dt) + K)
+    w = np.zeros(N, dtype=dt)
+    it = 0
+    while True:
+        w_new = vb_map(prob, theta, w, dt, K, L_cov)
+        err = np.sqrt(np.sum((w_new - w) ** 2, dtype=dt))
+        w = w_new
+        it += 1
+        if not (err > tol) or it >= maxiter:
+            break
+    return w, it
+
+
+def vb_objective(prob: Problem, theta, w, dtype=np.float64, K=None):
+    """``objective_VB`` (``implicit/VB.py:20-40``) at the weight w, term by term."""
+    dt = np.dtype(dtype).type
+    if K is None:
+        K = _K(prob, theta, dt)
+    _, _, sig, cut = prob.split(theta)
+    N = K.shape[0]
+    w = np.asarray(w, dtype=dt)
+    m = K @ w
+    L_cov = np.linalg.cholesky(dt(sig) ** 2 * np.eye(N, dtype=dt) + K)
+    L_inv = sla.solve_triangular(L_cov, np.eye(N, dtype=dt), lower=True)
+    cov = sla.solve_triangular(L_cov.T, L_inv, lower=False)
+    log_det_cov = -2.0 * np.sum(np.log(np.diag(L_cov)))
+    trace_cov = np.sum(np.diag(cov))
+    trace_posterior_cov_div_var = np.einsum("ij,ij->", K, cov)
+    trace_K_inv_posterior_cov = dt(sig) ** 2 * trace_cov
+    t = lik_terms(prob.likelihood, m, prob.y, sig, cut, dt)
+    return dt(0.5 * trace_posterior_cov_div_var + 0.5 * trace_K_inv_posterior_cov + 0.5 * m @ w
+              - N * np.log(sig) - 0.5 * log_det_cov - 0.5 * N - np.sum(t["logp"]))
+
+
+def vb_objective_bform(prob: Problem, theta, w, dtype=np.float64, K=None):
+    """The same objective in the form the CUDA path evaluates it, with
+    B = I + K / sigma^2 = L L^T (so sigma^2 I + K = sigma^2 B):
+    sum_i [1/2 rowdot_i / sigma + 1/2 (B^-1)_ii + 1/2 m_i w_i + log L_ii - 1/2 - log p_i],
+    rowdot_i = sum_j (B^-1)_ij K_ij / sigma."""
+    dt = np.dtype(dtype).type
+    if K is None:
+        K = _K(prob, theta, dt)
+    _, _, sig, cut = prob.split(theta)
+    N = K.shape[0]
+    w = np.asarray(w, dtype=dt)
+    m = K @ w
+    B = np.eye(N, dtype=dt) + K / dt(sig) ** 2
+    L = np.linalg.cholesky(B)
+    Binv = sla.cho_solve((L, True), np.eye(N, dtype=dt))
+    rowdot = np.sum(Binv * K, axis=1) / dt(sig)
+    t = lik_terms(prob.likelihood, m, prob.y, sig, cut, dt)
+    return dt(np.sum(0.5 * rowdot / sig + 0.5 * np.diag(Binv) + 0.5 * m * w + np.log(np.diag(L)) - 0.5
+                     - t["logp"]))

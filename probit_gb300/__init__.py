@@ -6,7 +6,7 @@ A drop-in for the Laplace path of the reference package (bb515/probit):
 CUDA kernels behind the C-ABI declared in ``include/probit_gb300.h``.
 """
 
-from .approximators import LaplaceGP
+from .approximators import LaplaceGP, VBGP
 from .batch import LaplaceBatch
 from .kernels import EQ, Matern12
 from .utilities import (
@@ -20,7 +20,7 @@ from .utilities import (
 )
 
 __all__ = [
-    "LaplaceGP", "LaplaceBatch", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
+    "LaplaceGP", "VBGP", "LaplaceBatch", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
     "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
     "check_cutpoints", "probit_predictive_distributions",
 ]

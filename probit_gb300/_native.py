@@ -88,6 +88,8 @@ _SIGS = {
     "pgb_precision": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_approximate_posterior": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_vb_weight": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_vb_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_factor": (C.c_int, [_VP, _VP]),
     "pgb_predict": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, _VP, C.c_int32, _VP]),

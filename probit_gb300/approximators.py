@@ -385,6 +385,82 @@ class LaplaceGP:
         return self.precision(weight, parameters)[1]
 
 
+class VBGP(LaplaceGP):
+    """A GP posterior approximation using Variational Bayes (``VBGP``,
+    ``approximators.py:280-339``).
+
+    The weight is the fixed point of ``f_VB`` (``implicit/VB.py:4-17``),
+    w <- (sigma^2 I + K)^-1 (K w + sigma d log p(K w)), iterated from w = 0
+    with the stopping rule of ``fwd_solver`` (``implicit/solvers.py:7-15``);
+    sigma^2 I + K = sigma^2 (I + K / sigma^2) is factored once on the device
+    and every step is a Gram matvec and two triangular solves.  The objective
+    is ``objective_VB`` (``implicit/VB.py:20-40``); its gradient
+    (``value_and_grad``) is not provided.  The precision is 1 / sigma^2 at
+    every point (``approximators.py:336-339``), so ``predict`` and
+    ``predict_covariance`` are those of the base class with that precision.
+    Same constructor, data and parameter conventions as :class:`LaplaceGP`.
+    """
+
+    def __repr__(self):
+        return "VBGP"
+
+    def construct(self):
+        raise NotImplementedError("VBGP.construct: the VB map is evaluated inside pgb_vb_weight only")
+
+    def objective(self):
+        """params -> objective_VB at the VB fixed point."""
+
+        def objective_fn(parameters):
+            import torch
+
+            theta, key = self._theta(parameters)
+            gp = self._handle(key)
+            X, y = self._device_data()
+            td = self._theta_dev(theta)
+            v = torch.empty(1, dtype=torch.float32, device=td.device)
+            N.check(gp.lib.pgb_vb_objective(gp.h, X.data_ptr(), y.data_ptr(), td.data_ptr(), v.data_ptr(),
+                                            stream_handle(td.device)), "pgb_vb_objective")
+            out = float(v.item())
+            self._after(gp, "objective")
+            return out
+
+        return objective_fn
+
+    def value_and_grad(self):
+        raise NotImplementedError("VBGP.value_and_grad: the gradient of the VB objective is not provided")
+
+    def weight(self, parameters):
+        """VB fixed point w* from w = 0 (``VBGP.weight``)."""
+        import torch
+
+        theta, key = self._theta(parameters)
+        gp = self._handle(key)
+        X, y = self._device_data()
+        td = self._theta_dev(theta)
+        w = torch.empty(self.N, dtype=torch.float32, device=td.device)
+        N.check(gp.lib.pgb_vb_weight(gp.h, X.data_ptr(), y.data_ptr(), td.data_ptr(), w.data_ptr(),
+                                     stream_handle(td.device)), "pgb_vb_weight")
+        self._after(gp, "weight")
+        return self._out(w)
+
+    def precision(self, weight, parameters):
+        """(1 / sigma^2 at every point, K weight) (``VBGP.precision``)."""
+        import torch
+
+        _, f = LaplaceGP.precision(self, weight, parameters)
+        lp = parameters[1] if isinstance(parameters[1], (tuple, list)) else (parameters[1],)
+        sig = float(lp[0].item() if hasattr(lp[0], "item") else lp[0])
+        W = torch.full((self.N,), 1.0 / (sig * sig), dtype=torch.float32, device=require_cuda())
+        return self._out(W), f
+
+    def approximate_posterior(self, parameters):
+        """(weight, precision) at the VB fixed point."""
+        w = self.weight(parameters)
+        W, _ = self.precision(w, parameters)
+        self._last = None
+        return w, W
+
+
 def _zip_grads(leaves, params):
     if isinstance(params, tuple):
         return tuple(_zip_grads(l, p) for l, p in zip(leaves, params))

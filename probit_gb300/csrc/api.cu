@@ -50,7 +50,12 @@ using namespace pgb;
 
 namespace {
 
-enum GraphOp { OP_WEIGHT = 0, OP_POSTERIOR = 1, OP_OBJECTIVE = 2, OP_VG = 3, OP_COUNT = 4 };
+enum GraphOp {
+  OP_WEIGHT = 0, OP_POSTERIOR = 1, OP_OBJECTIVE = 2, OP_VG = 3,   // Laplace
+  OP_VB_WEIGHT = 4, OP_VB_OBJECTIVE = 5,                         // Variational Bayes
+  OP_COUNT = 6
+};
+bool is_vb(int op) { return op == OP_VB_WEIGHT || op == OP_VB_OBJECTIVE; }
 enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_COUNT = 4 };
 enum Counter { C_DAG = 0, C_TRSV_T = 1, C_PREDICT = 2, C_TRSV_L = 3, C_SYRK = 4, C_COUNT = 8 };
 
@@ -149,7 +154,7 @@ struct Engine {
   int2* claims = nullptr;
   int nclaims = 0;
   // graphs
-  cudaGraphExec_t gexec[OP_COUNT] = {nullptr, nullptr, nullptr, nullptr};
+  cudaGraphExec_t gexec[OP_COUNT] = {};
   cudaStream_t cap_s = nullptr, cap_s2 = nullptr;
   int grad_ready = 0;
   int eager = 0;                           // PGB_EAGER=1: kernels launched directly, host-driven loop
@@ -664,13 +669,51 @@ void enq_grad(Engine& e, cudaStream_t s) {
   launch_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
 }
 
-void enq_prologue(Engine& e, cudaStream_t s) {
+// One step of the VB fixed point w <- (sigma^2 I + K)^-1 (K w + sigma d1(K w))
+// with the resident factor of B = I + K / sigma^2: f += K da, t = f + sigma
+// d1, x = B^-1 t by the two wavefront solves, w = x / sigma^2, stopping rule.
+void enq_vb_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
+  enq_matvec(e, MatvecOp{F_DA, F_NONE, F_F, 0, 1, 1}, s);
+  launch_vb_rhs(e.probs, e.vmap, e.nvb, s);
+  cudaMemsetAsync(e.tflags_all, 0, sizeof(int) * e.tflags_words, s);
+  cudaMemsetAsync(e.counters + C_TRSV_T, 0, sizeof(int) * 3, s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 0, e.counters + C_TRSV_L, 1, 1, trsv_grid(e), s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 1, e.counters + C_TRSV_T, 0, 1, trsv_grid(e), s);
+  launch_vb_update(e.probs, e.vmap, e.nvb, s);
+  launch_newton_finalize(e.probs, e.nprob, e.any_active, h, use_cond, s);
+}
+
+void enq_step(Engine& e, int op, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
+  if (is_vb(op))
+    enq_vb_step(e, s, h, use_cond);
+  else
+    enq_newton_step(e, s, h, use_cond);
+}
+
+void enq_prologue(Engine& e, int op, cudaStream_t s) {
   launch_reset_problems(e.probs, e.vmap, e.nvb, 1, s);
   launch_prep_features(e.probs, e.vmap, e.nvb, s);
+  if (is_vb(op)) {
+    // B = I + K / sigma^2 does not change along the VB iteration: factor once
+    launch_vb_setup(e.probs, e.vmap, e.nvb, s);
+    enq_dag(e, JOB_NONE, s);
+    launch_vb_mark(e.probs, e.nprob, s);
+  }
 }
 
 void enq_epilogue(Engine& e, int op, cudaStream_t s) {
-  if (op >= OP_POSTERIOR) {
+  if (op == OP_VB_OBJECTIVE) {
+    launch_activate_enabled(e.probs, e.nprob, s);
+    enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);       // f = K w
+    launch_vb_terms(e.probs, e.vmap, e.nvb, s);              // log p(f)
+    enq_dag(e, JOB_IDENT, s);                                // L^-T on the resident factor
+    cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
+    launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);   // B^-1
+    enq_matvec(e, MatvecOp{F_SW, F_NONE, F_ROWDOT, 1, 1}, s);   // rowdot_i = sum_j B^-1_ij K_ij / sigma
+    launch_vb_evidence(e.probs, e.vmap, e.nvb, e.nprob, s);
+    return;
+  }
+  if (op >= OP_POSTERIOR && !is_vb(op)) {
     launch_activate_enabled(e.probs, e.nprob, s);   // every enabled problem takes part from here on
     enq_precision(e, s);
     launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
@@ -685,14 +728,14 @@ void enq_epilogue(Engine& e, int op, cudaStream_t s) {
 // driven from the host (one flag read per step).  For profilers that do not
 // follow kernels inside conditional graph nodes.
 int run_eager(Engine& e, int op, cudaStream_t s) {
-  if (op == OP_VG) PGB_TRY(ensure_grad_buffers(e));
-  enq_prologue(e, s);
+  if (op == OP_VG || op == OP_VB_OBJECTIVE) PGB_TRY(ensure_grad_buffers(e));
+  enq_prologue(e, op, s);
   const char* tv = std::getenv("PGB_TRACE");
   const bool trace = tv && tv[0] == '1';
   int maxiter = 1;
   for (const pgb_desc& d : e.desc) maxiter = std::max(maxiter, d.maxiter);
   for (int it = 0; it < maxiter; ++it) {
-    enq_newton_step(e, s, 0, 0);
+    enq_step(e, op, s, 0, 0);
     int again = 0;
     float err = 0.0f;
     CU_TRY(cudaMemcpyAsync(&again, e.any_active + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
@@ -709,11 +752,11 @@ int run_eager(Engine& e, int op, cudaStream_t s) {
 // Capture the graph of one operation.
 int build_graph(Engine& e, int op) {
   if (e.gexec[op]) return PGB_OK;
-  if (op == OP_VG) PGB_TRY(ensure_grad_buffers(e));
+  if (op == OP_VG || op == OP_VB_OBJECTIVE) PGB_TRY(ensure_grad_buffers(e));
   cudaStream_t s = e.cap_s, s2 = e.cap_s2;
   cudaGraph_t g = nullptr;
   CU_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-  enq_prologue(e, s);
+  enq_prologue(e, op, s);
   // WHILE node for the Newton loop
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg = nullptr;
@@ -732,7 +775,7 @@ int build_graph(Engine& e, int op) {
   cudaGraph_t body = cp.conditional.phGraph_out[0];
   CU_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
   CU_TRY(cudaStreamBeginCaptureToGraph(s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  enq_newton_step(e, s2, h, 1);
+  enq_step(e, op, s2, h, 1);
   cudaGraph_t body_out = nullptr;
   CU_TRY(cudaStreamEndCapture(s2, &body_out));
   enq_epilogue(e, op, s);
@@ -898,6 +941,29 @@ int pgb_weight(pgb_gp* gp, const float* X, const void* y, const float* theta, fl
   PGB_TRY(run_op(e, OP_WEIGHT, s));
   gp->factor_valid = 0;
   CU_TRY(cudaMemcpyAsync(a_out, e.hp[0].a, sizeof(float) * e.sh[0].n, cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_vb_weight(pgb_gp* gp, const float* X, const void* y, const float* theta, float* w_out, void* stream) {
+  if (!gp || !w_out || !y) return PGB_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_VB_WEIGHT, s));
+  gp->factor_valid = 0;   // the resident factor is of I + K / sigma^2
+  CU_TRY(cudaMemcpyAsync(w_out, e.hp[0].a, sizeof(float) * e.sh[0].n, cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_vb_objective(pgb_gp* gp, const float* X, const void* y, const float* theta, float* value_out,
+                     void* stream) {
+  if (!gp || !value_out || !y) return PGB_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_VB_OBJECTIVE, s));
+  gp->factor_valid = 0;
+  CU_TRY(cudaMemcpyAsync(value_out, e.value_all, sizeof(float), cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 

@@ -143,6 +143,15 @@ void launch_newton_finalize(const Prob* probs, int nprob, int* any_active, cudaG
                             int use_cond, cudaStream_t st);
 void launch_lik_full(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
+// Variational Bayes (VBGP): B = I + K / sigma^2 (sw = 1 / sigma), so
+// sigma^2 I + K = sigma^2 B and the factor of B serves the fixed point and
+// the objective.
+void launch_vb_setup(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_mark(const Prob* probs, int nprob, cudaStream_t st);
+void launch_vb_rhs(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_terms(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_grad_vec1(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_scale_tz(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_grad_vec3(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);

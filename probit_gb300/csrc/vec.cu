@@ -266,6 +266,151 @@ void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob
   evidence_sum_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob);
 }
 
+// ---------------------------------------------------------------- Variational Bayes
+// VBGP (approximators.py:280-339) with the maps of implicit/VB.py:
+//   f_VB(w) = (sigma^2 I + K)^-1 (K w + sigma d log p(K w))        (VB.py:4-17)
+// iterated by fwd_solver from w = 0 (approximators.py:332-334), and
+//   objective_VB = 1/2 sum(K o cov) + 1/2 sigma^2 tr(cov) + 1/2 (K w)^T w
+//                  - N log sigma - 1/2 log det cov - N/2 - sum log p(K w)
+// with cov = (sigma^2 I + K)^-1 (VB.py:20-40).  With B = I + K / sigma^2
+// (the B of this library at W = 1 / sigma^2) and L L^T = B:
+//   (sigma^2 I + K)^-1 v = B^-1 v / sigma^2,  log det cov = -2 (N log sigma + sum log L_ii),
+// so objective_VB = sum_i [1/2 rowdot_i / sigma + 1/2 (B^-1)_ii + 1/2 f_i w_i
+//                          + log L_ii - 1/2 - log p_i]
+// where rowdot_i = sum_j (B^-1)_ij K_ij sw_j, sw = 1 / sigma.
+
+// sw = 1 / sigma, W = 1 / sigma^2 on the data points (0 on the padding)
+__global__ void vb_setup_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  const float sig = theta_sigma(P.sh, P.theta);
+  const bool in = i < P.sh.n;
+  P.sw[i] = in ? 1.0f / sig : 0.0f;
+  P.W[i] = in ? 1.0f / (sig * sig) : 0.0f;
+  P.sw_prev[i] = P.sw[i];
+}
+
+void launch_vb_setup(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_setup_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// After the factorisation of B: the resident factor serves every step.
+__global__ void vb_mark_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  if (*P.active == 0) return;
+  const int ok = P.status[ST_CODE] == 0 ? 1 : 0;
+  P.reuse[0] = ok;
+  P.reuse[2] = ok;
+}
+
+void launch_vb_mark(const Prob* probs, int nprob, cudaStream_t st) {
+  vb_mark_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
+}
+
+// t = f + sigma d log p(f) (padding 0): the right-hand side of one step
+__global__ void vb_rhs_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.d1[i] = 0.0f;
+    P.t[i] = 0.0f;
+    return;
+  }
+  const Shape sh = P.sh;
+  int yi;
+  const float yv = load_y(sh, P.y, i, &yi);
+  const float sig = theta_sigma(sh, P.theta);
+  LikOut o;
+  lik_point<false>(sh.lik, P.f[i], yv, yi, sig, theta_cutpoints(sh, P.theta), o);
+  P.d1[i] = o.d1;
+  P.t[i] = P.f[i] + sig * o.d1;
+}
+
+void launch_vb_rhs(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_rhs_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// w_new = (B^-1 t) / sigma^2 (x holds B^-1 t); block partial of ||w_new - w||^2;
+// da = w_new - w (f follows w by f += K da)
+__global__ void vb_update_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sred[VT / 32];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;   // uniform per block
+  const int i = m.y * VT + threadIdx.x;
+  float e = 0.0f;
+  if (i < P.sh.n) {
+    const float sig = theta_sigma(P.sh, P.theta);
+    const float ai = P.a[i];
+    const float an = P.x[i] / (sig * sig);
+    const float dlt = an - ai;
+    e = dlt * dlt;
+    P.a[i] = an;
+    P.da[i] = dlt;
+  } else if (i < P.n_pad) {
+    P.da[i] = 0.0f;
+  }
+  const double s = block_sum_d<VT>(e, sred);
+  if (threadIdx.x == 0) P.part[m.y] = s;
+}
+
+void launch_vb_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_update_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// log p at the final f = K w
+__global__ void vb_terms_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.logp[i] = 0.0f;
+    return;
+  }
+  const Shape sh = P.sh;
+  int yi;
+  const float yv = load_y(sh, P.y, i, &yi);
+  LikOut o;
+  lik_point<false>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
+  P.logp[i] = o.logp;
+}
+
+void launch_vb_terms(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_terms_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+__global__ void vb_evidence_partial_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sred[VT / 32];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  float v = 0.0f;
+  if (i < P.sh.n) {
+    const float sig = theta_sigma(P.sh, P.theta);
+    v = 0.5f * P.rowdot[i] / sig + 0.5f * __ldcg(P.Binv + (size_t)i * P.ld + i) + 0.5f * P.f[i] * P.a[i] +
+        logf(__ldcg(P.L + (size_t)i * P.ld + i)) - 0.5f - P.logp[i];
+  }
+  const double s = block_sum_d<VT>(v, sred);
+  if (threadIdx.x == 0) P.part[m.y] = s;
+}
+
+void launch_vb_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  vb_evidence_partial_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+  evidence_sum_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob);
+}
+
 // ---------------------------------------------------------------- gradient
 // s = 1/2 diag(Sigma) d3 with diag(Sigma)_i = rowdot_i / sw_i
 // (rowdot_i = sum_j B^-1_ij sw_j K_ji, i.e. Sigma = W^-1/2 B^-1 W^1/2 K),
