@@ -177,9 +177,17 @@ int pgb_vb_weight(pgb_gp* gp, const float* X, const void* y, const float* theta,
 
 /* The VB objective at the fixed point (one float written to value_out).
  * Replaces VBGP.objective (approximators.py:317-330) -> objective_VB
- * (implicit/VB.py:20-40).  Its gradient is not provided. */
+ * (implicit/VB.py:20-40). */
 int pgb_vb_objective(pgb_gp* gp, const float* X, const void* y, const float* theta,
                      float* value_out, void* stream);
+
+/* The VB objective and its gradient in theta (pgb_theta_size floats; entries
+ * for infinite cutpoints are 0) through the implicit layer: the adjoint
+ * fixed point of fixed_point_layer_bwd (implicit/solvers.py:52-64) over f_VB,
+ * solved by the same iteration and stopping rule.  Replaces
+ * Approximator.value_and_grad (approximators.py:132-134) for VBGP. */
+int pgb_vb_value_and_grad(pgb_gp* gp, const float* X, const void* y, const float* theta,
+                          float* value_out, float* grad_out, void* stream);
 
 /* Factor B = I + W^1/2 K W^1/2 at the handle's resident precision W (from
  * its last fit) into the resident L, without any right-hand side.  This is

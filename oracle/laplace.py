@@ -26,7 +26,7 @@ __all__ = [
     "scaled_sq_dists", "gram", "gram_diag", "lik_terms", "newton_weight",
     "precision", "objective", "value_and_grad", "predict", "predict_covariance",
     "predictive_distributions", "objective_bform", "newton_weight_bform",
-    "vb_map", "vb_weight", "vb_objective", "vb_objective_bform",
+    "vb_map", "vb_weight", "vb_objective", "vb_objective_bform", "vb_value_and_grad",
 ]
 
 KERNELS = ("eq", "matern12", "eq_periodic")
@@ -617,3 +617,53 @@ def vb_objective_bform(prob: Problem, theta, w, dtype=np.float64, K=None):
     t = lik_terms(prob.likelihood, m, prob.y, sig, cut, dt)
     return dt(np.sum(0.5 * rowdot / sig + 0.5 * np.diag(Binv) + 0.5 * m * w + np.log(np.diag(L)) - 0.5
                      - t["logp"]))
+
+
+def vb_value_and_grad(prob: Problem, theta, tol=1e-5, maxiter=100, dtype=np.float64):
+    """``VBGP`` value and gradient: ``objective_VB`` at w*(theta) through
+    ``fixed_point_layer`` (``implicit/solvers.py:28-64``) over ``f_VB``.
+
+    With A = sigma^2 I + K, m = K w*, D2 = diag(d2(m)): the adjoint of
+    ``fixed_point_layer_bwd`` is the fixed point u = K (I + sigma D2) A^-1 u
+    + zbar, zbar = d obj / d w = K (w - d1) (solved here directly), v = A^-1 u,
+    and, the trace terms of the objective summing to N/2 exactly,
+      prior k : 1/2 tr(A^-1 dK_k) + c^T dK_k w,  c = w/2 - d1 + sigma v d2
+      sigma   : (tr(B^-1) - N) / sigma - sum dlogp/dsigma
+                + v^T (d1 + sigma dd1/dsigma - 2 sigma w),   B = A / sigma^2
+      b (cut) : -sum dlogp/db + sigma v^T dd1/db.
+    Returns (value, grad (n_theta,), w, iterations)."""
+    dt = np.dtype(dtype).type
+    K = _K(prob, theta, dt)
+    w, it = vb_weight(prob, theta, tol, maxiter, dt, K=K)
+    val = vb_objective(prob, theta, w, dt, K=K)
+    ell, s, sig, cut = prob.split(theta)
+    N = K.shape[0]
+    m = K @ w
+    t = lik_terms(prob.likelihood, m, prob.y, sig, cut, dt)
+    A = dt(sig) ** 2 * np.eye(N, dtype=dt) + K
+    cf = sla.cho_factor(A, lower=True, check_finite=False)
+    Ainv = sla.cho_solve(cf, np.eye(N, dtype=dt), check_finite=False)
+    d1, d2 = t["d1"], t["d2"]
+    zbar = K @ (w - d1)
+    Jt = K @ ((dt(1) + dt(sig) * d2)[:, None] * Ainv)
+    u = sla.solve(np.eye(N, dtype=dt) - Jt, zbar, check_finite=False)
+    v = Ainv @ u
+    c = dt(0.5) * w - d1 + dt(sig) * v * d2
+    nl = prob.n_lengthscales
+    grad = np.zeros(prob.n_theta, dtype=np.float64)
+    _, dKs = gram_param_derivs(prob.kernel, prob.X, ell, float(s), prob.period)
+    for k, dK in enumerate(dKs):
+        grad[k] = 0.5 * np.sum(Ainv * dK) + c @ (dK @ w)
+    trBinv = float(sig) ** 2 * np.trace(Ainv)
+    grad[nl + 1] = ((trBinv - N) / sig - np.sum(t["dlogp_dsig"])
+                    + v @ (d1 + dt(sig) * t["dd1_dsig"] - dt(2 * sig) * w))
+    if prob.likelihood != "gaussian":
+        lo = -t["dlogp_dlo"] + dt(sig) * v * t["dd1_dlo"]
+        hi = -t["dlogp_dhi"] + dt(sig) * v * t["dd1_dhi"]
+        gc = np.zeros(prob.J + 1)
+        np.add.at(gc, t["y"], lo)
+        np.add.at(gc, t["y"] + 1, hi)
+        gc[0] = 0.0
+        gc[prob.J] = 0.0
+        grad[nl + 2:] = gc
+    return dt(val), grad.astype(dt), w, it

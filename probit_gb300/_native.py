@@ -90,6 +90,7 @@ _SIGS = {
     "pgb_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_vb_weight": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_vb_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_vb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_factor": (C.c_int, [_VP, _VP]),
     "pgb_predict": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP, _VP, C.c_int32, _VP]),

@@ -394,8 +394,9 @@ class VBGP(LaplaceGP):
     with the stopping rule of ``fwd_solver`` (``implicit/solvers.py:7-15``);
     sigma^2 I + K = sigma^2 (I + K / sigma^2) is factored once on the device
     and every step is a Gram matvec and two triangular solves.  The objective
-    is ``objective_VB`` (``implicit/VB.py:20-40``); its gradient
-    (``value_and_grad``) is not provided.  The precision is 1 / sigma^2 at
+    is ``objective_VB`` (``implicit/VB.py:20-40``) and ``value_and_grad`` its
+    gradient through the implicit layer (``implicit/solvers.py:28-64``): the
+    adjoint fixed point over ``f_VB`` on the same factor.  The precision is 1 / sigma^2 at
     every point (``approximators.py:336-339``), so ``predict`` and
     ``predict_covariance`` are those of the base class with that precision.
     Same constructor, data and parameter conventions as :class:`LaplaceGP`.
@@ -427,7 +428,28 @@ class VBGP(LaplaceGP):
         return objective_fn
 
     def value_and_grad(self):
-        raise NotImplementedError("VBGP.value_and_grad: the gradient of the VB objective is not provided")
+        """params -> (objective_VB, gradient pytree shaped like params) through the
+        implicit layer (the adjoint fixed point over f_VB)."""
+
+        def vg(parameters):
+            import torch
+
+            leaves = tree_map(_to_leaf_tensor, parameters)
+            theta, key = self._theta(leaves)
+            gp = self._handle(key)
+            X, y = self._device_data()
+            td = self._theta_dev(theta)
+            out = torch.empty(1 + td.numel(), dtype=torch.float32, device=td.device)
+            N.check(gp.lib.pgb_vb_value_and_grad(gp.h, X.data_ptr(), y.data_ptr(), td.data_ptr(),
+                                                 out.data_ptr(), out[1:].data_ptr(), stream_handle(td.device)),
+                    "pgb_vb_value_and_grad")
+            host = out.cpu().numpy().astype(np.float64)
+            self._after(gp, "value_and_grad")
+            if theta.requires_grad:
+                theta.backward(torch.from_numpy(host[1:]))
+            return float(host[0]), _zip_grads(leaves, parameters)
+
+        return vg
 
     def weight(self, parameters):
         """VB fixed point w* from w = 0 (``VBGP.weight``)."""

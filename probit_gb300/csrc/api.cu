@@ -52,10 +52,11 @@ namespace {
 
 enum GraphOp {
   OP_WEIGHT = 0, OP_POSTERIOR = 1, OP_OBJECTIVE = 2, OP_VG = 3,   // Laplace
-  OP_VB_WEIGHT = 4, OP_VB_OBJECTIVE = 5,                         // Variational Bayes
-  OP_COUNT = 6
+  OP_VB_WEIGHT = 4, OP_VB_OBJECTIVE = 5, OP_VB_VG = 6,          // Variational Bayes
+  OP_COUNT = 7
 };
-bool is_vb(int op) { return op == OP_VB_WEIGHT || op == OP_VB_OBJECTIVE; }
+bool is_vb(int op) { return op == OP_VB_WEIGHT || op == OP_VB_OBJECTIVE || op == OP_VB_VG; }
+bool needs_grad_buffers(int op) { return op == OP_VG || op == OP_VB_VG; }
 enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_COUNT = 4 };
 enum Counter { C_DAG = 0, C_TRSV_T = 1, C_PREDICT = 2, C_TRSV_L = 3, C_SYRK = 4, C_COUNT = 8 };
 
@@ -701,16 +702,55 @@ void enq_prologue(Engine& e, int op, cudaStream_t s) {
   }
 }
 
+// VB objective at the fixed point: f = K w, log p, d1, d2 at f, and the
+// objective sum_i [-log p_i + f_i w_i / 2 + log L_ii] (its trace terms
+// cancel exactly); zbar = K (w - d1) for the adjoint; the adjoint loop state.
+void enq_vb_value(Engine& e, cudaStream_t s) {
+  launch_activate_enabled(e.probs, e.nprob, s);
+  enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);
+  launch_vb_post(e.probs, e.vmap, e.nvb, s);
+  launch_evidence(e.probs, e.vmap, e.nvb, e.nprob, s);
+}
+
+// Between the VB fixed point and its adjoint loop (OP_VB_VG).
+void enq_vb_mid(Engine& e, cudaStream_t s) {
+  enq_vb_value(e, s);
+  enq_matvec(e, MatvecOp{F_RV, F_NONE, F_ZBAR, 0, 1}, s);   // zbar = K (w - d1)
+  launch_vb_adj_reset(e.probs, e.nprob, s);
+}
+
+// One step of the adjoint fixed point u <- K (I + sigma D2) A^-1 u + zbar.
+void enq_vb_adj_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
+  cudaMemsetAsync(e.tflags_all, 0, sizeof(int) * e.tflags_words, s);
+  cudaMemsetAsync(e.counters + C_TRSV_T, 0, sizeof(int) * 3, s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 0, e.counters + C_TRSV_L, 1, 1, trsv_grid(e), s);
+  launch_trsv(e.probs, e.claims, e.nclaims, 1, e.counters + C_TRSV_T, 0, 1, trsv_grid(e), s);
+  launch_vb_adj_scale(e.probs, e.vmap, e.nvb, s);
+  enq_matvec(e, MatvecOp{F_TZ, F_NONE, F_Y2, 0, 1}, s);
+  launch_vb_adj_update(e.probs, e.vmap, e.nvb, s);
+  launch_vb_adj_finalize(e.probs, e.nprob, e.any_active, h, use_cond, s);
+}
+
 void enq_epilogue(Engine& e, int op, cudaStream_t s) {
   if (op == OP_VB_OBJECTIVE) {
+    enq_vb_value(e, s);
+    return;
+  }
+  if (op == OP_VB_VG) {
+    // v = A^-1 u for the converged u (t = u), then the gradient: the prior
+    // trace with R = sw B^-1 sw = A^-1 and c = w/2 - d1 + sigma v d2, and the
+    // likelihood-parameter sums
     launch_activate_enabled(e.probs, e.nprob, s);
-    enq_matvec(e, MatvecOp{F_A, F_NONE, F_F, 0, 1}, s);       // f = K w
-    launch_vb_terms(e.probs, e.vmap, e.nvb, s);              // log p(f)
-    enq_dag(e, JOB_IDENT, s);                                // L^-T on the resident factor
+    cudaMemsetAsync(e.tflags_all, 0, sizeof(int) * e.tflags_words, s);
+    cudaMemsetAsync(e.counters + C_TRSV_T, 0, sizeof(int) * 3, s);
+    launch_trsv(e.probs, e.claims, e.nclaims, 0, e.counters + C_TRSV_L, 1, 1, trsv_grid(e), s);
+    launch_trsv(e.probs, e.claims, e.nclaims, 1, e.counters + C_TRSV_T, 0, 1, trsv_grid(e), s);
+    launch_vb_grad_vec(e.probs, e.vmap, e.nvb, s);
+    enq_dag(e, JOB_IDENT, s);   // L^-T on the resident factor
     cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
     launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);   // B^-1
-    enq_matvec(e, MatvecOp{F_SW, F_NONE, F_ROWDOT, 1, 1}, s);   // rowdot_i = sum_j B^-1_ij K_ij / sigma
-    launch_vb_evidence(e.probs, e.vmap, e.nvb, e.nprob, s);
+    for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), s);
+    launch_vb_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
     return;
   }
   if (op >= OP_POSTERIOR && !is_vb(op)) {
@@ -728,7 +768,7 @@ void enq_epilogue(Engine& e, int op, cudaStream_t s) {
 // driven from the host (one flag read per step).  For profilers that do not
 // follow kernels inside conditional graph nodes.
 int run_eager(Engine& e, int op, cudaStream_t s) {
-  if (op == OP_VG || op == OP_VB_OBJECTIVE) PGB_TRY(ensure_grad_buffers(e));
+  if (needs_grad_buffers(op)) PGB_TRY(ensure_grad_buffers(e));
   enq_prologue(e, op, s);
   const char* tv = std::getenv("PGB_TRACE");
   const bool trace = tv && tv[0] == '1';
@@ -744,20 +784,26 @@ int run_eager(Engine& e, int op, cudaStream_t s) {
     if (trace) std::fprintf(stderr, "probit_gb300: newton %d ||delta||[0]=%.6g\n", it + 1, err);
     if (!again) break;
   }
+  if (op == OP_VB_VG) {
+    enq_vb_mid(e, s);
+    for (int it = 0; it < maxiter; ++it) {
+      enq_vb_adj_step(e, s, 0, 0);
+      int again = 0;
+      CU_TRY(cudaMemcpyAsync(&again, e.any_active + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CU_TRY(cudaStreamSynchronize(s));
+      if (!again) break;
+    }
+  }
   enq_epilogue(e, op, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
 }
 
-// Capture the graph of one operation.
-int build_graph(Engine& e, int op) {
-  if (e.gexec[op]) return PGB_OK;
-  if (op == OP_VG || op == OP_VB_OBJECTIVE) PGB_TRY(ensure_grad_buffers(e));
-  cudaStream_t s = e.cap_s, s2 = e.cap_s2;
-  cudaGraph_t g = nullptr;
-  CU_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
-  enq_prologue(e, op, s);
-  // WHILE node for the Newton loop
+// Add a WHILE node at the current point of the capture on s whose body is
+// captured on s2 by `body(s2, handle)`; the body's last kernel sets the
+// condition (the loop runs at least once).
+template <class Body>
+int capture_while(cudaStream_t s, cudaStream_t s2, Body body) {
   cudaStreamCaptureStatus cs;
   cudaGraph_t cg = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -772,12 +818,31 @@ int build_graph(Engine& e, int op) {
   cp.conditional.size = 1;
   cudaGraphNode_t cnode;
   CU_TRY(cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp));
-  cudaGraph_t body = cp.conditional.phGraph_out[0];
+  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
   CU_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-  CU_TRY(cudaStreamBeginCaptureToGraph(s2, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  enq_step(e, op, s2, h, 1);
+  CU_TRY(cudaStreamBeginCaptureToGraph(s2, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  body(s2, h);
   cudaGraph_t body_out = nullptr;
   CU_TRY(cudaStreamEndCapture(s2, &body_out));
+  return PGB_OK;
+}
+
+// Capture the graph of one operation.
+int build_graph(Engine& e, int op) {
+  if (e.gexec[op]) return PGB_OK;
+  if (needs_grad_buffers(op)) PGB_TRY(ensure_grad_buffers(e));
+  cudaStream_t s = e.cap_s, s2 = e.cap_s2;
+  cudaGraph_t g = nullptr;
+  CU_TRY(cudaStreamBeginCapture(s, cudaStreamCaptureModeRelaxed));
+  enq_prologue(e, op, s);
+  // WHILE node for the fixed-point loop (Newton or VB)
+  PGB_TRY(capture_while(s, s2, [&](cudaStream_t bs, cudaGraphConditionalHandle h) { enq_step(e, op, bs, h, 1); }));
+  if (op == OP_VB_VG) {
+    enq_vb_mid(e, s);
+    PGB_TRY(capture_while(s, s2, [&](cudaStream_t bs, cudaGraphConditionalHandle h) {
+      enq_vb_adj_step(e, bs, h, 1);
+    }));
+  }
   enq_epilogue(e, op, s);
   CU_TRY(cudaStreamEndCapture(s, &g));
   CU_TRY(cudaGraphInstantiate(&e.gexec[op], g, 0));
@@ -964,6 +1029,19 @@ int pgb_vb_objective(pgb_gp* gp, const float* X, const void* y, const float* the
   PGB_TRY(run_op(e, OP_VB_OBJECTIVE, s));
   gp->factor_valid = 0;
   CU_TRY(cudaMemcpyAsync(value_out, e.value_all, sizeof(float), cudaMemcpyDeviceToDevice, s));
+  return PGB_OK;
+}
+
+int pgb_vb_value_and_grad(pgb_gp* gp, const float* X, const void* y, const float* theta, float* value_out,
+                          float* grad_out, void* stream) {
+  if (!gp || !value_out || !grad_out || !y) return PGB_EINVAL;
+  cudaStream_t s = (cudaStream_t)stream;
+  Engine& e = gp->e;
+  PGB_TRY(ingest(e, X, y, theta, s));
+  PGB_TRY(run_op(e, OP_VB_VG, s));
+  gp->factor_valid = 0;
+  CU_TRY(cudaMemcpyAsync(value_out, e.value_all, sizeof(float), cudaMemcpyDeviceToDevice, s));
+  CU_TRY(cudaMemcpyAsync(grad_out, e.grad_all, sizeof(float) * e.th_total, cudaMemcpyDeviceToDevice, s));
   return PGB_OK;
 }
 

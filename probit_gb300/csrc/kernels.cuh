@@ -150,8 +150,14 @@ void launch_vb_setup(const Prob* probs, const int2* vmap, int nblocks, cudaStrea
 void launch_vb_mark(const Prob* probs, int nprob, cudaStream_t st);
 void launch_vb_rhs(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_vb_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
-void launch_vb_terms(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
-void launch_vb_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
+void launch_vb_post(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_adj_reset(const Prob* probs, int nprob, cudaStream_t st);
+void launch_vb_adj_scale(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_adj_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_adj_finalize(const Prob* probs, int nprob, int* any_active, cudaGraphConditionalHandle cond,
+                            int use_cond, cudaStream_t st);
+void launch_vb_grad_vec(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
+void launch_vb_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_grad_vec1(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_scale_tz(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);
 void launch_grad_vec3(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st);

@@ -266,151 +266,6 @@ void launch_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob
   evidence_sum_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob);
 }
 
-// ---------------------------------------------------------------- Variational Bayes
-// VBGP (approximators.py:280-339) with the maps of implicit/VB.py:
-//   f_VB(w) = (sigma^2 I + K)^-1 (K w + sigma d log p(K w))        (VB.py:4-17)
-// iterated by fwd_solver from w = 0 (approximators.py:332-334), and
-//   objective_VB = 1/2 sum(K o cov) + 1/2 sigma^2 tr(cov) + 1/2 (K w)^T w
-//                  - N log sigma - 1/2 log det cov - N/2 - sum log p(K w)
-// with cov = (sigma^2 I + K)^-1 (VB.py:20-40).  With B = I + K / sigma^2
-// (the B of this library at W = 1 / sigma^2) and L L^T = B:
-//   (sigma^2 I + K)^-1 v = B^-1 v / sigma^2,  log det cov = -2 (N log sigma + sum log L_ii),
-// so objective_VB = sum_i [1/2 rowdot_i / sigma + 1/2 (B^-1)_ii + 1/2 f_i w_i
-//                          + log L_ii - 1/2 - log p_i]
-// where rowdot_i = sum_j (B^-1)_ij K_ij sw_j, sw = 1 / sigma.
-
-// sw = 1 / sigma, W = 1 / sigma^2 on the data points (0 on the padding)
-__global__ void vb_setup_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
-  const int2 m = vmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (*P.active == 0) return;
-  const int i = m.y * VT + threadIdx.x;
-  if (i >= P.n_pad) return;
-  const float sig = theta_sigma(P.sh, P.theta);
-  const bool in = i < P.sh.n;
-  P.sw[i] = in ? 1.0f / sig : 0.0f;
-  P.W[i] = in ? 1.0f / (sig * sig) : 0.0f;
-  P.sw_prev[i] = P.sw[i];
-}
-
-void launch_vb_setup(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
-  if (nblocks > 0) vb_setup_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-}
-
-// After the factorisation of B: the resident factor serves every step.
-__global__ void vb_mark_kernel(const Prob* __restrict__ probs, int nprob) {
-  const int p = blockIdx.x * blockDim.x + threadIdx.x;
-  if (p >= nprob) return;
-  const Prob& P = probs[p];
-  if (*P.active == 0) return;
-  const int ok = P.status[ST_CODE] == 0 ? 1 : 0;
-  P.reuse[0] = ok;
-  P.reuse[2] = ok;
-}
-
-void launch_vb_mark(const Prob* probs, int nprob, cudaStream_t st) {
-  vb_mark_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
-}
-
-// t = f + sigma d log p(f) (padding 0): the right-hand side of one step
-__global__ void vb_rhs_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
-  const int2 m = vmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (*P.active == 0) return;
-  const int i = m.y * VT + threadIdx.x;
-  if (i >= P.n_pad) return;
-  if (i >= P.sh.n) {
-    P.d1[i] = 0.0f;
-    P.t[i] = 0.0f;
-    return;
-  }
-  const Shape sh = P.sh;
-  int yi;
-  const float yv = load_y(sh, P.y, i, &yi);
-  const float sig = theta_sigma(sh, P.theta);
-  LikOut o;
-  lik_point<false>(sh.lik, P.f[i], yv, yi, sig, theta_cutpoints(sh, P.theta), o);
-  P.d1[i] = o.d1;
-  P.t[i] = P.f[i] + sig * o.d1;
-}
-
-void launch_vb_rhs(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
-  if (nblocks > 0) vb_rhs_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-}
-
-// w_new = (B^-1 t) / sigma^2 (x holds B^-1 t); block partial of ||w_new - w||^2;
-// da = w_new - w (f follows w by f += K da)
-__global__ void vb_update_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
-  __shared__ double sred[VT / 32];
-  const int2 m = vmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (*P.active == 0) return;   // uniform per block
-  const int i = m.y * VT + threadIdx.x;
-  float e = 0.0f;
-  if (i < P.sh.n) {
-    const float sig = theta_sigma(P.sh, P.theta);
-    const float ai = P.a[i];
-    const float an = P.x[i] / (sig * sig);
-    const float dlt = an - ai;
-    e = dlt * dlt;
-    P.a[i] = an;
-    P.da[i] = dlt;
-  } else if (i < P.n_pad) {
-    P.da[i] = 0.0f;
-  }
-  const double s = block_sum_d<VT>(e, sred);
-  if (threadIdx.x == 0) P.part[m.y] = s;
-}
-
-void launch_vb_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
-  if (nblocks > 0) vb_update_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-}
-
-// log p at the final f = K w
-__global__ void vb_terms_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
-  const int2 m = vmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (*P.active == 0) return;
-  const int i = m.y * VT + threadIdx.x;
-  if (i >= P.n_pad) return;
-  if (i >= P.sh.n) {
-    P.logp[i] = 0.0f;
-    return;
-  }
-  const Shape sh = P.sh;
-  int yi;
-  const float yv = load_y(sh, P.y, i, &yi);
-  LikOut o;
-  lik_point<false>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
-  P.logp[i] = o.logp;
-}
-
-void launch_vb_terms(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
-  if (nblocks > 0) vb_terms_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-}
-
-__global__ void vb_evidence_partial_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
-  __shared__ double sred[VT / 32];
-  const int2 m = vmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (*P.active == 0) return;
-  const int i = m.y * VT + threadIdx.x;
-  float v = 0.0f;
-  if (i < P.sh.n) {
-    const float sig = theta_sigma(P.sh, P.theta);
-    v = 0.5f * P.rowdot[i] / sig + 0.5f * __ldcg(P.Binv + (size_t)i * P.ld + i) + 0.5f * P.f[i] * P.a[i] +
-        logf(__ldcg(P.L + (size_t)i * P.ld + i)) - 0.5f - P.logp[i];
-  }
-  const double s = block_sum_d<VT>(v, sred);
-  if (threadIdx.x == 0) P.part[m.y] = s;
-}
-
-void launch_vb_evidence(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
-  if (nblocks <= 0) return;
-  vb_evidence_partial_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
-  evidence_sum_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob);
-}
-
 // ---------------------------------------------------------------- gradient
 // s = 1/2 diag(Sigma) d3 with diag(Sigma)_i = rowdot_i / sw_i
 // (rowdot_i = sum_j B^-1_ij sw_j K_ji, i.e. Sigma = W^-1/2 B^-1 W^1/2 K),
@@ -556,6 +411,295 @@ __global__ void __launch_bounds__(FINAL_THREADS) grad_final_kernel(const Prob* _
 void launch_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
   if (nblocks <= 0) return;
   grad_lik_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+  grad_final_kernel<<<nprob, FINAL_THREADS, 0, st>>>(probs);
+}
+
+// ---------------------------------------------------------------- Variational Bayes
+// VBGP (approximators.py:280-339) with the maps of implicit/VB.py:
+//   f_VB(w) = (sigma^2 I + K)^-1 (K w + sigma d log p(K w))        (VB.py:4-17)
+// iterated by fwd_solver from w = 0 (approximators.py:332-334), and
+//   objective_VB = 1/2 sum(K o cov) + 1/2 sigma^2 tr(cov) + 1/2 (K w)^T w
+//                  - N log sigma - 1/2 log det cov - N/2 - sum log p(K w)
+// with cov = (sigma^2 I + K)^-1 (VB.py:20-40).  With B = I + K / sigma^2
+// (the B of this library at W = 1 / sigma^2) and L L^T = B:
+//   (sigma^2 I + K)^-1 v = B^-1 v / sigma^2,  log det cov = -2 (N log sigma + sum log L_ii),
+// so objective_VB = sum_i [1/2 rowdot_i / sigma + 1/2 (B^-1)_ii + 1/2 f_i w_i
+//                          + log L_ii - 1/2 - log p_i]
+// where rowdot_i = sum_j (B^-1)_ij K_ij sw_j, sw = 1 / sigma.
+
+// sw = 1 / sigma, W = 1 / sigma^2 on the data points (0 on the padding)
+__global__ void vb_setup_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  const float sig = theta_sigma(P.sh, P.theta);
+  const bool in = i < P.sh.n;
+  P.sw[i] = in ? 1.0f / sig : 0.0f;
+  P.W[i] = in ? 1.0f / (sig * sig) : 0.0f;
+  P.sw_prev[i] = P.sw[i];
+}
+
+void launch_vb_setup(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_setup_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// After the factorisation of B: the resident factor serves every step.
+__global__ void vb_mark_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  if (*P.active == 0) return;
+  const int ok = P.status[ST_CODE] == 0 ? 1 : 0;
+  P.reuse[0] = ok;
+  P.reuse[2] = ok;
+}
+
+void launch_vb_mark(const Prob* probs, int nprob, cudaStream_t st) {
+  vb_mark_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
+}
+
+// t = f + sigma d log p(f) (padding 0): the right-hand side of one step
+__global__ void vb_rhs_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.d1[i] = 0.0f;
+    P.t[i] = 0.0f;
+    return;
+  }
+  const Shape sh = P.sh;
+  int yi;
+  const float yv = load_y(sh, P.y, i, &yi);
+  const float sig = theta_sigma(sh, P.theta);
+  LikOut o;
+  lik_point<false>(sh.lik, P.f[i], yv, yi, sig, theta_cutpoints(sh, P.theta), o);
+  P.d1[i] = o.d1;
+  P.t[i] = P.f[i] + sig * o.d1;
+}
+
+void launch_vb_rhs(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_rhs_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// w_new = (B^-1 t) / sigma^2 (x holds B^-1 t); block partial of ||w_new - w||^2;
+// da = w_new - w (f follows w by f += K da)
+__global__ void vb_update_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sred[VT / 32];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;   // uniform per block
+  const int i = m.y * VT + threadIdx.x;
+  float e = 0.0f;
+  if (i < P.sh.n) {
+    const float sig = theta_sigma(P.sh, P.theta);
+    const float ai = P.a[i];
+    const float an = P.x[i] / (sig * sig);
+    const float dlt = an - ai;
+    e = dlt * dlt;
+    P.a[i] = an;
+    P.da[i] = dlt;
+  } else if (i < P.n_pad) {
+    P.da[i] = 0.0f;
+  }
+  const double s = block_sum_d<VT>(e, sred);
+  if (threadIdx.x == 0) P.part[m.y] = s;
+}
+
+void launch_vb_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_update_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// After the fixed point, at f = K w: log p, d1 and d2 (kept in dsig), rv =
+// w - d1 (zbar = K rv is d objective / d w), and u = t = 0 for the adjoint.
+// The objective is then the Laplace-form sum over -log p + f w / 2 + log L_ii
+// (launch_evidence): the two trace terms of objective_VB add up to
+// tr((K + sigma^2 I) cov) / 2 = N / 2, which cancels its -N / 2.
+__global__ void vb_post_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  P.u[i] = 0.0f;
+  P.t[i] = 0.0f;
+  if (i >= P.sh.n) {
+    P.logp[i] = 0.0f; P.d1[i] = 0.0f; P.dsig[i] = 0.0f; P.rv[i] = 0.0f;
+    return;
+  }
+  const Shape sh = P.sh;
+  int yi;
+  const float yv = load_y(sh, P.y, i, &yi);
+  LikOut o;
+  lik_point<false>(sh.lik, P.f[i], yv, yi, theta_sigma(sh, P.theta), theta_cutpoints(sh, P.theta), o);
+  P.logp[i] = o.logp;
+  P.d1[i] = o.d1;
+  P.dsig[i] = o.d2;
+  P.rv[i] = P.a[i] - o.d1;
+}
+
+void launch_vb_post(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_post_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// ---- the adjoint of fixed_point_layer_bwd (implicit/solvers.py:52-64) for f_VB:
+// u <- K (I + sigma D2) A^-1 u + zbar, A = sigma^2 I + K, from u = 0, with
+// fwd_solver's stopping rule; reuse[3] counts its steps.
+__global__ void vb_adj_reset_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  *P.active = *P.enabled != 0 ? 1 : 0;
+  P.reuse[3] = 0;
+}
+
+void launch_vb_adj_reset(const Prob* probs, int nprob, cudaStream_t st) {
+  vb_adj_reset_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
+}
+
+// tz = (1 + sigma d2) x / sigma^2, x = B^-1 u (so tz = (I + sigma D2) A^-1 u)
+__global__ void vb_adj_scale_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  const float sig = theta_sigma(P.sh, P.theta);
+  P.tz[i] = i < P.sh.n ? (1.0f + sig * P.dsig[i]) * P.x[i] / (sig * sig) : 0.0f;
+}
+
+void launch_vb_adj_scale(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_adj_scale_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// u_new = K tz + zbar (y2 = K tz); block partial of ||u_new - u||^2; u = t = u_new
+__global__ void vb_adj_update_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sred[VT / 32];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;   // uniform per block
+  const int i = m.y * VT + threadIdx.x;
+  float e = 0.0f;
+  if (i < P.sh.n) {
+    const float un = P.y2[i] + P.zbar[i];
+    const float dlt = un - P.u[i];
+    e = dlt * dlt;
+    P.u[i] = un;
+    P.t[i] = un;
+  }
+  const double s = block_sum_d<VT>(e, sred);
+  if (threadIdx.x == 0) P.part[m.y] = s;
+}
+
+void launch_vb_adj_update(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_adj_update_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+__global__ void vb_adj_finalize_kernel(const Prob* __restrict__ probs, int nprob, int* __restrict__ any_active) {
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  if (w >= nprob) return;
+  const Prob& P = probs[w];
+  if (*P.active == 0) return;
+  const int nparts = ceil_div(P.n_pad, VT);
+  double s = 0.0;
+  for (int k = lane; k < nparts; k += 32) s += P.part[k];
+  s = warp_sum_d(s);
+  if (lane == 0) {
+    const float err = (float)sqrt(s);
+    const int it = P.reuse[3] + 1;
+    P.reuse[3] = it;
+    if (err != err) atomicCAS(P.status + ST_CODE, 0, PGB_ENAN);
+    const bool again = (err > P.tol) && (it < P.maxiter) && (P.status[ST_ABORT] == 0);
+    *P.active = again ? 1 : 0;
+    if (again) atomicOr(any_active, 1);
+  }
+}
+
+void launch_vb_adj_finalize(const Prob* probs, int nprob, int* any_active, cudaGraphConditionalHandle cond,
+                            int use_cond, cudaStream_t st) {
+  vb_adj_finalize_kernel<<<ceil_div(nprob, 8), 256, 0, st>>>(probs, nprob, any_active);
+  newton_cond_kernel<<<1, 1, 0, st>>>(any_active, cond, use_cond);
+}
+
+// v = A^-1 u = x / sigma^2 (x = B^-1 u), kept in y2; c = w/2 - d1 + sigma v d2,
+// the vector of the prior trace sum_ij (A^-1 / 2 + c w^T)_ij dK_ij
+__global__ void vb_grad_vec_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const int i = m.y * VT + threadIdx.x;
+  if (i >= P.n_pad) return;
+  if (i >= P.sh.n) {
+    P.y2[i] = 0.0f;
+    P.c[i] = 0.0f;
+    return;
+  }
+  const float sig = theta_sigma(P.sh, P.theta);
+  const float v = P.x[i] / (sig * sig);
+  P.y2[i] = v;
+  P.c[i] = 0.5f * P.a[i] - P.d1[i] + sig * v * P.dsig[i];
+}
+
+void launch_vb_grad_vec(const Prob* probs, const int2* vmap, int nblocks, cudaStream_t st) {
+  if (nblocks > 0) vb_grad_vec_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
+}
+
+// Per point, the likelihood-parameter part of the VB gradient (slots as in
+// grad_lik_kernel):
+//   sigma : ((B^-1)_ii - 1) / sigma - dlogp/dsigma + v (d1 + sigma dd1/dsigma - 2 sigma w)
+//   b     : -dlogp/db + sigma v dd1/db
+__global__ void vb_grad_lik_kernel(const Prob* __restrict__ probs, const int2* __restrict__ vmap) {
+  __shared__ double sacc[VT / 32][MAX_LIK_SLOTS];
+  const int2 m = vmap[blockIdx.x];
+  const Prob& P = probs[m.x];
+  if (*P.active == 0) return;
+  const Shape sh = P.sh;
+  const int nslots = 1 + (sh.lik == PGB_LIK_GAUSSIAN ? 0 : sh.J + 1);
+  const int i = m.y * VT + threadIdx.x;
+  float gs = 0.0f, glo = 0.0f, ghi = 0.0f;
+  int ylo = -1;
+  if (i < sh.n) {
+    int yi;
+    const float yv = load_y(sh, P.y, i, &yi);
+    const float sig = theta_sigma(sh, P.theta);
+    LikOut o;
+    lik_point<true>(sh.lik, P.f[i], yv, yi, sig, theta_cutpoints(sh, P.theta), o);
+    const float v = P.y2[i];
+    const float bii = __ldcg(P.Binv + (size_t)i * P.ld + i);
+    gs = (bii - 1.0f) / sig - o.lp_s + v * (o.d1 + sig * o.d1_s - 2.0f * sig * P.a[i]);
+    if (sh.lik != PGB_LIK_GAUSSIAN) {
+      glo = -o.lp_lo + sig * v * o.d1_lo;
+      ghi = -o.lp_hi + sig * v * o.d1_hi;
+      ylo = o.ylo;
+    }
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const double s = warp_sum_d((double)gs);
+  if (lane == 0) sacc[warp][0] = s;
+  if (sh.lik != PGB_LIK_GAUSSIAN) {
+    for (int cls = 0; cls <= sh.J; ++cls) {
+      double v = 0.0;
+      if (ylo == cls) v += glo;
+      if (ylo >= 0 && ylo + 1 == cls) v += ghi;
+      v = warp_sum_d(v);
+      if (lane == 0) sacc[warp][1 + cls] = v;
+    }
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < nslots; k += VT) {
+    double t = 0.0;
+    for (int w = 0; w < VT / 32; ++w) t += sacc[w][k];
+    P.lpart[(size_t)m.y * nslots + k] = t;
+  }
+}
+
+void launch_vb_grad_lik_final(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st) {
+  if (nblocks <= 0) return;
+  vb_grad_lik_kernel<<<nblocks, VT, 0, st>>>(probs, vmap);
   grad_final_kernel<<<nprob, FINAL_THREADS, 0, st>>>(probs);
 }
 

@@ -1,8 +1,9 @@
-"""VBGP through the C-ABI (pgb_vb_weight, pgb_vb_objective) against the
-float64 oracle restatement of VBGP (approximators.py:280-339, implicit/VB.py):
-the fixed point to 1e-3 of its largest entry, the objective to 1e-4 relative,
-the iteration count within 2 of the oracle's, and predictions with the VB
-precision 1 / sigma^2 against the oracle's Approximator.predict."""
+"""VBGP through the C-ABI (pgb_vb_weight, pgb_vb_objective,
+pgb_vb_value_and_grad) against the float64 oracle restatement of VBGP
+(approximators.py:280-339, implicit/VB.py): the fixed point to 1e-3 of its
+largest entry, the objective to 1e-4 relative, the iteration count within 2
+of the oracle's, the gradient to 1e-3 of its largest entry, and predictions
+with the VB precision 1 / sigma^2 against the oracle's Approximator.predict."""
 
 import math
 
@@ -38,6 +39,21 @@ def test_vb_weight_and_objective(cuda_device, seed, N, D, J, kind):
     v = gp.objective()(params)
     v64 = L.vb_objective(op, p.theta(), w64)
     assert abs(v - v64) <= 1e-4 * abs(v64), (v, v64)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("seed,N,D,J,kind", CASES)
+def test_vb_value_and_grad(cuda_device, seed, N, D, J, kind):
+    p, op, gp = _setup(seed, N, D, J, kind)
+    params = p.params()
+    v, g = gp.value_and_grad()(params)
+    from probit_gb300.approximators import tree_leaves
+
+    gf = np.concatenate([np.atleast_1d(np.asarray(x, np.float64)) for x in tree_leaves(g)])
+    v64, g64, _, _ = L.vb_value_and_grad(op, p.theta(), tol=TOL)
+    assert abs(v - v64) <= 1e-4 * abs(v64), (v, v64)
+    assert np.abs(gf - g64).max() <= 1e-3 * np.abs(g64).max(), (gf, g64)
+    assert abs(gp.objective()(params) - v) <= 1e-6 * abs(v)
 
 
 @pytest.mark.gpu

@@ -49,3 +49,27 @@ def test_vb_float32_close_to_float64():
     o64 = L.vb_objective(op, th, w64)
     o32 = L.vb_objective(op, th, w32, dtype=np.float32)
     assert abs(o32 - o64) <= 1e-4 * abs(o64)
+
+
+@pytest.mark.parametrize("seed,N,D,J,kind", CASES)
+def test_vb_gradient_matches_finite_differences(seed, N, D, J, kind):
+    """The oracle's implicit-layer VB gradient (adjoint fixed point over f_VB)
+    against central differences of objective_VB(theta, w*(theta)), float64."""
+    op, th = _problem(seed, N, D, J, kind)
+    th = th.astype(np.float64)
+    _, g, _, _ = L.vb_value_and_grad(op, th, tol=1e-13, maxiter=5000)
+
+    def F(t):
+        w, _ = L.vb_weight(op, t, tol=1e-13, maxiter=5000)
+        return L.vb_objective(op, t, w)
+
+    for k in range(th.size):
+        if not np.isfinite(th[k]):
+            assert g[k] == 0.0
+            continue
+        h = 1e-5 * max(1.0, abs(th[k]))
+        tp, tm = th.copy(), th.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd = (F(tp) - F(tm)) / (2 * h)
+        assert abs(g[k] - fd) <= 1e-6 * max(1.0, abs(fd)), (k, g[k], fd)
