@@ -142,7 +142,7 @@ class _Model:
 class Server:
     """Continuous-batching request server on the current CUDA device."""
 
-    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4):
+    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True):
         import torch
 
         self.torch = torch
@@ -153,6 +153,10 @@ class Server:
         self.used = 0
         self.small_n = small_n
         self.large_blocks = large_blocks   # SM share of the launches of a problem with n > small_n
+        # after the first fit of a small model, its evidence + gradient handle is
+        # created and its graph captured (one evaluation at the fitted
+        # hyperparameters) before the model is released, so no request pays it
+        self.warm_small = warm_small
         self.models: dict[int, _Model] = {}
         self.evicted = set()
         self.lock = threading.Condition()
@@ -320,12 +324,32 @@ class Server:
             except Exception as exc:   # reported per request
                 req.error = repr(exc)
             req.done = self.now()
+            warm = (self.warm_small and req.kind == "fit" and req.error is None and m.hvg is None
+                    and m.problem.n <= self.small_n)
             with self.lock:
-                m.busy = False
-                m.last_used = req.done
+                if warm:   # account the handle first; skip the warm-up if it does not fit
+                    grow = m.footprint(True, True, m.cap_m) - m.bytes
+                    warm = self.used + grow <= self.budget
+                    if warm:
+                        self.used += grow
+                        m.bytes += grow
+                if not warm:
+                    m.busy = False
+                    m.last_used = req.done
                 if req.kind == "predict" and req.error is None:
                     m.cap_m = max(m.cap_m, -(-req.Xs.shape[0] // 128) * 128)
                 self.lock.notify_all()
+            if warm:
+                try:
+                    with torch.cuda.stream(stream):
+                        self._warm_vg(m, stream)
+                    stream.synchronize()
+                except Exception:   # the first request on the model creates it instead
+                    pass
+                with self.lock:
+                    m.busy = False
+                    m.last_used = self.now()
+                    self.lock.notify_all()
 
     def _upload(self, m):
         torch = self.torch
@@ -341,6 +365,19 @@ class Server:
         if p.n > self.small_n and self.large_blocks:
             N.check(self.lib.pgb_gp_set_max_blocks(h, self.large_blocks), "pgb_gp_set_max_blocks")
         return h
+
+    def _warm_vg(self, m, stream):
+        """Create the model's evidence + gradient handle and capture its graph
+        (one evaluation at the fitted hyperparameters; the result is dropped)."""
+        torch = self.torch
+        p = m.problem
+        if m.hvg is None:
+            m.hvg = self._create(p)
+        d = m.dev
+        theta = torch.from_numpy(np.asarray(p.theta, np.float32)).to(self.device, non_blocking=True)
+        out = torch.empty(1 + theta.numel(), dtype=torch.float32, device=self.device)
+        N.check(self.lib.pgb_value_and_grad(m.hvg, d["X"].data_ptr(), d["y"].data_ptr(), theta.data_ptr(),
+                                            out.data_ptr(), out[1:].data_ptr(), stream.cuda_stream), "warm-up")
 
     def _run(self, req, m, stream):
         torch = self.torch
