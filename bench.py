@@ -20,6 +20,7 @@ runs an independent replica ("scaling": "weak"); value = total solves/s.
 from __future__ import annotations
 
 import argparse
+import gc
 import json
 import math
 import os
@@ -471,12 +472,18 @@ def run_serving(args, dev):
     for tag, rate, dur, seed in (("offered_2000_per_s", 2000.0, args.serve_seconds, 4),
                                  ("offered_150_per_s", 150.0, max(5.0, args.serve_seconds), 5)):
         probs, reqs = Wk.serving_c4(rate=rate, duration=dur, pool=256, seed=seed, device=dev)
+        gc.collect()   # the previous run's objects are not collected during this one
         srv = S.Server(workers=args.serve_workers)
         try:
             t0 = time.perf_counter()
             srv.replay([S.Request(0.0, "fit", k, p) for k, p in enumerate(probs)], realtime=False)
             prefit = time.perf_counter() - t0
-            done = srv.replay(reqs, realtime=True)
+            gc.collect()
+            gc.freeze()    # objects alive now are never scanned by a collection during the replay
+            try:
+                done = srv.replay(reqs, realtime=True)
+            finally:
+                gc.unfreeze()
             summ = S.latency_summary(done)
             summ.update({"rate_req_s": rate, "window_s": dur, "requests": len(reqs), "prefit_s": prefit,
                          "evictions": srv.evictions})
