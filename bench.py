@@ -477,6 +477,7 @@ def run_serving(args, dev):
         try:
             t0 = time.perf_counter()
             srv.replay([S.Request(0.0, "fit", k, p) for k, p in enumerate(probs)], realtime=False)
+            srv.wait_idle()   # warm-ups of the fitted models finish before the arrivals start
             prefit = time.perf_counter() - t0
             gc.collect()
             gc.freeze()    # objects alive now are never scanned by a collection during the replay

@@ -142,7 +142,8 @@ class _Model:
 class Server:
     """Continuous-batching request server on the current CUDA device."""
 
-    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True):
+    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True,
+                 warm_rows=4096):
         import torch
 
         self.torch = torch
@@ -155,8 +156,12 @@ class Server:
         self.large_blocks = large_blocks   # SM share of the launches of a problem with n > small_n
         # after the first fit of a small model, its evidence + gradient handle is
         # created and its graph captured (one evaluation at the fitted
-        # hyperparameters) before the model is released, so no request pays it
+        # hyperparameters) and its predict workspace sized for `warm_rows`
+        # test points (one prediction) before the model is released, so no
+        # request pays a first-use graph build or workspace allocation
         self.warm_small = warm_small
+        self.warm_rows = int(warm_rows)
+        self.busy_workers = 0
         self.models: dict[int, _Model] = {}
         self.evicted = set()
         self.lock = threading.Condition()
@@ -313,6 +318,7 @@ class Server:
                         return
                     got = self._take(role)
                     if got is not None:
+                        self.busy_workers += 1   # counted before the lock is released (wait_idle)
                         break
                     self.lock.wait(timeout=0.002)
             req, m = got
@@ -327,12 +333,14 @@ class Server:
             warm = (self.warm_small and req.kind == "fit" and req.error is None and m.hvg is None
                     and m.problem.n <= self.small_n)
             with self.lock:
-                if warm:   # account the handle first; skip the warm-up if it does not fit
-                    grow = m.footprint(True, True, m.cap_m) - m.bytes
+                if warm:   # account the handles first; skip the warm-up if they do not fit
+                    cap = max(m.cap_m, -(-self.warm_rows // 128) * 128)
+                    grow = m.footprint(True, True, cap) - m.bytes
                     warm = self.used + grow <= self.budget
                     if warm:
                         self.used += grow
                         m.bytes += grow
+                        m.cap_m = cap
                 if not warm:
                     m.busy = False
                     m.last_used = req.done
@@ -350,6 +358,9 @@ class Server:
                     m.busy = False
                     m.last_used = self.now()
                     self.lock.notify_all()
+            with self.lock:
+                self.busy_workers -= 1
+                self.lock.notify_all()
 
     def _upload(self, m):
         torch = self.torch
@@ -368,7 +379,9 @@ class Server:
 
     def _warm_vg(self, m, stream):
         """Create the model's evidence + gradient handle and capture its graph
-        (one evaluation at the fitted hyperparameters; the result is dropped)."""
+        (one evaluation at the fitted hyperparameters), and size the fit
+        handle's predict workspace for m.cap_m rows (one prediction at the
+        training inputs' first row, repeated); the results are dropped."""
         torch = self.torch
         p = m.problem
         if m.hvg is None:
@@ -378,6 +391,14 @@ class Server:
         out = torch.empty(1 + theta.numel(), dtype=torch.float32, device=self.device)
         N.check(self.lib.pgb_value_and_grad(m.hvg, d["X"].data_ptr(), d["y"].data_ptr(), theta.data_ptr(),
                                             out.data_ptr(), out[1:].data_ptr(), stream.cuda_stream), "warm-up")
+        M = m.cap_m
+        if M > 0:
+            Xs = d["X"][:1].expand(M, -1).contiguous()
+            mean = torch.empty(M, dtype=torch.float32, device=self.device)
+            var = torch.empty_like(mean)
+            N.check(self.lib.pgb_predict(m.h, d["X"].data_ptr(), d["theta"].data_ptr(), d["a"].data_ptr(),
+                                         d["W"].data_ptr(), Xs.data_ptr(), M, mean.data_ptr(), var.data_ptr(), 1,
+                                         stream.cuda_stream), "warm-up predict")
 
     def _run(self, req, m, stream):
         torch = self.torch
@@ -421,6 +442,13 @@ class Server:
             mh, vh = mean.to("cpu", non_blocking=True), var.to("cpu", non_blocking=True)
             stream.synchronize()
             req.result = (mh.numpy(), vh.numpy())
+
+    def wait_idle(self):
+        """Block until no request is queued and every worker is idle (warm-ups
+        included)."""
+        with self.lock:
+            while self._pending() or self.busy_workers:
+                self.lock.wait(timeout=0.01)
 
     # -- open-loop replay --------------------------------------------------------
     def replay(self, requests, realtime=True):
