@@ -8,6 +8,7 @@ CUDA kernels behind the C-ABI declared in ``include/probit_gb300.h``.
 
 from .approximators import LaplaceGP, VBGP
 from .batch import LaplaceBatch
+from .shard import ShardedBatch, lpt_partition
 from .kernels import EQ, Matern12
 from .utilities import (
     check_cutpoints,
@@ -20,7 +21,7 @@ from .utilities import (
 )
 
 __all__ = [
-    "LaplaceGP", "VBGP", "LaplaceBatch", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
+    "LaplaceGP", "VBGP", "LaplaceBatch", "ShardedBatch", "lpt_partition", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
     "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
     "check_cutpoints", "probit_predictive_distributions",
 ]
