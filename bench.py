@@ -44,7 +44,8 @@ FACTOR_TRAFFIC_N8192 = 85.472512e6 + 116.641792e6
 TF32_NOMINAL_TFLOPS = 1100.0
 UNIT = "solves/s"
 TOL = 1.0
-CONFIG_NAME = "gaussian_eq_ard_N8192_D4_evidence_grad"
+def config_name(n):
+    return f"gaussian_eq_ard_N{n}_D4_evidence_grad"
 
 
 def parse():
@@ -185,7 +186,7 @@ def run_reference(args, ws, rank):
         "impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus, "steps": done,
         "warmup": warm, "ms_per_step": 1e3 * dt / done, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": CONFIG_NAME, "N": args.n, "D": 4, "tolerance": TOL},
+        "config": {"workload": config_name(args.n), "N": args.n, "D": 4, "tolerance": TOL},
         "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"{done} full evidence+grad solve(s) at N={args.n} with the NumPy/SciPy "
                                    "restatement of the reference algorithm (dense-Jacobian LU Newton), float32"},
@@ -628,7 +629,7 @@ def run_gb300(args, ws, rank, local):
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": CONFIG_NAME, "N": n, "D": D, "kernel": "EQ ARD (0.5,1,1.5,2)", "likelihood":
+        "config": {"workload": config_name(n), "N": n, "D": D, "kernel": "EQ ARD (0.5,1,1.5,2)", "likelihood":
                    "gaussian sigma=0.2", "tolerance": TOL, "newton_iterations": iters,
                    "parallelism": "replicas" if ws > 1 else "single", "l2": "256 MB buffer written between steps"},
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
