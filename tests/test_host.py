@@ -86,3 +86,35 @@ def test_laplacegp_theta_layout_and_key():
     with pytest.raises(ValueError):
         LaplaceGP((np.zeros(5), y), lambda p: EQ(), pg.log_probit_likelihood)
     assert repr(gp) == "LaplaceGP"
+
+
+def test_evidence_autograd_function_carries_the_flat_gradient_to_the_leaves(monkeypatch):
+    """probit_gb300.autograd.evidence: the backward scales the flat gradient of
+    one value-and-gradient call by the cotangent and autograd maps it to the
+    torch leaves (the native call is replaced by a stand-in on the CPU)."""
+    import torch
+
+    from probit_gb300 import autograd as AG
+
+    calls = []
+
+    def fake(gp, theta, key):
+        t = theta.numpy()
+        calls.append(key)
+        g = np.where(np.isfinite(t), 2.0 * t, 0.0)
+        return float(np.sum(np.where(np.isfinite(t), t * t, 0.0))), g
+
+    monkeypatch.setattr(AG, "_value_and_grad_flat", fake)
+    X = np.zeros((5, 2), np.float32)
+    y = np.zeros(5, np.int32)
+    gp = LaplaceGP((X, y), lambda p: p[1] * Matern12().stretch(p[0]), pg.log_probit_likelihood)
+    ell = torch.tensor([0.5, 0.7], dtype=torch.float64, requires_grad=True)
+    s = torch.tensor(1.5, dtype=torch.float64, requires_grad=True)
+    sig = torch.tensor(0.6, dtype=torch.float64, requires_grad=True)
+    cut = torch.tensor([-np.inf, 0.25, np.inf], dtype=torch.float64)
+    v = AG.evidence(gp, ((torch.log(torch.exp(ell)), s), (sig, cut)))
+    assert calls == [(N.KERNEL_MATERN12, 2, 1.0, 2)]
+    assert abs(v.item() - (0.25 + 0.49 + 2.25 + 0.36 + 0.0625)) < 1e-12
+    (3.0 * v).backward()
+    assert np.allclose(ell.grad.numpy(), 3.0 * 2.0 * np.array([0.5, 0.7]))
+    assert abs(s.grad.item() - 3.0 * 3.0) < 1e-12 and abs(sig.grad.item() - 3.0 * 1.2) < 1e-12
