@@ -11,7 +11,9 @@ from .batch import LaplaceBatch
 from .shard import ShardedBatch, lpt_partition
 from .kernels import EQ, Matern12
 from .utilities import (
+    InvalidKernel,
     check_cutpoints,
+    check_data,
     grad_log_probit_likelihood,
     hessian_log_probit_likelihood,
     log_gaussian_likelihood,
@@ -23,6 +25,6 @@ from .utilities import (
 __all__ = [
     "LaplaceGP", "VBGP", "LaplaceBatch", "ShardedBatch", "lpt_partition", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
     "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
-    "check_cutpoints", "probit_predictive_distributions",
+    "check_cutpoints", "check_data", "InvalidKernel", "probit_predictive_distributions",
 ]
 __version__ = "0.1.0"

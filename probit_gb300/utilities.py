@@ -179,3 +179,21 @@ def check_cutpoints(cutpoints, J):
     if not all(c[i] <= c[i + 1] for i in range(J)):
         raise CutpointValueError(c)
     return c
+
+
+def check_data(data):
+    """(X, y) with integer class labels (``check_data``, ``utilities.py:252-260``):
+    y must hold integers; returned as int64."""
+    X, y = data
+    ya = np.asarray(y)
+    if not np.issubdtype(ya.dtype, np.integer):
+        raise TypeError(f"t must contain only integer values (got {ya.dtype})")
+    return X, ya.astype(np.int64)
+
+
+class InvalidKernel(Exception):
+    """A prior that is not a kernel this library evaluates (``InvalidKernel``,
+    ``utilities.py:348-360``; raised by the reference's examples)."""
+
+    def __init__(self, kernel):
+        super().__init__(f"{kernel} is not an instance of mlkernels.Kernel")

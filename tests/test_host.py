@@ -118,3 +118,13 @@ def test_evidence_autograd_function_carries_the_flat_gradient_to_the_leaves(monk
     (3.0 * v).backward()
     assert np.allclose(ell.grad.numpy(), 3.0 * 2.0 * np.array([0.5, 0.7]))
     assert abs(s.grad.item() - 3.0 * 3.0) < 1e-12 and abs(sig.grad.item() - 3.0 * 1.2) < 1e-12
+
+
+def test_check_data_and_invalid_kernel():
+    X = np.zeros((3, 2))
+    Xo, yo = pg.check_data((X, np.array([0, 2, 1], np.int32)))
+    assert Xo is X and yo.dtype == np.int64 and yo.tolist() == [0, 2, 1]
+    with pytest.raises(TypeError):
+        pg.check_data((X, np.array([0.0, 1.5, 1.0])))
+    e = pg.InvalidKernel("k")
+    assert "is not an instance of mlkernels.Kernel" in str(e)
