@@ -1,9 +1,13 @@
-"""probit_gb300: GB300-native (sm_103a) Laplace approximate inference for GPs.
+"""probit_gb300: GB300-native (sm_103a) approximate inference for GPs.
 
-A drop-in for the Laplace path of the reference package (bb515/probit):
-``LaplaceGP`` with ``weight``, ``precision``, ``approximate_posterior``,
-``objective``, ``value_and_grad`` and ``predict``, computed by hand-written
-CUDA kernels behind the C-ABI declared in ``include/probit_gb300.h``.
+A drop-in for the approximate-inference path of the reference package
+(bb515/probit): ``LaplaceGP`` and ``VBGP`` with ``weight``, ``precision``,
+``approximate_posterior``, ``objective``, ``value_and_grad``, ``predict`` and
+``predict_covariance``; ``LaplaceBatch`` / ``ShardedBatch`` for many GPs of
+any shapes, ``optimize.minimize_lockstep`` for their hyperparameter fits,
+``serving.Server`` for request serving and ``autograd.evidence`` for torch
+training loops — computed by hand-written CUDA kernels behind the C-ABI
+declared in ``include/probit_gb300.h``.
 """
 
 from .approximators import LaplaceGP, VBGP
@@ -23,8 +27,9 @@ from .utilities import (
 )
 
 __all__ = [
-    "LaplaceGP", "VBGP", "LaplaceBatch", "ShardedBatch", "lpt_partition", "EQ", "Matern12", "log_gaussian_likelihood", "log_probit_likelihood",
-    "log_probit_likelihood_stable", "grad_log_probit_likelihood", "hessian_log_probit_likelihood",
-    "check_cutpoints", "check_data", "InvalidKernel", "probit_predictive_distributions",
+    "LaplaceGP", "VBGP", "LaplaceBatch", "ShardedBatch", "lpt_partition", "EQ", "Matern12",
+    "log_gaussian_likelihood", "log_probit_likelihood", "log_probit_likelihood_stable",
+    "grad_log_probit_likelihood", "hessian_log_probit_likelihood", "check_cutpoints", "check_data",
+    "InvalidKernel", "probit_predictive_distributions",
 ]
 __version__ = "0.1.0"
