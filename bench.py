@@ -488,7 +488,7 @@ def run_serving(args, dev):
                 gc.unfreeze()
             summ = S.latency_summary(done)
             summ.update({"rate_req_s": rate, "window_s": dur, "requests": len(reqs), "prefit_s": prefit,
-                         "evictions": srv.evictions})
+                         "evictions": srv.evictions, "warm_up_errors": len(srv.warm_errors)})
         finally:
             srv.close()
         out[tag] = summ

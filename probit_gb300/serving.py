@@ -161,6 +161,7 @@ class Server:
         # request pays a first-use graph build or workspace allocation
         self.warm_small = warm_small
         self.warm_rows = int(warm_rows)
+        self.warm_errors = []          # warm-ups that failed (the first request then builds instead)
         self.busy_workers = 0
         self.models: dict[int, _Model] = {}
         self.evicted = set()
@@ -352,8 +353,8 @@ class Server:
                     with torch.cuda.stream(stream):
                         self._warm_vg(m, stream)
                     stream.synchronize()
-                except Exception:   # the first request on the model creates it instead
-                    pass
+                except Exception as exc:   # the first request on the model creates it instead
+                    self.warm_errors.append((m.id, repr(exc)))
                 with self.lock:
                     m.busy = False
                     m.last_used = self.now()
