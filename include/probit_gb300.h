@@ -97,6 +97,9 @@ int pgb_gp_create(const pgb_desc* desc, pgb_gp** out);
 /* Release a handle and all its device memory (after its work completed). */
 int pgb_gp_destroy(pgb_gp* gp);
 
+/* The descriptor the handle was created with (host copy). */
+int pgb_gp_desc(const pgb_gp* gp, pgb_desc* out);
+
 /* Cap the persistent blocks of the handle's launches at max_blocks (0: one
  * per SM, the default).  A server gives large problems a share of the SMs so
  * that the launches of small requests on other streams run beside them
@@ -256,6 +259,12 @@ int pgb_batch_create(const pgb_desc* descs, int32_t count, pgb_batch** out);
 
 /* Release a batch and its device memory (after its work completed). */
 int pgb_batch_destroy(pgb_batch* b);
+
+/* Number of problems of the batch. */
+int pgb_batch_size(const pgb_batch* b, int32_t* count);
+
+/* Descriptor of problem `index` (creation order) of the batch. */
+int pgb_batch_desc(const pgb_batch* b, int32_t index, pgb_desc* out);
 
 /* Element offsets of each problem's block in the packed X, y and theta
  * (host arrays of count + 1 entries; any may be NULL). */

@@ -1,4 +1,5 @@
-"""ctypes binding of ``libprobit_gb300.so`` (the C-ABI of include/probit_gb300.h).
+"""ctypes binding of ``libprobit_gb300.so`` (the C-ABI of include/probit_gb300.h
+and its DLPack entry points, include/probit_gb300_dlpack.h).
 
 The library is the only compute path: if it is missing or cannot be loaded,
 every entry point raises ``NativeLibraryError``; there is no CPU fallback.
@@ -72,6 +73,39 @@ class Status(C.Structure):
     ]
 
 
+class DLTensor(C.Structure):
+    """DLPack's DLTensor (the ``pgb_dltensor`` of include/probit_gb300_dlpack.h)."""
+
+    _fields_ = [
+        ("data", C.c_void_p),
+        ("device_type", C.c_int32),
+        ("device_id", C.c_int32),
+        ("ndim", C.c_int32),
+        ("dtype_code", C.c_uint8),
+        ("dtype_bits", C.c_uint8),
+        ("dtype_lanes", C.c_uint16),
+        ("shape", C.POINTER(C.c_int64)),
+        ("strides", C.POINTER(C.c_int64)),
+        ("byte_offset", C.c_uint64),
+    ]
+
+
+_capsule_ptr = C.pythonapi.PyCapsule_GetPointer
+_capsule_ptr.restype = C.c_void_p
+_capsule_ptr.argtypes = [C.py_object, C.c_char_p]
+
+
+def dlpack_tensor(obj):
+    """(capsule, address of its DLTensor) for a torch tensor or any object
+    with ``__dlpack__`` (legacy, unversioned capsule).  The capsule must stay
+    referenced while the address is used; the producer keeps ownership."""
+    if hasattr(obj, "__dlpack__"):
+        cap = obj.__dlpack__()
+    else:
+        cap = obj
+    return cap, _capsule_ptr(cap, b"dltensor")
+
+
 _VP = C.c_void_p
 _SIGS = {
     "pgb_version": (C.c_char_p, []),
@@ -105,6 +139,18 @@ _SIGS = {
     "pgb_batch_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
     "pgb_batch_set_enabled": (C.c_int, [_VP, _VP, _VP]),
     "pgb_batch_status": (C.c_int, [_VP, C.POINTER(Status), _VP]),
+    "pgb_gp_desc": (C.c_int, [_VP, C.POINTER(Desc)]),
+    "pgb_batch_size": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
+    "pgb_batch_desc": (C.c_int, [_VP, C.c_int32, C.POINTER(Desc)]),
+    # include/probit_gb300_dlpack.h (DLTensor arguments as addresses)
+    "pgb_dl_check": (C.c_int, [_VP, C.c_int32, C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
+    "pgb_dl_weight": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_dl_approximate_posterior": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_dl_objective": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_dl_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_dl_vb_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
+    "pgb_dl_predict": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP, _VP, C.c_int32, _VP]),
+    "pgb_dl_batch_value_and_grad": (C.c_int, [_VP, _VP, _VP, _VP, _VP, _VP, _VP]),
 }
 
 _lib = None

@@ -947,6 +947,12 @@ int pgb_gp_destroy(pgb_gp* gp) {
   return PGB_OK;
 }
 
+int pgb_gp_desc(const pgb_gp* gp, pgb_desc* out) {
+  if (!gp || !out) return PGB_EINVAL;
+  *out = gp->e.desc[0];
+  return PGB_OK;
+}
+
 int pgb_gp_set_max_blocks(pgb_gp* gp, int32_t max_blocks) {
   if (!gp || max_blocks < 0) return PGB_EINVAL;
   Engine& e = gp->e;
@@ -1269,6 +1275,18 @@ int pgb_batch_destroy(pgb_batch* b) {
   if (!b) return PGB_OK;
   engine_free(b->e);
   delete b;
+  return PGB_OK;
+}
+
+int pgb_batch_size(const pgb_batch* b, int32_t* count) {
+  if (!b || !count) return PGB_EINVAL;
+  *count = b->e.nprob;
+  return PGB_OK;
+}
+
+int pgb_batch_desc(const pgb_batch* b, int32_t index, pgb_desc* out) {
+  if (!b || !out || index < 0 || index >= b->e.nprob) return PGB_EINVAL;
+  *out = b->e.desc[index];
   return PGB_OK;
 }
 

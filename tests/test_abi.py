@@ -1,4 +1,4 @@
-"""The C-ABI library loads and exports every function include/probit_gb300.h declares."""
+"""The C-ABI library loads and exports every function include/*.h declares."""
 
 import ctypes as C
 import re
@@ -8,13 +8,15 @@ import pytest
 
 from probit_gb300 import _native as N
 
-HEADER = Path(__file__).resolve().parents[1] / "include" / "probit_gb300.h"
+HEADERS = sorted((Path(__file__).resolve().parents[1] / "include").glob("*.h"))
 
 
 def declared_functions():
-    text = HEADER.read_text()
-    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\b(pgb_[a-z_]+)\s*\(", text)))
+    names = set()
+    for h in HEADERS:
+        text = re.sub(r"/\*.*?\*/", "", h.read_text(), flags=re.S)
+        names.update(re.findall(r"\b(pgb_[a-z_]+)\s*\(", text))
+    return sorted(names)
 
 
 def test_header_declares_the_binding():
