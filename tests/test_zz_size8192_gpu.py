@@ -64,7 +64,7 @@ def test_n8192_evidence_and_gradient(cuda_device):
     import probit_gb300 as pg
     from probit_gb300 import workloads as W
 
-    p = W.regression_c1(N=8192, M=0, device=cuda_device)
+    p = W.regression_c1(N=8192, M=0)   # the benchmark's problem (host draw)
     gp = pg.LaplaceGP((p.X, p.y), p.prior(), pg.log_gaussian_likelihood, tolerance=1.0)
     v, g = gp.value_and_grad()(p.params())
     g = np.concatenate([np.ravel(np.asarray(g[0][0], np.float64)), [float(g[0][1])], [float(g[1][0])]])
