@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--predict-m", type=int, default=65536)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the float64 check of the headline value (a host Cholesky of N x N)")
     ap.add_argument("--batch", type=int, default=1024,
                     help="problems of the batched ordinal workload reported beside the headline (0: skip)")
     ap.add_argument("--batch-tol", type=float, default=1e-3)
@@ -210,6 +212,46 @@ def cpu_baseline(args):
     return {"value": 1.0 / dt, "unit": UNIT, "cores": len(os.sched_getaffinity(0)), "kind": "port",
             "sample": f"1 full evidence+grad solve at N={n} (NumPy/SciPy restatement of the reference "
                       f"algorithm, float32, OpenBLAS on all host threads): {dt:.1f} s"}
+
+
+def exact_gaussian_nll(X, y, ell, s, sigma):
+    """-log p(y) of GP regression with an EQ kernel (lengthscales ell, signal
+    variance s) and Gaussian noise std sigma, in float64 on the host:
+    1/2 y^T C^-1 y + sum log diag chol(C) + n/2 log 2 pi, C = K + sigma^2 I.
+    With a Gaussian likelihood the Laplace evidence is exactly this."""
+    import scipy.linalg as sla
+
+    Z = np.asarray(X, np.float64) / np.asarray(ell, np.float64)
+    y = np.asarray(y, np.float64)
+    sq = np.einsum("ij,ij->i", Z, Z)
+    C = Z @ Z.T
+    C *= -2.0
+    C += sq[:, None]
+    C += sq[None, :]
+    np.maximum(C, 0.0, out=C)
+    C *= -0.5
+    np.exp(C, out=C)
+    C *= s
+    C[np.diag_indices_from(C)] += sigma * sigma
+    c, low = sla.cho_factor(C, lower=True, overwrite_a=True, check_finite=False)
+    alpha = sla.cho_solve((c, low), y, check_finite=False)
+    return 0.5 * float(y @ alpha) + float(np.log(np.diag(c)).sum()) + 0.5 * y.size * math.log(2 * math.pi)
+
+
+def accuracy_check(p, value):
+    """The headline solve's value against the float64 closed form (a
+    size-independent property: Laplace evidence = marginal likelihood for a
+    Gaussian likelihood)."""
+    try:
+        th = np.asarray(p.theta(), np.float32).astype(np.float64)   # the float32 theta the GPU was given
+        t0 = time.perf_counter()
+        v64 = exact_gaussian_nll(p.X, p.y, th[:4], float(th[4]), float(th[5]))
+        return {"neg_log_evidence": value, "exact_float64": v64, "rel_err": abs(value - v64) / abs(v64),
+                "bar": 1e-4, "host_s": time.perf_counter() - t0,
+                "what": "Gaussian likelihood: the Laplace evidence is the exact GP marginal likelihood; "
+                        "closed form in float64 (Cholesky of K + sigma^2 I) on the host"}
+    except Exception as e:  # the check must not cost the bench line
+        return {"error": f"{type(e).__name__}: {e}"}
 
 
 # ---------------------------------------------------------------- batched workload
@@ -644,6 +686,8 @@ def run_gb300(args, ws, rank, local):
     }
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
+    if rank == 0 and ws == 1 and not args.no_accuracy:
+        line["accuracy"] = accuracy_check(p, float(out[0].item()))
     lib.pgb_gp_destroy(h)
     del flush
     if rank == 0 and ws == 1 and args.batch > 0:

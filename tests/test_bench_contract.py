@@ -23,3 +23,30 @@ def test_reference_arm_json_line():
     assert d["config"]["N"] == 256 and "N256" in d["config"]["workload"]
     assert d["cpu_baseline"]["kind"] == "port" and d["cpu_baseline"]["value"] == d["value"]
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["e2e"]["value"] == d["value"]
+
+
+def test_accuracy_check_closed_form():
+    """The bench's float64 check of the headline value: its closed form is the
+    oracle's objective for a Gaussian likelihood (N = 300), and a failure
+    inside it is reported instead of raised."""
+    import numpy as np
+
+    sys.path.insert(0, str(ROOT))
+    import bench
+    from oracle import laplace as L
+    from probit_gb300 import workloads as W
+
+    p = W.regression_problem(np.random.default_rng(4), 300, 4, "eq", [0.5, 1.0, 1.5, 2.0], 1.0, 0.2)
+    th = p.theta()
+    v = bench.exact_gaussian_nll(p.X, p.y, th[:4], th[4], th[5])
+    op = L.Problem(np.asarray(p.X, np.float64), np.asarray(p.y, np.float64), "eq", "gaussian", 4)
+    v64, _, _ = L.objective(op, th, tol=1e-10)
+    assert abs(v - v64) <= 1e-10 * abs(v64)
+    d = bench.accuracy_check(p, v * (1 + 2e-5))
+    assert abs(d["rel_err"] - 2e-5) < 1e-9 and d["exact_float64"] == v
+
+    class Broken:
+        def theta(self):
+            raise ValueError("no data")
+
+    assert "error" in bench.accuracy_check(Broken(), 0.0)
