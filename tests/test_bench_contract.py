@@ -42,8 +42,11 @@ def test_accuracy_check_closed_form():
     op = L.Problem(np.asarray(p.X, np.float64), np.asarray(p.y, np.float64), "eq", "gaussian", 4)
     v64, _, _ = L.objective(op, th, tol=1e-10)
     assert abs(v - v64) <= 1e-10 * abs(v64)
-    d = bench.accuracy_check(p, v * (1 + 2e-5))
-    assert abs(d["rel_err"] - 2e-5) < 1e-9 and d["exact_float64"] == v
+    # the check uses theta rounded to float32, as the GPU receives it
+    th32 = th.astype(np.float32).astype(np.float64)
+    v32 = bench.exact_gaussian_nll(p.X, p.y, th32[:4], th32[4], th32[5])
+    d = bench.accuracy_check(p, v32 * (1 + 2e-5))
+    assert abs(d["rel_err"] - 2e-5) < 1e-12 and d["exact_float64"] == v32
 
     class Broken:
         def theta(self):
