@@ -1,14 +1,14 @@
 """DLPack entry points (include/probit_gb300_dlpack.h).
 
-CPU: the library reads the DLTensor that torch's own DLPack producer writes
+The library reads the DLTensor that torch's own DLPack producer writes
 (pointer, device, dtype, shape, strides), and rejects wrong dtypes, shapes,
-strides, devices and null handles before any CUDA call.  GPU: the DLPack
-calls give the same bits as the pointer calls on the same data.
+strides, devices and null handles before any CUDA call (CPU).  The GPU
+check (DLPack and pointer calls give the same bits) is in
+test_zz_interfaces_gpu.py.
 """
 
 import ctypes as C
 
-import numpy as np
 import pytest
 
 from probit_gb300 import _native as N
@@ -97,44 +97,3 @@ def test_null_handles_are_rejected(native_lib):
     assert native_lib.pgb_dl_check(None, FLOAT, 32, 0, None, 1) == N.PGB_EINVAL
     assert native_lib.pgb_gp_desc(None, None) == N.PGB_EINVAL
     assert native_lib.pgb_batch_size(None, None) == N.PGB_EINVAL
-
-
-@pytest.mark.gpu
-def test_dlpack_calls_match_pointer_calls(native_lib, cuda_device):
-    import torch
-
-    import probit_gb300 as pg
-    from probit_gb300 import workloads as W
-
-    n, d, J = 300, 2, 3
-    p = W.ordinal_problem(np.random.default_rng(11), n, d, J, "matern12", 0.9, 1.1, 0.6, [-0.5, 0.5])
-    gp = pg.LaplaceGP((p.X, p.y), p.prior(), pg.log_probit_likelihood, tolerance=1e-4)
-    value, _ = gp.value_and_grad()(p.params())
-    h = list(gp._handles.values())[0]
-    desc = N.Desc()
-    N.check(native_lib.pgb_gp_desc(h.h, C.byref(desc)), "pgb_gp_desc")
-    assert (desc.n, desc.d, desc.j) == (n, d, J)
-    nth = native_lib.pgb_theta_size(C.byref(desc))
-    theta = torch.tensor(p.theta().astype(np.float32), device=cuda_device)
-    assert theta.numel() == nth
-    Xd = torch.tensor(np.asarray(p.X, np.float32), device=cuda_device)
-    yd = torch.tensor(np.asarray(p.y, np.int32), device=cuda_device)
-    stream = torch.cuda.current_stream().cuda_stream
-    out = {}
-    for mode in ("pointer", "dlpack"):
-        v = torch.full((1,), float("nan"), device=cuda_device)
-        g = torch.full((nth,), float("nan"), device=cuda_device)
-        if mode == "pointer":
-            N.check(native_lib.pgb_value_and_grad(h.h, Xd.data_ptr(), yd.data_ptr(), theta.data_ptr(),
-                                                  v.data_ptr(), g.data_ptr(), stream), "pgb_value_and_grad")
-        else:
-            caps = [N.dlpack_tensor(t) for t in (Xd, yd, theta, v, g)]
-            N.check(native_lib.pgb_dl_value_and_grad(h.h, *[a for _, a in caps], stream), "pgb_dl_value_and_grad")
-        torch.cuda.synchronize()
-        out[mode] = (v.cpu().numpy(), g.cpu().numpy())
-    assert np.array_equal(out["pointer"][0], out["dlpack"][0])
-    assert np.array_equal(out["pointer"][1], out["dlpack"][1])
-    assert np.isclose(out["dlpack"][0][0], value, rtol=1e-6)
-    # a wrong label dtype is refused before anything is enqueued
-    caps = [N.dlpack_tensor(t) for t in (Xd, yd.float(), theta, v, g)]
-    assert native_lib.pgb_dl_value_and_grad(h.h, *[a for _, a in caps], stream) == N.PGB_EINVAL
