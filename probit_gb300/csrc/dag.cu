@@ -746,7 +746,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       const int r = e >> 7, c = e & (T - 1);
       Linv_j[(size_t)r * T + c] = c <= r ? sC[c * SC_LD + r] : 0.0f;
     }
-  } else if (!is_rhs && i <= j + near_depth(nt)) {
+  } else if (!is_rhs && i <= j + jb.near) {
     // the tiles just below the diagonal feed the next columns' critical
     // path: substitution with each panel of L_jj as soon as it is
     // published, instead of waiting for L_jj^-1.  The tile just below
