@@ -113,6 +113,7 @@ struct Engine {
   std::vector<int> nt, th;                 // tiles per dimension, theta size
   std::vector<int> near;                   // near band depth of each problem's factorisations
   std::vector<int> rank;                   // position of each problem in the size order (largest first)
+  int whole_max = kWholeMaxTiles;          // problems of at most this many tile rows: one block each
   std::vector<size_t> x_off, y_off, th_off;   // offsets (elements) into the packed inputs
   size_t x_total = 0, y_total = 0, th_total = 0;
   int num_sms = 0, device = 0, dag_dm = 4, nt_max = 1;
@@ -238,15 +239,20 @@ int dag_stage(int i, int j, int nt, int near) {
 
 // One task list from every problem's tasks: by stage, then problem rank,
 // then column, then row.
+// A problem of at most `whole_max` tile rows becomes one task (job, -1, 0, 0)
+// at stage 0: one block runs all its tiles in order (no waits on other blocks).
 std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const std::vector<int>& nt,
-                              const std::vector<int>& rank, const std::vector<int>& near) {
+                              const std::vector<int>& rank, const std::vector<int>& near, int whole_max) {
   struct Key {
     int stage, rank, j, i;
     int4 t;
   };
   std::vector<Key> all;
   for (size_t p = 0; p < per.size(); ++p)
-    for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p], near[p]), rank[p], t.z, t.y, t});
+    if (nt[p] <= whole_max && !per[p].empty())
+      all.push_back(Key{0, rank[p], 0, -1, make_int4(per[p][0].x, -1, 0, 0)});
+    else
+      for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p], near[p]), rank[p], t.z, t.y, t});
   std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
     if (a.stage != b.stage) return a.stage < b.stage;
     if (a.rank != b.rank) return a.rank < b.rank;
@@ -442,7 +448,7 @@ void build_task_lists(Engine& e) {
     std::vector<std::vector<int4>> per(e.nprob);
     for (int p = 0; p < e.nprob; ++p)
       per[p] = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
-    e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near);
+    e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near, e.whole_max);
     e.ntasks[k] = (int)e.h_tasks[k].size();
   }
 }
@@ -571,6 +577,12 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   e.rank = rank;
   e.near.resize(count);
   for (int p = 0; p < count; ++p) e.near[p] = near_depth(e.nt[p]);
+  {
+    // PGB_WHOLE_TILES=k: problems of at most k tile rows run whole on one
+    // block (0: every tile is its own task)
+    const char* wv = std::getenv("PGB_WHOLE_TILES");
+    if (wv && wv[0] >= '0' && wv[0] <= '9') e.whole_max = std::atoi(wv);
+  }
   build_task_lists(e);
   // merged solve claims: position by position, problems by rank
   {
@@ -1210,7 +1222,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
       ws_free(e.cap_s, gp->tasks_c);
       gp->tasks_c = nullptr;
     }
-    std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0}, {e.near[0]});
+    std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0}, {e.near[0]}, 0);
     PGB_TRY(ws_alloc(e.cap_s, reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)));
     PGB_TRY(upload(gp->tasks_c, v, e.cap_s));
     gp->ntasks_c = (int)v.size();
@@ -1421,9 +1433,11 @@ int pgbx_batch_tasks(pgb_batch* b, int slot, const void** tasks, const void** tr
 // Internal diagnostic entry (host only, no GPU needed): the merged task list
 // the engine builds for `count` problems of nt[p] tile rows (kind 0 Newton
 // step, 1 factor only, 2 with L^-T) with near band depths near[p] (NULL:
-// the built-in rule), written to out[4 * task] as (job, i, j, 0); returns
+// the built-in rule) and problems of at most whole_max tile rows as one
+// task (job, -1, 0, 0), written to out[4 * task] as (job, i, j, 0); returns
 // the task count (call with out = NULL to size).
-int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t* near, int32_t* out) {
+int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t* near, int32_t whole_max,
+                   int32_t* out) {
   if (!nt || count < 1 || kind < 0 || kind > 2) return -1;
   std::vector<int> nearv(count);
   for (int p = 0; p < count; ++p) {
@@ -1437,7 +1451,7 @@ int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nt[a] > nt[b]; });
   for (int r = 0; r < count; ++r) rank[order[r]] = r;
   for (int p = 0; p < count; ++p) per[p] = build_tasks(p * JOB_COUNT + kind, nt[p], kinds[kind], kind == 0 ? 1 : nt[p], true);
-  std::vector<int4> v = merge_tasks(per, ntv, rank, nearv);
+  std::vector<int4> v = merge_tasks(per, ntv, rank, nearv, whole_max);
   if (out)
     for (size_t t = 0; t < v.size(); ++t) {
       out[4 * t] = v[t].x;

@@ -895,7 +895,25 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     const DagJob jb = jobs[tk.x];
     if (jb.active && __ldcg(jb.active) == 0) continue;           // problem has stopped
     if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
-    dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
+    if (tk.y >= 0) {
+      dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
+      continue;
+    }
+    // a whole small problem: every tile task of the job in column order on
+    // this block, so each dependency is already published when it is waited
+    // for; stops at the first abort of the problem
+    const int nt = jb.nt;
+    for (int j = 0; j < nt; ++j) {
+      const int nr = jb.rhs_kind == RHS_VEC ? 1 : jb.rhs_kind == RHS_IDENT ? j + 1 : jb.rhs_kind == RHS_CROSS ? jb.nrt : 0;
+      for (int i = j; i < nt + nr; ++i) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_task = ld_relaxed(jb.status + ST_ABORT);
+        __syncthreads();
+        if (s_task) break;
+        dag_task<DM>(jb, i, j, tc, s_ok, t);   // i >= nt: right-hand-side row i - nt
+        fence_proxy_async_smem();   // this task's shared-memory writes before the next task's tensor loads
+      }
+    }
   }
   tc_teardown(tc);
 }

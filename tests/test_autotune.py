@@ -67,14 +67,14 @@ def test_builtin_rule_matches_library_order(native_lib):
 
     native_lib.pgbx_dag_order.restype = C.c_int
     native_lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32),
-                                          C.POINTER(C.c_int32)]
+                                          C.c_int32, C.POINTER(C.c_int32)]
     for nt in (3, 15, 16, 40):
         arr = (C.c_int32 * 1)(nt)
-        n = native_lib.pgbx_dag_order(arr, 1, 1, None, None)
+        n = native_lib.pgbx_dag_order(arr, 1, 1, None, 0, None)
         a = (C.c_int32 * (4 * n))()
         b = (C.c_int32 * (4 * n))()
-        native_lib.pgbx_dag_order(arr, 1, 1, None, a)
-        native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(A.builtin_depth(nt)), b)
+        native_lib.pgbx_dag_order(arr, 1, 1, None, 0, a)
+        native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(A.builtin_depth(nt)), 0, b)
         assert a[:] == b[:]
 
 
@@ -105,3 +105,23 @@ def test_depths_agree_and_tuner_runs(cuda_device):
     t = A.tune(A.gpu_timer(reps=2, warmup=1), buckets=((1, 2), (5, 8)), candidates=(1, 2, 3))
     assert [e.depth for e in t.entries] and all(1 <= e.depth <= 3 for e in t.entries)
     assert all(ms > 0 for e in t.entries for ms in e.ms.values())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("n", [90, 200, 256])
+def test_whole_problem_blocks_give_the_same_bits(cuda_device, monkeypatch, n):
+    """A problem of at most two tile rows factored whole by one block gives
+    the bits of the tile-per-task order (same tile arithmetic, same order)."""
+    import probit_gb300 as pg
+    from probit_gb300 import workloads as W
+
+    p = W.ordinal_problem(np.random.default_rng(n), n, 2, 3, "matern12", 0.9, 1.1, 0.6, [-0.5, 0.5])
+    out = {}
+    for whole in ("0", "2"):
+        monkeypatch.setenv("PGB_WHOLE_TILES", whole)
+        gp = pg.LaplaceGP((p.X, p.y), p.prior(), pg.log_probit_likelihood, tolerance=1e-4)
+        v, g = gp.value_and_grad()(p.params())
+        a, W_ = gp.approximate_posterior(p.params())
+        out[whole] = (np.float32(v), np.asarray(a), np.asarray(W_), np.asarray(g[0][0]), np.asarray(g[1][1]))
+    for x, y in zip(out["0"], out["2"]):
+        assert np.array_equal(np.asarray(x).view(np.uint32), np.asarray(y).view(np.uint32))

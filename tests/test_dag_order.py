@@ -15,16 +15,16 @@ import numpy as np
 import pytest
 
 
-def _order(lib, nts, kind, near=None):
+def _order(lib, nts, kind, near=None, whole_max=0):
     lib.pgbx_dag_order.restype = C.c_int
-    lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32),
+    lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_int32,
                                    C.POINTER(C.c_int32)]
     arr = (C.c_int32 * len(nts))(*nts)
     nr = None if near is None else (C.c_int32 * len(nts))(*([near] * len(nts)))
-    n = lib.pgbx_dag_order(arr, len(nts), kind, nr, None)
+    n = lib.pgbx_dag_order(arr, len(nts), kind, nr, whole_max, None)
     assert n > 0
     out = (C.c_int32 * (4 * n))()
-    assert lib.pgbx_dag_order(arr, len(nts), kind, nr, out) == n
+    assert lib.pgbx_dag_order(arr, len(nts), kind, nr, whole_max, out) == n
     return np.array(out[:], dtype=np.int64).reshape(n, 4)
 
 
@@ -86,4 +86,23 @@ def test_dag_order_near_depth(native_lib):
             assert all(seq.index((j + d, j)) < nxt for d in range(1, q + 1)), (q, j)
             assert seq.index((j + q + 1, j)) > nxt, (q, j)
     arr = (C.c_int32 * 1)(12)
-    assert native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(0), None) == -1   # depth 0 is refused
+    assert native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(0), 0, None) == -1   # depth 0 is refused
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_small_problems_run_whole(native_lib, kind):
+    """Problems of at most whole_max tile rows are one task (i = -1) in the
+    first stage; the others keep every tile task, in the same order."""
+    nts = [5, 1, 2, 3, 2]
+    tasks = _order(native_lib, nts, kind, whole_max=2)
+    whole = [int(job) // 4 for job, i, _, _ in tasks if i == -1]
+    assert sorted(whole) == [1, 2, 4]
+    # first stage: the diagonal tile of column 0 of the large problems and the
+    # whole problems, by size
+    first = [(int(job) // 4, int(i)) for job, i, _, _ in tasks[:5]]
+    assert first == [(0, 0), (3, 0), (2, -1), (4, -1), (1, -1)]
+    rest = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in tasks if i != -1]
+    assert {p for p, _, _ in rest} == {0, 3}
+    full = _order(native_lib, nts, kind, whole_max=0)
+    kept = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in full if int(job) // 4 in (0, 3)]
+    assert rest == kept
