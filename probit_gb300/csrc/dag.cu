@@ -911,7 +911,10 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
         __syncthreads();
         if (s_task) break;
         dag_task<DM>(jb, i, j, tc, s_ok, t);   // i >= nt: right-hand-side row i - nt
-        fence_proxy_async_smem();   // this task's shared-memory writes before the next task's tensor loads
+        // this task's shared-memory and global writes (its tile of L) before
+        // the next task's tensor loads read them
+        fence_proxy_async_smem();
+        fence_proxy_async_global();
       }
     }
   }
