@@ -107,6 +107,17 @@ int pgb_gp_desc(const pgb_gp* gp, pgb_desc* out);
  * reference. */
 int pgb_gp_set_max_blocks(pgb_gp* gp, int32_t max_blocks);
 
+/* Launch tuning of the handle's factorisations (the knob the project's
+ * autotuner sets per problem-size bucket; no counterpart in the reference):
+ * the number of tiles below each 128 x 128 diagonal tile of L that are
+ * solved by substitution with the diagonal tile's panels as they are
+ * published (the factorisation's critical path), 1 .. 16; the tiles further
+ * down wait for the diagonal tile's inverse and use the tensor cores.
+ * 0 restores the built-in rule (3 for factors of 16 or more tiles, else 2).
+ * Waits for the device when the depth changes; results agree to rounding
+ * across depths. */
+int pgb_gp_set_near_depth(pgb_gp* gp, int32_t near_depth);
+
 /* Read the handle's device status word; synchronises `stream` first. */
 int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream);
 
@@ -259,6 +270,10 @@ int pgb_batch_create(const pgb_desc* descs, int32_t count, pgb_batch** out);
 
 /* Release a batch and its device memory (after its work completed). */
 int pgb_batch_destroy(pgb_batch* b);
+
+/* pgb_gp_set_near_depth for each problem of a batch (host array of count
+ * entries, creation order). */
+int pgb_batch_set_near_depth(pgb_batch* b, const int32_t* near_depth);
 
 /* Number of problems of the batch. */
 int pgb_batch_size(const pgb_batch* b, int32_t* count);

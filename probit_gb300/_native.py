@@ -140,6 +140,8 @@ _SIGS = {
     "pgb_batch_set_enabled": (C.c_int, [_VP, _VP, _VP]),
     "pgb_batch_status": (C.c_int, [_VP, C.POINTER(Status), _VP]),
     "pgb_gp_desc": (C.c_int, [_VP, C.POINTER(Desc)]),
+    "pgb_gp_set_near_depth": (C.c_int, [_VP, C.c_int32]),
+    "pgb_batch_set_near_depth": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
     "pgb_batch_size": (C.c_int, [_VP, C.POINTER(C.c_int32)]),
     "pgb_batch_desc": (C.c_int, [_VP, C.c_int32, C.POINTER(Desc)]),
     # include/probit_gb300_dlpack.h (DLTensor arguments as addresses)

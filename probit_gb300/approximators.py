@@ -17,6 +17,7 @@ import warnings
 import numpy as np
 
 from . import _native as N
+from . import autotune
 from ._device import as_device, require_cuda, stream_handle
 from .kernels import KIND_EQ, KIND_EQ_PERIODIC, KIND_MATERN12, resolve
 from .utilities import likelihood_mode
@@ -184,6 +185,9 @@ class LaplaceGP:
         N.check(lib.pgb_gp_create(desc, C.byref(h)), "pgb_gp_create")
         gp = _Handle(lib, h, desc)
         self._handles[key] = gp
+        depth = autotune.depth_for(self.N)
+        if depth:
+            N.check(lib.pgb_gp_set_near_depth(h, depth), "pgb_gp_set_near_depth")
         return gp
 
     def _theta_dev(self, theta64):

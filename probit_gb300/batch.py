@@ -18,6 +18,7 @@ import warnings
 import numpy as np
 
 from . import _native as N
+from . import autotune
 from ._device import require_cuda, stream_handle
 from .approximators import _to_leaf_tensor, _zip_grads, tree_map
 
@@ -53,6 +54,10 @@ class LaplaceBatch:
         h = C.c_void_p()
         N.check(self.lib.pgb_batch_create(self.descs, self.B, C.byref(h)), "pgb_batch_create")
         self.h = h
+        depths = [autotune.depth_for(d.n) for d in self.descs]
+        if any(depths):
+            N.check(self.lib.pgb_batch_set_near_depth(self.h, (C.c_int32 * self.B)(*depths)),
+                    "pgb_batch_set_near_depth")
         xo = (C.c_int64 * (self.B + 1))()
         yo = (C.c_int64 * (self.B + 1))()
         to = (C.c_int64 * (self.B + 1))()

@@ -111,6 +111,9 @@ struct Engine {
   std::vector<pgb_desc> desc;
   std::vector<Shape> sh;
   std::vector<int> nt, th;                 // tiles per dimension, theta size
+  std::vector<int> near;                   // near band depth of each problem's factorisations
+  std::vector<int> rank;                   // position of each problem in the size order (largest first)
+  int whole_max = kWholeMaxTiles;          // problems of at most this many tile rows: one block each
   std::vector<size_t> x_off, y_off, th_off;   // offsets (elements) into the packed inputs
   size_t x_total = 0, y_total = 0, th_total = 0;
   int num_sms = 0, device = 0, dag_dm = 4, nt_max = 1;
@@ -217,8 +220,8 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
 }
 
 // Lookahead stage of tile task (i, j) of a problem with nt tile rows
-// (i >= nt: right-hand-side rows):
-//   diagonal (j, j) -> 2j,  the near_depth(nt) tiles below it -> 2j+1,
+// (i >= nt: right-hand-side rows) and near band depth `near`:
+//   diagonal (j, j) -> 2j,  the `near` tiles below it -> 2j+1,
 //   other tiles of column j and right-hand-side tiles -> 2j+3,
 // so the diagonal of column j+1 and the tiles below it (the critical path:
 // they solve with the panels of L_jj as they are published) are handed out
@@ -228,23 +231,28 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
 // keeps every task after all tasks it waits for: a task (i, j) waits for
 // (i, k), (j, k) with k < j (stages <= 2j+1, and at stage 2j+1 only column
 // j-1 < j) and for (j, j) (stage 2j).
-int dag_stage(int i, int j, int nt) {
+int dag_stage(int i, int j, int nt, int near) {
   if (i < nt && i == j) return 2 * j;
-  if (i < nt && i <= j + near_depth(nt)) return 2 * j + 1;
+  if (i < nt && i <= j + near) return 2 * j + 1;
   return 2 * j + 3;
 }
 
 // One task list from every problem's tasks: by stage, then problem rank,
 // then column, then row.
+// A problem of at most `whole_max` tile rows becomes one task (job, -1, 0, 0)
+// at stage 0: one block runs all its tiles in order (no waits on other blocks).
 std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const std::vector<int>& nt,
-                              const std::vector<int>& rank) {
+                              const std::vector<int>& rank, const std::vector<int>& near, int whole_max) {
   struct Key {
     int stage, rank, j, i;
     int4 t;
   };
   std::vector<Key> all;
   for (size_t p = 0; p < per.size(); ++p)
-    for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p]), rank[p], t.z, t.y, t});
+    if (nt[p] <= whole_max && !per[p].empty())
+      all.push_back(Key{0, rank[p], 0, -1, make_int4(per[p][0].x, -1, 0, 0)});
+    else
+      for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p], near[p]), rank[p], t.z, t.y, t});
   std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
     if (a.stage != b.stage) return a.stage < b.stage;
     if (a.rank != b.rank) return a.rank < b.rank;
@@ -371,6 +379,7 @@ size_t layout(Engine& e, uintptr_t base) {
       j.n = s.n;
       j.nt = nt;
       j.ld = (long long)ld;
+      j.near = e.near[p];
       j.L = q.L;
       j.Linv = q.Linv;
       j.Xf = q.Xf;
@@ -427,6 +436,42 @@ void engine_free(Engine& e) {
 int engine_upload_tables(Engine& e) {
   PGB_TRY(h2d(e.probs, e.hp.data(), sizeof(Prob) * e.hp.size(), e.cap_s));
   return h2d(e.jobs, e.hjobs.data(), sizeof(DagJob) * e.hjobs.size(), e.cap_s);
+}
+
+// The three merged DAG task lists (Newton step, factor only, factor with
+// L^-T) from every problem's tiles, in lookahead order (dag_stage with the
+// problem's near band depth), problems by rank within a stage.  The task
+// counts do not depend on the depths.
+void build_task_lists(Engine& e) {
+  const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
+  for (int k = 0; k < 3; ++k) {
+    std::vector<std::vector<int4>> per(e.nprob);
+    for (int p = 0; p < e.nprob; ++p)
+      per[p] = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
+    e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near, e.whole_max);
+    e.ntasks[k] = (int)e.h_tasks[k].size();
+  }
+}
+
+// Set the near band depth of every problem (near[p] = 0: the built-in
+// rule) and rebuild the task lists and job tables.  Waits for the device
+// first: launches in flight read both.  Captured graphs stay valid (they read
+// the lists from the same device arrays; the task counts do not change).
+int engine_set_near(Engine& e, const int32_t* near) {
+  if (!near) return PGB_EINVAL;
+  std::vector<int> v(e.nprob);
+  for (int p = 0; p < e.nprob; ++p) {
+    v[p] = near[p] == 0 ? near_depth(e.nt[p]) : near[p];
+    if (v[p] < 1 || v[p] > kMaxNearDepth) return PGB_EINVAL;
+  }
+  if (v == e.near) return PGB_OK;
+  CU_TRY(cudaDeviceSynchronize());
+  e.near = v;
+  build_task_lists(e);
+  for (int p = 0; p < e.nprob; ++p)
+    for (int k = 0; k < JOB_COUNT; ++k) e.hjobs[(size_t)p * JOB_COUNT + k].near = v[p];
+  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
+  return engine_upload_tables(e);
 }
 
 // Build the engine of `count` problems: shapes, maps, task lists, one
@@ -529,16 +574,16 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   }
   // merged DAG task lists in lookahead order (dag_stage), problems by rank
   // within a stage
+  e.rank = rank;
+  e.near.resize(count);
+  for (int p = 0; p < count; ++p) e.near[p] = near_depth(e.nt[p]);
   {
-    const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
-    for (int k = 0; k < 3; ++k) {
-      std::vector<std::vector<int4>> per(count);
-      for (int p = 0; p < count; ++p)
-        per[p] = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
-      e.h_tasks[k] = merge_tasks(per, e.nt, rank);
-      e.ntasks[k] = (int)e.h_tasks[k].size();
-    }
+    // PGB_WHOLE_TILES=k: problems of at most k tile rows run whole on one
+    // block (0: every tile is its own task)
+    const char* wv = std::getenv("PGB_WHOLE_TILES");
+    if (wv && wv[0] >= '0' && wv[0] <= '9') e.whole_max = std::atoi(wv);
   }
+  build_task_lists(e);
   // merged solve claims: position by position, problems by rank
   {
     for (int q = 0; q < e.nt_max; ++q)
@@ -966,6 +1011,11 @@ int pgb_gp_set_max_blocks(pgb_gp* gp, int32_t max_blocks) {
   return PGB_OK;
 }
 
+int pgb_gp_set_near_depth(pgb_gp* gp, int32_t near_depth) {
+  if (!gp) return PGB_EINVAL;
+  return engine_set_near(gp->e, &near_depth);
+}
+
 int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream) {
   if (!gp || !out) return PGB_EINVAL;
   int h[kStatusWords];
@@ -1172,7 +1222,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
       ws_free(e.cap_s, gp->tasks_c);
       gp->tasks_c = nullptr;
     }
-    std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0});
+    std::vector<int4> v = merge_tasks({build_tasks(JOB_CROSS, nt, RHS_CROSS, mt, false)}, {nt}, {0}, {e.near[0]}, 0);
     PGB_TRY(ws_alloc(e.cap_s, reinterpret_cast<void**>(&gp->tasks_c), v.size() * sizeof(int4)));
     PGB_TRY(upload(gp->tasks_c, v, e.cap_s));
     gp->ntasks_c = (int)v.size();
@@ -1278,6 +1328,11 @@ int pgb_batch_destroy(pgb_batch* b) {
   return PGB_OK;
 }
 
+int pgb_batch_set_near_depth(pgb_batch* b, const int32_t* near_depth) {
+  if (!b) return PGB_EINVAL;
+  return engine_set_near(b->e, near_depth);
+}
+
 int pgb_batch_size(const pgb_batch* b, int32_t* count) {
   if (!b || !count) return PGB_EINVAL;
   *count = b->e.nprob;
@@ -1377,10 +1432,18 @@ int pgbx_batch_tasks(pgb_batch* b, int slot, const void** tasks, const void** tr
 
 // Internal diagnostic entry (host only, no GPU needed): the merged task list
 // the engine builds for `count` problems of nt[p] tile rows (kind 0 Newton
-// step, 1 factor only, 2 with L^-T), written to out[4 * task] as (job, i, j,
-// 0); returns the task count (call with out = NULL to size).
-int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, int32_t* out) {
+// step, 1 factor only, 2 with L^-T) with near band depths near[p] (NULL:
+// the built-in rule) and problems of at most whole_max tile rows as one
+// task (job, -1, 0, 0), written to out[4 * task] as (job, i, j, 0); returns
+// the task count (call with out = NULL to size).
+int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t* near, int32_t whole_max,
+                   int32_t* out) {
   if (!nt || count < 1 || kind < 0 || kind > 2) return -1;
+  std::vector<int> nearv(count);
+  for (int p = 0; p < count; ++p) {
+    nearv[p] = near ? near[p] : near_depth(nt[p]);
+    if (nearv[p] < 1 || nearv[p] > kMaxNearDepth) return -1;
+  }
   const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
   std::vector<std::vector<int4>> per(count);
   std::vector<int> ntv(nt, nt + count), order(count), rank(count);
@@ -1388,7 +1451,7 @@ int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, int32_t* out)
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nt[a] > nt[b]; });
   for (int r = 0; r < count; ++r) rank[order[r]] = r;
   for (int p = 0; p < count; ++p) per[p] = build_tasks(p * JOB_COUNT + kind, nt[p], kinds[kind], kind == 0 ? 1 : nt[p], true);
-  std::vector<int4> v = merge_tasks(per, ntv, rank);
+  std::vector<int4> v = merge_tasks(per, ntv, rank, nearv, whole_max);
   if (out)
     for (size_t t = 0; t < v.size(); ++t) {
       out[4 * t] = v[t].x;

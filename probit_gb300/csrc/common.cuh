@@ -143,12 +143,21 @@ __device__ __forceinline__ double block_sum_d(float v, double* smem_red) {
 
 __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; }
 
-// Tiles (i, j) with j < i <= j + near_depth(nt) of an nt-tile factor are
-// solved by substitution with the panels of L_jj as they are published (the
-// next columns' critical path); the tiles further down wait for L_jj^-1 and
-// use the tensor cores.  A deeper band keeps the inverse off the critical
-// path of long factorisations; short ones save the substitution work.
+// Tiles (i, j) with j < i <= j + near of an nt-tile factor are solved by
+// substitution with the panels of L_jj as they are published (the next
+// columns' critical path); the tiles further down wait for L_jj^-1 and use
+// the tensor cores.  A deeper band keeps the inverse off the critical path of
+// long factorisations; short ones save the substitution work.  near >= 1:
+// the tile just below the diagonal publishes its panels for the next
+// diagonal tile.  This is the built-in rule; a handle's tuning may set
+// another depth per problem (DagJob::near).
 __host__ __device__ inline int near_depth(int nt) { return nt >= 16 ? 3 : 2; }
+constexpr int kMaxNearDepth = 16;
+
+// Problems of at most this many tile rows (N <= 256) are factored whole by
+// one block: their tiles are few, and one block running them in order waits
+// for no other block.
+constexpr int kWholeMaxTiles = 2;
 
 }  // namespace pgb
 

@@ -746,7 +746,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       const int r = e >> 7, c = e & (T - 1);
       Linv_j[(size_t)r * T + c] = c <= r ? sC[c * SC_LD + r] : 0.0f;
     }
-  } else if (!is_rhs && i <= j + near_depth(nt)) {
+  } else if (!is_rhs && i <= j + jb.near) {
     // the tiles just below the diagonal feed the next columns' critical
     // path: substitution with each panel of L_jj as soon as it is
     // published, instead of waiting for L_jj^-1.  The tile just below
@@ -895,7 +895,28 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     const DagJob jb = jobs[tk.x];
     if (jb.active && __ldcg(jb.active) == 0) continue;           // problem has stopped
     if (jb.reuse_mode == 2 && __ldcg(jb.reuse) != 0) continue;   // solved elsewhere
-    dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
+    if (tk.y >= 0) {
+      dag_task<DM>(jb, tk.y, tk.z, tc, s_ok, t);
+      continue;
+    }
+    // a whole small problem: every tile task of the job in column order on
+    // this block, so each dependency is already published when it is waited
+    // for; stops at the first abort of the problem
+    const int nt = jb.nt;
+    for (int j = 0; j < nt; ++j) {
+      const int nr = jb.rhs_kind == RHS_VEC ? 1 : jb.rhs_kind == RHS_IDENT ? j + 1 : jb.rhs_kind == RHS_CROSS ? jb.nrt : 0;
+      for (int i = j; i < nt + nr; ++i) {
+        __syncthreads();
+        if (threadIdx.x == 0) s_task = ld_relaxed(jb.status + ST_ABORT);
+        __syncthreads();
+        if (s_task) break;
+        dag_task<DM>(jb, i, j, tc, s_ok, t);   // i >= nt: right-hand-side row i - nt
+        // this task's shared-memory and global writes (its tile of L) before
+        // the next task's tensor loads read them
+        fence_proxy_async_smem();
+        fence_proxy_async_global();
+      }
+    }
   }
   tc_teardown(tc);
 }

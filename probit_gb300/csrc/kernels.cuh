@@ -56,6 +56,7 @@ struct DagJob {
   long long ld;      // floats per row of L and R
   float* L;          // nt*T rows: lower tiles of the factor
   float* Linv;       // nt tiles of T x T: inverses of the diagonal tiles of L
+  int near;          // tiles below each diagonal tile solved by substitution (1 .. kMaxNearDepth)
   int rhs_kind;      // RhsKind
   int nrt;           // RHS tile rows
   int nrhs;          // RHS rows in use

@@ -15,14 +15,16 @@ import numpy as np
 import pytest
 
 
-def _order(lib, nts, kind):
+def _order(lib, nts, kind, near=None, whole_max=0):
     lib.pgbx_dag_order.restype = C.c_int
-    lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32)]
+    lib.pgbx_dag_order.argtypes = [C.POINTER(C.c_int32), C.c_int32, C.c_int32, C.POINTER(C.c_int32), C.c_int32,
+                                   C.POINTER(C.c_int32)]
     arr = (C.c_int32 * len(nts))(*nts)
-    n = lib.pgbx_dag_order(arr, len(nts), kind, None)
+    nr = None if near is None else (C.c_int32 * len(nts))(*([near] * len(nts)))
+    n = lib.pgbx_dag_order(arr, len(nts), kind, nr, whole_max, None)
     assert n > 0
     out = (C.c_int32 * (4 * n))()
-    assert lib.pgbx_dag_order(arr, len(nts), kind, out) == n
+    assert lib.pgbx_dag_order(arr, len(nts), kind, nr, whole_max, out) == n
     return np.array(out[:], dtype=np.int64).reshape(n, 4)
 
 
@@ -38,10 +40,11 @@ def _deps(i, j, nt, kind):
     return [(i, k) for k in range(k0, j)] + [(j, k) for k in range(k0, j)] + [(j, j)]
 
 
+@pytest.mark.parametrize("near", [None, 1, 2, 4, 16])
 @pytest.mark.parametrize("kind", [0, 1, 2])
 @pytest.mark.parametrize("nts", [[1], [2], [5], [17], [3, 1, 7, 2, 7], [32, 1, 1, 4, 9, 2, 16]])
-def test_dag_order_topological(native_lib, nts, kind):
-    tasks = _order(native_lib, nts, kind)
+def test_dag_order_topological(native_lib, nts, kind, near):
+    tasks = _order(native_lib, nts, kind, near)
     pos = {}
     for t, (job, i, j, _) in enumerate(tasks):
         p = job // 4
@@ -71,3 +74,35 @@ def test_dag_order_lookahead(native_lib):
     assert seq.index((3, 3)) < seq.index((5, 2))
     assert seq.index((2, 0)) < seq.index((1, 1))
     assert seq.index((3, 1)) < seq.index((2, 2))
+
+
+def test_dag_order_near_depth(native_lib):
+    """With a near band of depth q the q tiles below a diagonal come before
+    the next diagonal and the (q+1)-th after it."""
+    for q in (1, 3, 5):
+        seq = [(int(i), int(j)) for _, i, j, _ in _order(native_lib, [12], 1, q)]
+        for j in range(4):
+            nxt = seq.index((j + 1, j + 1))
+            assert all(seq.index((j + d, j)) < nxt for d in range(1, q + 1)), (q, j)
+            assert seq.index((j + q + 1, j)) > nxt, (q, j)
+    arr = (C.c_int32 * 1)(12)
+    assert native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(0), 0, None) == -1   # depth 0 is refused
+
+
+@pytest.mark.parametrize("kind", [0, 1, 2])
+def test_small_problems_run_whole(native_lib, kind):
+    """Problems of at most whole_max tile rows are one task (i = -1) in the
+    first stage; the others keep every tile task, in the same order."""
+    nts = [5, 1, 2, 3, 2]
+    tasks = _order(native_lib, nts, kind, whole_max=2)
+    whole = [int(job) // 4 for job, i, _, _ in tasks if i == -1]
+    assert sorted(whole) == [1, 2, 4]
+    # first stage: the diagonal tile of column 0 of the large problems and the
+    # whole problems, by size
+    first = [(int(job) // 4, int(i)) for job, i, _, _ in tasks[:5]]
+    assert first == [(0, 0), (3, 0), (2, -1), (4, -1), (1, -1)]
+    rest = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in tasks if i != -1]
+    assert {p for p, _, _ in rest} == {0, 3}
+    full = _order(native_lib, nts, kind, whole_max=0)
+    kept = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in full if int(job) // 4 in (0, 3)]
+    assert rest == kept
