@@ -154,10 +154,10 @@ __host__ __device__ inline int ceil_div(int a, int b) { return (a + b - 1) / b; 
 __host__ __device__ inline int near_depth(int nt) { return nt >= 16 ? 3 : 2; }
 constexpr int kMaxNearDepth = 16;
 
-// Problems of at most this many tile rows (N <= 256) are factored whole by
-// one block: their tiles are few, and one block running them in order waits
-// for no other block.
-constexpr int kWholeMaxTiles = 2;
+// Problems of at most this many tile rows are factored whole by one block
+// (their tiles run in order on that block, which waits for no other block).
+// Off by default (0): PGB_WHOLE_TILES=k turns it on for N <= 128 k.
+constexpr int kWholeMaxTiles = 0;
 
 }  // namespace pgb
 
