@@ -1,4 +1,5 @@
-"""Full-size parity: the N = 8192 evidence + gradient workload (Gaussian
+"""Full-size parity: the N = 8192 evidence + gradient and M = 65,536 predict
+workloads (Gaussian
 likelihood, EQ with four lengthscales, D = 4, the benchmark's problem)
 against a size-independent property.  For a Gaussian likelihood the Laplace
 evidence is the exact GP marginal likelihood
@@ -71,3 +72,35 @@ def test_n8192_evidence_and_gradient(cuda_device):
     v64, g64 = exact_gaussian(p.X, p.y, p.theta(), 4)
     assert abs(float(v) - v64) <= 1e-4 * abs(v64), (float(v), v64)
     assert np.abs(g - g64).max() <= 1e-2 * np.abs(g64).max(), (g, g64)
+
+
+@pytest.mark.gpu
+def test_n8192_predict_m65536(cuda_device):
+    """Predictive mean and variance at the benchmark's 65,536 test points
+    against the Gaussian closed form (mean K_*^T C^-1 y, variance
+    s - diag(K_*^T C^-1 K_*)) in float64 at every 64th point: the mean to
+    1e-4 of its largest magnitude, the variance to 1e-4 of the signal
+    variance s."""
+    import probit_gb300 as pg
+    from probit_gb300 import workloads as W
+
+    p = W.regression_c1(N=8192, M=65536)
+    params = p.params()
+    gp = pg.LaplaceGP((p.X, p.y), p.prior(), pg.log_gaussian_likelihood, tolerance=1.0)
+    a, Wp = gp.approximate_posterior(params)
+    mean, var = gp.predict(p.Xtest, params, a, Wp)
+    assert mean.shape == (65536,) and var.shape == (65536,)
+    th = p.theta()
+    ell, s, sig = th[:4], float(th[4]), float(th[5])
+    X = np.asarray(p.X, np.float64)
+    Xs = np.asarray(p.Xtest, np.float64)[::64]
+    C = L.gram("eq", X, X, ell, s)
+    C[np.diag_indices(X.shape[0])] += sig * sig
+    cf = sla.cho_factor(C, lower=True, overwrite_a=True, check_finite=False)
+    Ks = L.gram("eq", X, Xs, ell, s)
+    m64 = Ks.T @ sla.cho_solve(cf, np.asarray(p.y, np.float64), check_finite=False)
+    V = sla.solve_triangular(cf[0], Ks, lower=True, check_finite=False)
+    v64 = s - np.einsum("ij,ij->j", V, V)
+    m, v = np.asarray(mean, np.float64)[::64], np.asarray(var, np.float64)[::64]
+    assert np.abs(m - m64).max() <= 1e-4 * np.abs(m64).max(), np.abs(m - m64).max()
+    assert np.abs(v - v64).max() <= 1e-4 * s, np.abs(v - v64).max()
