@@ -214,42 +214,70 @@ def cpu_baseline(args):
                       f"algorithm, float32, OpenBLAS on all host threads): {dt:.1f} s"}
 
 
-def exact_gaussian_nll(X, y, ell, s, sigma):
-    """-log p(y) of GP regression with an EQ kernel (lengthscales ell, signal
-    variance s) and Gaussian noise std sigma, in float64 on the host:
-    1/2 y^T C^-1 y + sum log diag chol(C) + n/2 log 2 pi, C = K + sigma^2 I.
-    With a Gaussian likelihood the Laplace evidence is exactly this."""
-    import scipy.linalg as sla
-
-    Z = np.asarray(X, np.float64) / np.asarray(ell, np.float64)
-    y = np.asarray(y, np.float64)
-    sq = np.einsum("ij,ij->i", Z, Z)
-    C = Z @ Z.T
+def eq_gram64(X1, X2, ell, s):
+    """s exp(-|x1 - x2|^2 / 2) with inputs divided by the lengthscales, float64."""
+    A = np.asarray(X1, np.float64) / np.asarray(ell, np.float64)
+    Bm = np.asarray(X2, np.float64) / np.asarray(ell, np.float64)
+    C = A @ Bm.T
     C *= -2.0
-    C += sq[:, None]
-    C += sq[None, :]
+    C += np.einsum("ij,ij->i", A, A)[:, None]
+    C += np.einsum("ij,ij->i", Bm, Bm)[None, :]
     np.maximum(C, 0.0, out=C)
     C *= -0.5
     np.exp(C, out=C)
     C *= s
+    return C
+
+
+def exact_gaussian(X, y, ell, s, sigma, Xs=None):
+    """GP regression with an EQ kernel (lengthscales ell, signal variance s)
+    and Gaussian noise std sigma, in float64 on the host: -log p(y) =
+    1/2 y^T C^-1 y + sum log diag chol(C) + n/2 log 2 pi with C = K + sigma^2 I
+    (with a Gaussian likelihood the Laplace evidence is exactly this) and, at
+    test points Xs, the predictive mean K_*^T C^-1 y and latent variance
+    s - diag(K_*^T C^-1 K_*).  Returns (nll, mean or None, var or None)."""
+    import scipy.linalg as sla
+
+    y = np.asarray(y, np.float64)
+    C = eq_gram64(X, X, ell, s)
     C[np.diag_indices_from(C)] += sigma * sigma
     c, low = sla.cho_factor(C, lower=True, overwrite_a=True, check_finite=False)
     alpha = sla.cho_solve((c, low), y, check_finite=False)
-    return 0.5 * float(y @ alpha) + float(np.log(np.diag(c)).sum()) + 0.5 * y.size * math.log(2 * math.pi)
+    nll = 0.5 * float(y @ alpha) + float(np.log(np.diag(c)).sum()) + 0.5 * y.size * math.log(2 * math.pi)
+    if Xs is None:
+        return nll, None, None
+    Ks = eq_gram64(X, Xs, ell, s)
+    V = sla.solve_triangular(c, Ks, lower=True, check_finite=False)
+    return nll, Ks.T @ alpha, s - np.einsum("ij,ij->j", V, V)
 
 
-def accuracy_check(p, value):
-    """The headline solve's value against the float64 closed form (a
-    size-independent property: Laplace evidence = marginal likelihood for a
-    Gaussian likelihood)."""
+def exact_gaussian_nll(X, y, ell, s, sigma):
+    """-log p(y) of exact_gaussian."""
+    return exact_gaussian(X, y, ell, s, sigma)[0]
+
+
+def accuracy_check(p, value, mean=None, var=None, stride=64):
+    """The headline solve's value, and the predictive mean and variance at
+    every `stride`-th test point, against the float64 closed forms (a
+    size-independent property: for a Gaussian likelihood the Laplace
+    evidence is the marginal likelihood and the predictions are the GP's)."""
     try:
         th = np.asarray(p.theta(), np.float32).astype(np.float64)   # the float32 theta the GPU was given
         t0 = time.perf_counter()
-        v64 = exact_gaussian_nll(p.X, p.y, th[:4], float(th[4]), float(th[5]))
-        return {"neg_log_evidence": value, "exact_float64": v64, "rel_err": abs(value - v64) / abs(v64),
-                "bar": 1e-4, "host_s": time.perf_counter() - t0,
-                "what": "Gaussian likelihood: the Laplace evidence is the exact GP marginal likelihood; "
-                        "closed form in float64 (Cholesky of K + sigma^2 I) on the host"}
+        Xs = None if mean is None else np.asarray(p.Xtest)[::stride]
+        v64, m64, var64 = exact_gaussian(p.X, p.y, th[:4], float(th[4]), float(th[5]), Xs)
+        out = {"neg_log_evidence": value, "exact_float64": v64, "rel_err": abs(value - v64) / abs(v64),
+               "bar": 1e-4,
+               "what": "Gaussian likelihood: the Laplace evidence is the exact GP marginal likelihood; "
+                       "closed form in float64 (Cholesky of K + sigma^2 I) on the host"}
+        if mean is not None:
+            m = np.asarray(mean, np.float64)[::stride]
+            v = np.asarray(var, np.float64)[::stride]
+            out["predict"] = {"points": int(m.size), "stride": stride,
+                              "mean_err_of_max": float(np.abs(m - m64).max() / np.abs(m64).max()),
+                              "var_err_of_s": float(np.abs(v - var64).max() / th[4]), "bar": 1e-4}
+        out["host_s"] = time.perf_counter() - t0
+        return out
     except Exception as e:  # the check must not cost the bench line
         return {"error": f"{type(e).__name__}: {e}"}
 
@@ -646,6 +674,7 @@ def run_gb300(args, ws, rank, local):
 
     # ---- predict at M test points (reported beside the headline)
     pred = None
+    pred_mv = (None, None)
     if args.predict_m > 0 and rank == 0:
         Xs = torch.from_numpy(p.Xtest).to(dev)
         a = torch.empty(n, device=dev)
@@ -665,6 +694,7 @@ def run_gb300(args, ws, rank, local):
             times.append(e0.elapsed_time(e1))
         pf = float(n) * n * args.predict_m
         pred = {"M": args.predict_m, "ms": min(times), "tflops_algorithmic": pf / (min(times) / 1e3) / 1e12}
+        pred_mv = (mean.cpu().numpy(), var.cpu().numpy())
 
     launches_per_step = launches_per_solve(iters)
     line = {
@@ -687,7 +717,7 @@ def run_gb300(args, ws, rank, local):
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args)
     if rank == 0 and ws == 1 and not args.no_accuracy:
-        line["accuracy"] = accuracy_check(p, float(out[0].item()))
+        line["accuracy"] = accuracy_check(p, float(out[0].item()), *pred_mv)
     lib.pgb_gp_destroy(h)
     del flush
     if rank == 0 and ws == 1 and args.batch > 0:

@@ -48,6 +48,18 @@ def test_accuracy_check_closed_form():
     d = bench.accuracy_check(p, v32 * (1 + 2e-5))
     assert abs(d["rel_err"] - 2e-5) < 1e-12 and d["exact_float64"] == v32
 
+    # predictions: the closed form's own mean and variance give no error
+    Xt = np.random.default_rng(5).standard_normal((200, 4)).astype(np.float32)
+    p.Xtest = Xt
+    _, m32, var32 = bench.exact_gaussian(p.X, p.y, th32[:4], th32[4], th32[5], Xt)
+    d = bench.accuracy_check(p, v32, m32, var32, stride=4)
+    assert d["predict"]["points"] == 50 and d["predict"]["mean_err_of_max"] < 1e-12
+    assert d["predict"]["var_err_of_s"] < 1e-12
+    # and agree with the oracle's predict at the weight and precision of the fit
+    a = np.linalg.solve(L.gram("eq", p.X, p.X, th32[:4], th32[4]) + th32[5] ** 2 * np.eye(300), p.y)
+    m64, v64 = L.predict(op, th32, Xt.astype(np.float64), a, np.full(300, th32[5] ** -2))
+    assert np.allclose(m32, m64, rtol=1e-8, atol=1e-10) and np.allclose(var32, v64, rtol=1e-8, atol=1e-10)
+
     class Broken:
         def theta(self):
             raise ValueError("no data")
