@@ -59,6 +59,30 @@ def _to_leaf_tensor(x):
     return t.requires_grad_(True)
 
 
+def _assign_flat_grads(leaves, srcs, flat):
+    """Write slices of a flat theta gradient straight into the ``.grad`` of
+    the leaf tensors, when every part of theta is one of the leaves itself
+    (``srcs``: (object, offset, size) of the lengthscales, the signal
+    variance, the noise std and the cutpoints, as ``_theta(sources=True)``
+    gives them) — the usual ``((l, s), (sigma, cutpoints))`` pytree.  Returns
+    False, writing nothing, when some part was computed from the leaves (a
+    transformed parametrisation); the caller then back-propagates through
+    theta with autograd, which gives the same gradients."""
+    import torch
+
+    ids = {id(t): t for t in tree_leaves(leaves) if isinstance(t, torch.Tensor)}
+    plan = []
+    for obj, off, n in srcs:
+        t = ids.get(id(obj))
+        if t is None or t.numel() != n:
+            return False
+        plan.append((t, off, n))
+    for t, off, n in plan:
+        g = torch.from_numpy(np.array(flat[off:off + n], dtype=np.float64)).reshape(t.shape)
+        t.grad = g if t.grad is None else t.grad + g
+    return True
+
+
 def _grad_like(t, orig):
     g = t.grad
     if g is None:
@@ -139,8 +163,10 @@ class LaplaceGP:
         return self._Xd, self._yd
 
     # -- hyperparameters ----------------------------------------------------
-    def _theta(self, params):
-        """Flat theta (float64 torch, autograd-connected to the leaves) and the shape key."""
+    def _theta(self, params, sources=False):
+        """Flat theta (float64 torch, autograd-connected to the leaves) and the
+        shape key; with `sources`, also the (object, offset, size) each part of
+        theta was taken from (for _assign_flat_grads)."""
         import torch
 
         prior_params, lik_params = params[0], params[1]
@@ -171,6 +197,11 @@ class LaplaceGP:
         theta = torch.cat(parts)
         period = float(spec.period) if spec.period is not None else 1.0
         key = (_KIND_CODE[spec.kind], nl, period, J)
+        if sources:
+            srcs = [(spec.lengthscale, 0, nl), (spec.variance, nl, 1), (lp[0], nl + 1, 1)]
+            if J:
+                srcs.append((lp[1], nl + 2, J + 1))
+            return theta, key, srcs
         return theta, key
 
     def _handle(self, key):
@@ -265,7 +296,8 @@ class LaplaceGP:
             import torch
 
             leaves = tree_map(_to_leaf_tensor, parameters)
-            theta, key = self._theta(leaves)
+            with torch.no_grad():   # autograd is needed only for a transformed parametrisation
+                theta, key, srcs = self._theta(leaves, sources=True)
             gp = self._handle(key)
             X, y = self._device_data()
             td = self._theta_dev(theta)
@@ -275,8 +307,10 @@ class LaplaceGP:
                     "pgb_value_and_grad")
             host = out.cpu().numpy().astype(np.float64)
             self._after(gp, "value_and_grad")
-            if theta.requires_grad:
-                theta.backward(torch.from_numpy(host[1:]))
+            if not _assign_flat_grads(leaves, srcs, host[1:]):
+                theta, _ = self._theta(leaves)
+                if theta.requires_grad:
+                    theta.backward(torch.from_numpy(host[1:]))
             grads = _zip_grads(leaves, parameters)
             return float(host[0]), grads
 
@@ -439,7 +473,8 @@ class VBGP(LaplaceGP):
             import torch
 
             leaves = tree_map(_to_leaf_tensor, parameters)
-            theta, key = self._theta(leaves)
+            with torch.no_grad():   # autograd is needed only for a transformed parametrisation
+                theta, key, srcs = self._theta(leaves, sources=True)
             gp = self._handle(key)
             X, y = self._device_data()
             td = self._theta_dev(theta)
@@ -449,8 +484,10 @@ class VBGP(LaplaceGP):
                     "pgb_vb_value_and_grad")
             host = out.cpu().numpy().astype(np.float64)
             self._after(gp, "value_and_grad")
-            if theta.requires_grad:
-                theta.backward(torch.from_numpy(host[1:]))
+            if not _assign_flat_grads(leaves, srcs, host[1:]):
+                theta, _ = self._theta(leaves)
+                if theta.requires_grad:
+                    theta.backward(torch.from_numpy(host[1:]))
             return float(host[0]), _zip_grads(leaves, parameters)
 
         return vg

@@ -20,7 +20,7 @@ import numpy as np
 from . import _native as N
 from . import autotune
 from ._device import require_cuda, stream_handle
-from .approximators import _to_leaf_tensor, _zip_grads, tree_map
+from .approximators import _assign_flat_grads, _to_leaf_tensor, _zip_grads, tree_map
 
 
 class LaplaceBatch:
@@ -98,13 +98,19 @@ class LaplaceBatch:
         self.yd = torch.as_tensor(y).to(self.device, non_blocking=True)
 
     # -- hyperparameters --------------------------------------------------------
-    def pack_theta(self, parameters):
-        """Flat float64 theta of every problem (torch, autograd-connected) and the packed vector."""
+    def pack_theta(self, parameters, sources=None):
+        """Flat float64 theta of every problem (torch, autograd-connected) and the
+        packed vector; appends each problem's theta sources (the objects its
+        parts were taken from, see LaplaceGP._theta) to `sources` if given."""
         import torch
 
         thetas = []
         for b, (gp, p) in enumerate(zip(self.gps, parameters)):
-            t, key = gp._theta(p)
+            if sources is None:
+                t, key = gp._theta(p)
+            else:
+                t, key, src = gp._theta(p, sources=True)
+                sources.append(src)
             if key != self.keys[b]:
                 raise ValueError(f"problem {b}: parameters changed the problem's shape {self.keys[b]} -> {key}")
             thetas.append(t)
@@ -163,15 +169,20 @@ class LaplaceBatch:
             import torch
 
             leaves = [tree_map(_to_leaf_tensor, p) for p in parameters]
-            thetas, packed = self.pack_theta(leaves)
+            srcs = []
+            with torch.no_grad():   # autograd is needed only for a transformed parametrisation
+                thetas, packed = self.pack_theta(leaves, srcs)
             v, g = self.value_and_grad_flat(packed)
             v = v.cpu().numpy().astype(np.float64)
             g = g.cpu().numpy().astype(np.float64)
             self._warn()
             out = []
             for b, (t, lv, p) in enumerate(zip(thetas, leaves, parameters)):
-                if t.requires_grad:
-                    t.backward(torch.from_numpy(g[self.theta_off[b]:self.theta_off[b + 1]].copy()))
+                gb = g[self.theta_off[b]:self.theta_off[b + 1]]
+                if not _assign_flat_grads(lv, srcs[b], gb):
+                    t, _ = self.gps[b]._theta(lv)
+                    if t.requires_grad:
+                        t.backward(torch.from_numpy(gb.copy()))
                 out.append(_zip_grads(lv, p))
             return v, out
 

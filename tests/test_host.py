@@ -128,3 +128,65 @@ def test_check_data_and_invalid_kernel():
         pg.check_data((X, np.array([0.0, 1.5, 1.0])))
     e = pg.InvalidKernel("k")
     assert "is not an instance of mlkernels.Kernel" in str(e)
+
+
+@pytest.mark.parametrize("case", ["isotropic", "ard", "log_param", "gaussian", "shared_leaf", "tensor_leaves"])
+def test_flat_gradient_mapping_matches_autograd(case):
+    """value_and_grad maps the flat gradient to the parameter pytree either by
+    writing slices into the leaves (when theta's parts are the leaves
+    themselves) or through torch autograd (when the prior transforms them):
+    both give the same gradients, and the direct route is taken exactly when
+    every part is a leaf."""
+    import torch
+
+    from probit_gb300.approximators import _assign_flat_grads, _to_leaf_tensor, _zip_grads, tree_map
+    from probit_gb300.kernels import EQ
+
+    X = np.zeros((6, 3), np.float32)
+    cut = np.array([-np.inf, -0.3, 0.4, np.inf])
+    lik = pg.log_probit_likelihood
+    y = np.zeros(6, np.int32)
+    prior = lambda p: p[1] * Matern12().stretch(p[0])  # noqa: E731
+    direct = True
+    if case == "isotropic":
+        params = ((0.7, 1.3), (0.5, cut))
+    elif case == "ard":
+        params = ((np.array([0.5, 0.8, 1.1]), 1.3), (0.5, cut))
+    elif case == "log_param":
+        prior = lambda p: torch.exp(p[1]) * EQ().stretch(torch.exp(p[0]))  # noqa: E731
+        params = ((np.log(0.7), np.log(1.3)), (0.5, cut))
+        direct = False
+    elif case == "gaussian":
+        lik = pg.log_gaussian_likelihood
+        y = np.zeros(6, np.float32)
+        params = ((np.array([0.5, 0.8, 1.1]), 1.3), (0.5,))
+    elif case == "shared_leaf":
+        prior = lambda p: p[0] * EQ().stretch(p[0])  # noqa: E731
+        params = ((0.9, 0.0), (0.5, cut))
+    else:
+        params = ((torch.tensor([0.5, 0.8, 1.1]), torch.tensor(1.3)), (torch.tensor(0.5), torch.tensor(cut)))
+    gp = LaplaceGP((X, y), prior, lik)
+    rng = np.random.default_rng(len(case))
+
+    def mapped(use_direct):
+        # the steps of value_and_grad around the native call
+        leaves = tree_map(_to_leaf_tensor, params)
+        with torch.no_grad():
+            theta, key, srcs = gp._theta(leaves, sources=True)
+        flat = rng.standard_normal(theta.numel())
+        took = use_direct and _assign_flat_grads(leaves, srcs, flat)
+        if not took:
+            theta, _ = gp._theta(leaves)
+            theta.backward(torch.from_numpy(flat))
+        return took, _zip_grads(leaves, params)
+
+    rng = np.random.default_rng(7)
+    took, fast = mapped(True)
+    rng = np.random.default_rng(7)
+    _, slow = mapped(False)
+    assert took == direct
+    fl = [np.asarray(g, np.float64) for g in pg.approximators.tree_leaves(fast)]
+    sl = [np.asarray(g, np.float64) for g in pg.approximators.tree_leaves(slow)]
+    assert len(fl) == len(sl)
+    for a, b in zip(fl, sl):
+        assert a.shape == b.shape and np.allclose(a, b, rtol=1e-12, atol=0)
