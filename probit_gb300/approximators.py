@@ -140,6 +140,15 @@ class LaplaceGP:
             raise NotImplementedError(f"D = {self.D} > {N.MAX_D} input dimensions")
         if tuple(y.shape)[:1] != (self.N,):
             raise ValueError("y must have N entries")
+        if getattr(self, "_shape", None) not in (None, (self.N, self.D)) and self._handles:
+            # native handles are sized for the old shape; work still queued on
+            # the caller's streams may use them, so the device is drained first
+            import torch
+
+            if torch.cuda.is_available():
+                torch.cuda.synchronize()
+            self._handles.clear()
+        self._shape = (self.N, self.D)
         self._data = data
         self._Xd = None
         self._yd = None

@@ -190,3 +190,19 @@ def test_flat_gradient_mapping_matches_autograd(case):
     assert len(fl) == len(sl)
     for a, b in zip(fl, sl):
         assert a.shape == b.shape and np.allclose(a, b, rtol=1e-12, atol=0)
+
+
+def test_new_data_shape_drops_handles():
+    """Handles are sized for the data they were created with: data of another
+    shape drops them (the same shape keeps them)."""
+    X = np.zeros((5, 2), np.float32)
+    y = np.zeros(5, np.int32)
+    gp = LaplaceGP((X, y), lambda p: p[1] * Matern12().stretch(p[0]), pg.log_probit_likelihood)
+    gp._handles[("k",)] = object()
+    gp.data = (np.ones((5, 2), np.float32), y)
+    assert ("k",) in gp._handles
+    gp.data = (np.zeros((7, 2), np.float32), np.zeros(7, np.int32))
+    assert gp._handles == {} and (gp.N, gp.D) == (7, 2)
+    gp._handles[("k",)] = object()
+    gp.data = (np.zeros((7, 3), np.float32), np.zeros(7, np.int32))
+    assert gp._handles == {}
