@@ -59,6 +59,14 @@ def _to_leaf_tensor(x):
     return t.requires_grad_(True)
 
 
+def _vector_of_n(t, n, name):
+    """`t` as a flat vector of n entries (the C-ABI reads exactly n)."""
+    t = t.reshape(-1)
+    if t.numel() != n:
+        raise ValueError(f"{name} must have N = {n} entries, got {t.numel()}")
+    return t
+
+
 def _assign_flat_grads(leaves, srcs, flat):
     """Write slices of a flat theta gradient straight into the ``.grad`` of
     the leaf tensors, when every part of theta is one of the leaves itself
@@ -266,7 +274,7 @@ class LaplaceGP:
             gp = self._handle(key)
             X, y = self._device_data()
             td = self._theta_dev(theta)
-            a = as_device(weight, torch.float32)
+            a = _vector_of_n(as_device(weight, torch.float32), self.N, "weight")
             W = torch.empty(self.N, dtype=torch.float32, device=td.device)
             f = torch.empty_like(W)
             s = stream_handle(td.device)
@@ -347,7 +355,7 @@ class LaplaceGP:
         gp = self._handle(key)
         X, y = self._device_data()
         td = self._theta_dev(theta)
-        a = as_device(weight, torch.float32)
+        a = _vector_of_n(as_device(weight, torch.float32), self.N, "weight")
         W = torch.empty(self.N, dtype=torch.float32, device=td.device)
         f = torch.empty_like(W)
         N.check(gp.lib.pgb_precision(gp.h, X.data_ptr(), y.data_ptr(), td.data_ptr(), a.data_ptr(),
@@ -391,8 +399,8 @@ class LaplaceGP:
             a, W, reuse = last[2], last[3], 1
         else:
             gp.gen += 1
-            a = as_device(weight, torch.float32)
-            W = as_device(precision, torch.float32)
+            a = _vector_of_n(as_device(weight, torch.float32), self.N, "weight")
+            W = _vector_of_n(as_device(precision, torch.float32), self.N, "precision")
         mean = torch.empty(M, dtype=torch.float32, device=td.device)
         var = torch.empty_like(mean)
         N.check(gp.lib.pgb_predict(gp.h, X.data_ptr(), td.data_ptr(), a.data_ptr(), W.data_ptr(),
@@ -420,7 +428,7 @@ class LaplaceGP:
             W, reuse = last[3], 1
         else:
             gp.gen += 1
-            W = as_device(precision, torch.float32)
+            W = _vector_of_n(as_device(precision, torch.float32), self.N, "precision")
         cov = torch.empty((M, M), dtype=torch.float32, device=td.device)
         N.check(gp.lib.pgb_predict_covariance(gp.h, X.data_ptr(), td.data_ptr(), W.data_ptr(), Xs.data_ptr(), M,
                                               cov.data_ptr(), M, reuse, stream_handle(td.device)),

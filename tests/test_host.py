@@ -206,3 +206,15 @@ def test_new_data_shape_drops_handles():
     gp._handles[("k",)] = object()
     gp.data = (np.zeros((7, 3), np.float32), np.zeros(7, np.int32))
     assert gp._handles == {}
+
+
+def test_vector_size_checks():
+    """Weights and precisions handed to the C-ABI must have N entries (it
+    reads exactly N)."""
+    import torch
+
+    from probit_gb300.approximators import _vector_of_n
+
+    assert _vector_of_n(torch.zeros(2, 3), 6, "weight").shape == (6,)
+    with pytest.raises(ValueError, match="weight must have N = 5"):
+        _vector_of_n(torch.zeros(4), 5, "weight")
