@@ -195,6 +195,16 @@ class Server:
 
     # -- submission -------------------------------------------------------------
     def submit(self, req: Request):
+        if req.kind not in ("fit", "vg", "predict"):
+            raise ValueError(f"unknown request kind {req.kind!r}")
+        if req.kind == "predict":
+            Xs = np.asarray(req.Xs)
+            if Xs.ndim != 2 or Xs.shape[0] < 1 or Xs.shape[1] != req.problem.d:
+                raise ValueError(f"predict request: Xs must be (m >= 1, {req.problem.d}), got {Xs.shape}")
+        if req.kind == "vg" and req.theta is not None:
+            want = self.lib.pgb_theta_size(req.problem.desc())
+            if np.asarray(req.theta).size != want:
+                raise ValueError(f"vg request: theta must have {want} entries, got {np.asarray(req.theta).size}")
         with self.lock:
             cls = 0 if req.n <= self.small_n else 1
             heapq.heappush(self.heaps[cls], (req.arrival, next(self.seq), req))

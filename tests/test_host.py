@@ -218,3 +218,32 @@ def test_vector_size_checks():
     assert _vector_of_n(torch.zeros(2, 3), 6, "weight").shape == (6,)
     with pytest.raises(ValueError, match="weight must have N = 5"):
         _vector_of_n(torch.zeros(4), 5, "weight")
+
+
+def test_serving_rejects_malformed_requests():
+    """Server.submit checks what the C-ABI calls would read: a predict
+    request's test points are (m >= 1, d), an evaluation's theta has the
+    length the problem's descriptor gives."""
+    import itertools
+    import threading
+
+    from probit_gb300 import serving as S
+
+    srv = object.__new__(S.Server)
+    srv.lock = threading.Condition()
+    srv.heaps = ([], [])
+    srv.seq = itertools.count()
+    srv.small_n = 2048
+    srv.lib = N.load()
+    X = np.zeros((10, 3), np.float32)
+    p = S.Problem(X, np.zeros(10, np.int32), "eq", np.array([1.0, 1.0, 0.5, -np.inf, 0.0, np.inf]), nl=1, J=2)
+    srv.submit(S.Request(0.0, "predict", 0, p, Xs=np.zeros((4, 3), np.float32)))
+    for bad in (np.zeros((4, 2), np.float32), np.zeros((0, 3), np.float32), np.zeros(3, np.float32)):
+        with pytest.raises(ValueError):
+            srv.submit(S.Request(0.0, "predict", 0, p, Xs=bad))
+    srv.submit(S.Request(0.0, "vg", 0, p, theta=p.theta))
+    with pytest.raises(ValueError):
+        srv.submit(S.Request(0.0, "vg", 0, p, theta=p.theta[:-1]))
+    with pytest.raises(ValueError):
+        srv.submit(S.Request(0.0, "refit", 0, p))
+    assert len(srv.heaps[0]) == 2
