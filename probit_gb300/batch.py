@@ -94,8 +94,15 @@ class LaplaceBatch:
         if packed is None:
             packed = self.pack_data(datas)
         X, y = packed
-        self.Xd = torch.as_tensor(X).to(self.device, non_blocking=True)
-        self.yd = torch.as_tensor(y).to(self.device, non_blocking=True)
+        Xd = torch.as_tensor(X)
+        yd = torch.as_tensor(y)
+        # the C-ABI reads exactly the packed totals of pgb_batch_layout
+        if Xd.numel() != int(self.x_off[-1]) or Xd.dtype != torch.float32:
+            raise ValueError(f"packed X must be {int(self.x_off[-1])} float32 values")
+        if yd.numel() != int(self.y_off[-1]) or yd.element_size() != 4:
+            raise ValueError(f"packed y must be {int(self.y_off[-1])} 4-byte values")
+        self.Xd = Xd.to(self.device, non_blocking=True).reshape(-1).contiguous()
+        self.yd = yd.to(self.device, non_blocking=True).reshape(-1).contiguous()
 
     # -- hyperparameters --------------------------------------------------------
     def pack_theta(self, parameters, sources=None):
@@ -146,6 +153,8 @@ class LaplaceBatch:
         import torch
 
         td = torch.as_tensor(theta_packed).to(self.device, dtype=torch.float32).contiguous()
+        if td.numel() != int(self.theta_off[-1]):
+            raise ValueError(f"theta has {td.numel()} entries, the batch needs {int(self.theta_off[-1])}")
         s = stream if stream is not None else stream_handle(self.device)
         N.check(self.lib.pgb_batch_objective(self.h, self.Xd.data_ptr(), self.yd.data_ptr(), td.data_ptr(),
                                              self.values.data_ptr(), s), "pgb_batch_objective")

@@ -247,3 +247,24 @@ def test_serving_rejects_malformed_requests():
     with pytest.raises(ValueError):
         srv.submit(S.Request(0.0, "refit", 0, p))
     assert len(srv.heaps[0]) == 2
+
+
+def test_batch_packed_data_sizes():
+    """LaplaceBatch.set_data(packed=...) takes exactly the packed totals the
+    C-ABI reads (float32 X, 4-byte y)."""
+    import torch
+
+    from probit_gb300.batch import LaplaceBatch
+
+    b = object.__new__(LaplaceBatch)
+    b.x_off = np.array([0, 6, 15])
+    b.y_off = np.array([0, 3, 6])
+    b.device = torch.device("cpu")
+    b.set_data(packed=(np.zeros(15, np.float32), np.zeros(6, np.int32)))
+    assert b.Xd.shape == (15,) and b.yd.shape == (6,)
+    for X, y in ((np.zeros(14, np.float32), np.zeros(6, np.int32)),
+                 (np.zeros(15, np.float64), np.zeros(6, np.int32)),
+                 (np.zeros(15, np.float32), np.zeros(6, np.int64)),
+                 (np.zeros(15, np.float32), np.zeros(5, np.int32))):
+        with pytest.raises(ValueError):
+            b.set_data(packed=(X, y))
