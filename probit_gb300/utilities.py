@@ -48,6 +48,8 @@ def _eval(mode, f, y, likelihood_parameters, which):
     fd = as_device(f, torch.float32).reshape(-1)
     yd = yd.reshape(-1)
     n = fd.numel()
+    if yd.numel() != n:
+        raise ValueError(f"y has {yd.numel()} entries, f {n}")
     theta = torch.tensor(np.concatenate([[1.0, 1.0, sigma], cut]), dtype=torch.float32, device=fd.device)
     desc = N.Desc(max(n, 1), 1, N.KERNEL_EQ, 1, 1.0, mode, J, 1e-5, 100, 0)
     outs = [torch.empty(n, dtype=torch.float32, device=fd.device) for _ in range(4)]
@@ -73,6 +75,8 @@ def probit_predictive_distributions(likelihood_parameters, posterior_mean, poste
     md = as_device(posterior_mean, torch.float32).reshape(-1)
     vd = as_device(posterior_variance, torch.float32, md.device).reshape(-1)
     m = md.numel()
+    if vd.numel() != m:
+        raise ValueError(f"posterior_variance has {vd.numel()} entries, posterior_mean {m}")
     sigma = float(np.asarray(noise_std, dtype=np.float64))
     theta = torch.tensor(np.concatenate([[1.0, 1.0, sigma], cut]), dtype=torch.float32, device=md.device)
     desc = N.Desc(max(m, 1), 1, N.KERNEL_EQ, 1, 1.0, N.LIK_PROBIT, J, 1e-5, 100, 0)
