@@ -19,10 +19,28 @@ def require_cuda():
     return torch.device("cuda", torch.cuda.current_device())
 
 
+def from_dlpack_or_none(x):
+    """A torch view of an array from another framework that speaks DLPack
+    (a JAX or CuPy array: no copy when it is already on the device), or None
+    for torch tensors, NumPy arrays, Python objects and producers torch
+    cannot import."""
+    torch = _torch()
+    if isinstance(x, (torch.Tensor, np.ndarray)) or not hasattr(x, "__dlpack__"):
+        return None
+    try:
+        return torch.from_dlpack(x)
+    except (TypeError, ValueError, RuntimeError, BufferError):
+        return None
+
+
 def as_device(x, dtype, device=None):
-    """Contiguous CUDA tensor of `dtype` holding `x` (copied only if needed)."""
+    """Contiguous CUDA tensor of `dtype` holding `x` (copied only if needed;
+    DLPack arrays of other frameworks are taken without a host round trip)."""
     torch = _torch()
     dev = device if device is not None else require_cuda()
+    t = from_dlpack_or_none(x)
+    if t is not None:
+        x = t
     if isinstance(x, torch.Tensor):
         t = x.detach()
         if t.device != dev or t.dtype != dtype:

@@ -268,3 +268,38 @@ def test_batch_packed_data_sizes():
                  (np.zeros(15, np.float32), np.zeros(5, np.int32))):
         with pytest.raises(ValueError):
             b.set_data(packed=(X, y))
+
+
+def test_dlpack_arrays_of_other_frameworks_are_imported_without_copy():
+    """An array that only speaks DLPack (as a JAX or CuPy array does) becomes a
+    torch view of the same memory; torch tensors, NumPy arrays and plain
+    Python values are left to the usual conversions."""
+    import torch
+
+    from probit_gb300._device import from_dlpack_or_none
+
+    class Foreign:
+        def __init__(self, t):
+            self._t = t
+
+        def __dlpack__(self, stream=None, **kw):
+            return self._t.__dlpack__()
+
+        def __dlpack_device__(self):
+            return self._t.__dlpack_device__()
+
+    base = torch.arange(6, dtype=torch.float32)
+    v = from_dlpack_or_none(Foreign(base))
+    assert v is not None and v.data_ptr() == base.data_ptr() and torch.equal(v, base)
+    assert from_dlpack_or_none(base) is None
+    assert from_dlpack_or_none(np.zeros(3)) is None
+    assert from_dlpack_or_none([1.0, 2.0]) is None
+
+    class Broken:
+        def __dlpack__(self, stream=None, **kw):
+            raise BufferError("no export")
+
+        def __dlpack_device__(self):
+            return (1, 0)
+
+    assert from_dlpack_or_none(Broken()) is None
