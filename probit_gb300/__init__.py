@@ -5,9 +5,11 @@ A drop-in for the approximate-inference path of the reference package
 ``approximate_posterior``, ``objective``, ``value_and_grad``, ``predict`` and
 ``predict_covariance``; ``LaplaceBatch`` / ``ShardedBatch`` for many GPs of
 any shapes, ``optimize.minimize_lockstep`` for their hyperparameter fits,
-``serving.Server`` for request serving and ``autograd.evidence`` for torch
-training loops — computed by hand-written CUDA kernels behind the C-ABI
-declared in ``include/probit_gb300.h``.
+``serving.Server`` for request serving, ``autograd.evidence`` for torch
+training loops and ``autotune`` for the factorisation's launch tuning —
+computed by hand-written CUDA kernels behind the C-ABI declared in
+``include/probit_gb300.h`` (raw device pointers) and
+``include/probit_gb300_dlpack.h`` (DLPack tensors).
 """
 
 from .approximators import LaplaceGP, VBGP
