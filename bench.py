@@ -451,9 +451,10 @@ def run_hyperopt(args, dev):
     batch = pg.LaplaceBatch(gps, params)
     lp = LogParams(nl=1, J=5)
     rng = np.random.default_rng(30)
-    u0 = np.stack([lp.from_theta(q.theta()[None])[0] for q in probs])
+    th0 = np.stack([np.asarray(q.theta(), np.float64) for q in probs])
+    th0[:, 4:8] *= rng.uniform(0.7, 1.3, size=(B, 1))        # interior cutpoints scaled, still ordered
+    u0 = lp.from_theta(th0)
     u0[:, :3] += rng.normal(0.0, 0.5, size=(B, 3))          # log l, log s, log sigma away from the truth
-    u0[:, 3:] *= rng.uniform(0.7, 1.3, size=(B, 1))          # cutpoints scaled, still ordered
     fg_batch = batch_objective(batch, lp)
     solved = [0]
 

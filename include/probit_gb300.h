@@ -131,8 +131,9 @@ int pgb_gram(const pgb_desc* desc, const float* theta, const float* X1, int32_t 
  * allocator, work recorded by a framework's stream capture, services that
  * reserve memory at start-up).  This entry point has no counterpart in the
  * reference.  Its scratch is a fixed 4 MiB array inside the library, held by
- * every GPU that loads it: (n1 + n2) * ceil4(d) must not exceed 1,048,576
- * floats, else PGB_EUNSUPPORTED.  All calls share that array, so calls whose
+ * every GPU that loads it: (n1 + n2) * ceil4(F) must not exceed 1,048,576
+ * floats, else PGB_EUNSUPPORTED, where F is the kernel's feature count (d;
+ * 2d for eq_periodic).  Descriptors are checked as pgb_gram checks them.  All calls share that array, so calls whose
  * work overlaps on the GPU race; order them on one stream.  The first call on
  * a device resolves the array's address and may load device code: make it
  * before any stream capture. */

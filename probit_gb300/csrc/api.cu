@@ -48,6 +48,25 @@ using namespace pgb;
     if (_r != PGB_OK) return _r; \
   } while (0)
 
+// Descriptor check shared by every entry point that takes a pgb_desc
+// (declared in kernels.cuh; pgb_gram_noalloc uses it too).
+namespace pgb {
+int validate_desc(const pgb_desc* d) {
+  if (!d) return PGB_EINVAL;
+  if (d->n < 1 || d->n > (1 << 20)) return PGB_EINVAL;
+  if (d->d < 1 || d->d > PGB_MAX_D) return PGB_EINVAL;
+  if (d->kernel < PGB_KERNEL_EQ || d->kernel > PGB_KERNEL_EQ_PERIODIC) return PGB_EINVAL;
+  if (d->n_lengthscales != 1 && d->n_lengthscales != d->d) return PGB_EINVAL;
+  if (d->likelihood < PGB_LIK_GAUSSIAN || d->likelihood > PGB_LIK_PROBIT_STABLE) return PGB_EINVAL;
+  if (d->likelihood != PGB_LIK_GAUSSIAN && (d->j < 1 || d->j > 40)) return PGB_EINVAL;
+  if (d->kernel == PGB_KERNEL_EQ_PERIODIC && !(d->period > 0.0f)) return PGB_EINVAL;
+  if (!(d->tolerance >= 0.0f) || d->maxiter < 1) return PGB_EINVAL;
+  if (d->flags != 0) return PGB_EINVAL;
+  if (feature_count(d) > MAX_D) return PGB_EUNSUPPORTED;   // eq_periodic: 2 features per input dimension
+  return PGB_OK;
+}
+}  // namespace pgb
+
 namespace {
 
 enum GraphOp {
@@ -164,21 +183,6 @@ struct Engine {
   int eager = 0;                           // PGB_EAGER=1: kernels launched directly, host-driven loop
   unsigned long long* trace = nullptr;     // PGB_TRACE=1: per-task timestamps of the DAG
 };
-
-int validate(const pgb_desc* d) {
-  if (!d) return PGB_EINVAL;
-  if (d->n < 1 || d->n > (1 << 20)) return PGB_EINVAL;
-  if (d->d < 1 || d->d > PGB_MAX_D) return PGB_EINVAL;
-  if (d->kernel < PGB_KERNEL_EQ || d->kernel > PGB_KERNEL_EQ_PERIODIC) return PGB_EINVAL;
-  if (d->n_lengthscales != 1 && d->n_lengthscales != d->d) return PGB_EINVAL;
-  if (d->likelihood < PGB_LIK_GAUSSIAN || d->likelihood > PGB_LIK_PROBIT_STABLE) return PGB_EINVAL;
-  if (d->likelihood != PGB_LIK_GAUSSIAN && (d->j < 1 || d->j > 40)) return PGB_EINVAL;
-  if (d->kernel == PGB_KERNEL_EQ_PERIODIC && !(d->period > 0.0f)) return PGB_EINVAL;
-  if (!(d->tolerance >= 0.0f) || d->maxiter < 1) return PGB_EINVAL;
-  if (d->flags != 0) return PGB_EINVAL;
-  if (feature_count(d) > MAX_D) return PGB_EUNSUPPORTED;   // eq_periodic: 2 features per input dimension
-  return PGB_OK;
-}
 
 Shape make_shape(const pgb_desc* d) { return shape_from_desc(d); }
 
@@ -479,7 +483,7 @@ int engine_set_near(Engine& e, const int32_t* near) {
 // solve orders, so the longest critical paths start first.
 int engine_init(Engine& e, const pgb_desc* descs, int count) {
   if (!descs || count < 1) return PGB_EINVAL;
-  for (int p = 0; p < count; ++p) PGB_TRY(validate(descs + p));
+  for (int p = 0; p < count; ++p) PGB_TRY(validate_desc(descs + p));
   setup_attributes();
   e.nprob = count;
   e.desc.assign(descs, descs + count);
@@ -962,7 +966,7 @@ const char* pgb_strerror(int code) {
 }
 
 int pgb_theta_size(const pgb_desc* desc) {
-  int r = validate(desc);
+  int r = validate_desc(desc);
   if (r != PGB_OK) return r;
   return theta_size_of(desc);
 }
@@ -970,7 +974,7 @@ int pgb_theta_size(const pgb_desc* desc) {
 int pgb_gp_create(const pgb_desc* desc, pgb_gp** out) {
   if (!out) return PGB_EINVAL;
   *out = nullptr;
-  int r = validate(desc);
+  int r = validate_desc(desc);
   if (r != PGB_OK) return r;
   pgb_gp* gp = new pgb_gp();
   r = engine_init(gp->e, desc, 1);
@@ -1027,7 +1031,7 @@ int pgb_gp_status(pgb_gp* gp, pgb_status* out, void* stream) {
 
 int pgb_gram(const pgb_desc* desc, const float* theta, const float* X1, int32_t n1, const float* X2, int32_t n2,
              float* K, int64_t ldk, void* stream) {
-  if (validate(desc) != PGB_OK || !theta || !X1 || !X2 || !K || n1 < 0 || n2 < 0 || ldk < n2) return PGB_EINVAL;
+  if (validate_desc(desc) != PGB_OK || !theta || !X1 || !X2 || !K || n1 < 0 || n2 < 0 || ldk < n2) return PGB_EINVAL;
   if (n1 == 0 || n2 == 0) return PGB_OK;
   cudaStream_t s = (cudaStream_t)stream;
   const Shape sh = make_shape(desc);
@@ -1045,7 +1049,7 @@ int pgb_gram(const pgb_desc* desc, const float* theta, const float* X1, int32_t 
 
 int pgb_log_likelihood(const pgb_desc* desc, const float* theta, const float* f, const void* y, int32_t n,
                        float* logp, float* d1, float* d2, float* d3, void* stream) {
-  if (validate(desc) != PGB_OK || !theta || !f || !y || n < 0) return PGB_EINVAL;
+  if (validate_desc(desc) != PGB_OK || !theta || !f || !y || n < 0) return PGB_EINVAL;
   if (n == 0) return PGB_OK;
   Shape sh = make_shape(desc);
   sh.n = n;
@@ -1297,7 +1301,7 @@ int pgb_predict_covariance(pgb_gp* gp, const float* X, const float* theta, const
 
 int pgb_predictive_distributions(const pgb_desc* desc, const float* theta, const float* mean, const float* var,
                                  int32_t m, float* dist_out, void* stream) {
-  if (validate(desc) != PGB_OK || desc->likelihood == PGB_LIK_GAUSSIAN || !theta || !mean || !var || !dist_out ||
+  if (validate_desc(desc) != PGB_OK || desc->likelihood == PGB_LIK_GAUSSIAN || !theta || !mean || !var || !dist_out ||
       m < 0)
     return PGB_EINVAL;
   launch_predictive_dist(make_shape(desc), theta, mean, var, m, dist_out, (cudaStream_t)stream);
@@ -1310,7 +1314,7 @@ int pgb_batch_create(const pgb_desc* descs, int32_t count, pgb_batch** out) {
   if (!out) return PGB_EINVAL;
   *out = nullptr;
   if (!descs || count < 1) return PGB_EINVAL;
-  for (int p = 0; p < count; ++p) PGB_TRY(validate(descs + p));
+  for (int p = 0; p < count; ++p) PGB_TRY(validate_desc(descs + p));
   pgb_batch* b = new pgb_batch();
   int r = engine_init(b->e, descs, count);
   if (r != PGB_OK) {
@@ -1395,6 +1399,31 @@ int pgb_batch_status(pgb_batch* b, pgb_status* out, void* stream) {
   CU_TRY(cudaStreamSynchronize((cudaStream_t)stream));
   for (int p = 0; p < e.nprob; ++p) status_from_words(h.data() + (size_t)p * kStatusWords, out + p);
   return PGB_OK;
+}
+
+// Internal test hook (not part of the public C-ABI): makes the bounded
+// device-side waits of one problem of a batch run out without any fault.
+// The problem's flag waits give up after wait_limit_us microseconds (0: the
+// built-in 4 s), and the factorisation tile (tile_i, tile_j), tile_i > tile_j
+// (an off-diagonal tile of L), never releases its ready flag, so every task
+// that depends on it waits, gives up, and the problem ends with
+// PGB_ETIMEOUT while the other problems of the batch finish normally.
+// problem < 0 clears the hook of every problem.  Waits for the device first
+// (launches in flight read the tables).
+int pgbx_batch_test_hook(pgb_batch* b, int32_t problem, int32_t wait_limit_us, int32_t tile_i, int32_t tile_j) {
+  if (!b) return PGB_EINVAL;
+  Engine& e = b->e;
+  if (problem >= e.nprob || wait_limit_us < 0) return PGB_EINVAL;
+  if (problem >= 0 && tile_i >= 0 && !(tile_i > tile_j && tile_j >= 0 && tile_i < e.nt[problem])) return PGB_EINVAL;
+  CU_TRY(cudaDeviceSynchronize());
+  for (int p = 0; p < e.nprob; ++p) {
+    const bool on = problem < 0 ? false : p == problem;
+    const int wh = (on && tile_i >= 0) ? ((tile_i << 16) | tile_j) + 1 : 0;
+    for (int k = 0; k < JOB_COUNT; ++k) e.hjobs[(size_t)p * JOB_COUNT + k].withhold = wh;
+    const int us = on ? wait_limit_us : 0;
+    PGB_TRY(h2d(e.status_all + (size_t)p * kStatusWords + ST_WAIT_US, &us, sizeof(int), e.cap_s));
+  }
+  return engine_upload_tables(e);
 }
 
 // Internal diagnostic entry (not part of the public C-ABI): device pointer of

@@ -26,7 +26,8 @@ enum StatusSlot {
   ST_NOTPD_COL = 2,   // first column whose pivot was not positive (or -1)
   ST_ABORT = 3,       // set by any kernel that gave up waiting
   ST_CONVERGED = 4,   // 1 once the fixed point test passed
-  ST_SPARE0 = 5,
+  ST_WAIT_US = 5,     // limit of this problem's flag waits in microseconds (0: WAIT_LIMIT_NS);
+                      // written only by a test hook, kept across operations
   ST_STALL = 6,       // consecutive Newton steps that did not halve ||delta||
   ST_PREV_ERR = 7,    // float bits of the previous step's ||delta||
 };
@@ -58,11 +59,11 @@ __device__ __forceinline__ uint64_t global_ns() {
   return t;
 }
 
-// Bounded wait for *flag >= target.  Gives up after `limit_ns` of wall time
-// or as soon as another block has raised the abort word; a give-up raises the
-// abort word itself (with PGB_ETIMEOUT as the status code when none is set)
-// so every other waiter of this launch returns promptly.  Returns true when
-// the flag was seen.
+// Bounded wait for *flag >= target.  Gives up after WAIT_LIMIT_NS of wall
+// time (or the problem's ST_WAIT_US override) or as soon as another block has
+// raised the abort word; a give-up raises the abort word itself (with
+// PGB_ETIMEOUT as the status code when none is set) so every other waiter of
+// this launch returns promptly.  Returns true when the flag was seen.
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;   // 4 s
 // wait_flag_value: the same wait for a target >= 1, returning the value
 // seen (>= target), or 0 when it gave up.
@@ -70,12 +71,14 @@ __device__ __forceinline__ int wait_flag_value(const int* flag, int target, int*
   int v = ld_acquire(flag);
   if (v >= target) return v;
   const uint64_t t0 = global_ns();
+  const int limit_us = ld_relaxed(status + ST_WAIT_US);
+  const uint64_t limit_ns = limit_us > 0 ? (uint64_t)limit_us * 1000ull : WAIT_LIMIT_NS;
   unsigned ns = 32;
   while (true) {
     v = ld_acquire(flag);
     if (v >= target) return v;
     if (ld_relaxed(status + ST_ABORT)) return 0;
-    if (global_ns() - t0 > WAIT_LIMIT_NS) {
+    if (global_ns() - t0 > limit_ns) {
       atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
       atomicExch(status + ST_ABORT, 1);
       return 0;

@@ -671,11 +671,12 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const int ri = i - nt;
   float* rowbase = is_rhs ? jb.R + (size_t)ri * T * ld : jb.L + (size_t)i * T * ld;
   const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
+  const bool withheld = jb.withhold == ((i << 16) | j) + 1;
   if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
     // the resident L tile (and, on the diagonal, its inverse) is already the
     // factor: publish it and move on
     __syncthreads();
-    if (threadIdx.x == 0) st_release(jb.ready + (size_t)i * nt + j, i == j ? 2 : 1);
+    if (threadIdx.x == 0 && !withheld) st_release(jb.ready + (size_t)i * nt + j, i == j ? 2 : 1);
     return;
   }
 
@@ -828,7 +829,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     if (tr) tr[2] = global_ns();
     __threadfence();
     // diagonal tiles: 2 = L_jj and its inverse published; others: 1 = tile ready
-    st_release(jb.ready + (size_t)i * nt + j, (!is_rhs && i == j) ? 2 : 1);
+    if (!withheld) st_release(jb.ready + (size_t)i * nt + j, (!is_rhs && i == j) ? 2 : 1);
     if (tr) tr[3] = global_ns();
   }
 }

@@ -11,8 +11,10 @@
 // this variant takes them from a fixed array compiled into the library.
 //
 // The scratch is a file-scope __device__ array of kScratchFloats floats
-// (4 MiB).  Every GPU that loads this library holds it until the process
-// exits.  All calls share it and each call overwrites what it uses (nothing
+// (4 MiB): the prepared features of both point sets, (n1 + n2) * ceil4(F)
+// floats, where F is the kernel's feature count (d, or 2d for eq_periodic,
+// whose inputs become sin/cos pairs).  Every GPU that loads this library
+// holds it until the process exits.  All calls share it and each call overwrites what it uses (nothing
 // has to start at zero), so two calls whose work overlaps on the GPU — on
 // different streams without ordering between them — race on it and give
 // wrong results; order them on one stream.
@@ -21,8 +23,10 @@
 // The first call on each device (with that device current) resolves the
 // device address once with cudaGetSymbolAddress and caches it; that first
 // call may load the library's device code, so make it before any stream
-// capture begins.  It calls no cudaMalloc/cudaFree and no allocating library
-// routine.
+// capture begins.  The cached address belongs to the device's primary
+// context, the one the CUDA runtime uses: it assumes that context lives as
+// long as the process (no cudaDeviceReset while the library is in use).
+// It calls no cudaMalloc/cudaFree and no allocating library routine.
 #include <cstdio>
 #include <mutex>
 
@@ -56,18 +60,13 @@ int scratch_address(float** out) {
   return PGB_OK;
 }
 
-bool desc_ok(const pgb_desc* d) {
-  return d && d->n >= 1 && d->d >= 1 && d->d <= PGB_MAX_D && d->kernel >= PGB_KERNEL_EQ &&
-         d->kernel <= PGB_KERNEL_EQ_PERIODIC && (d->n_lengthscales == 1 || d->n_lengthscales == d->d) &&
-         (d->kernel != PGB_KERNEL_EQ_PERIODIC || d->period > 0.0f) && d->flags == 0 &&
-         pgb::feature_count(d) <= pgb::MAX_D;
-}
-
 }  // namespace
 
 extern "C" int pgb_gram_noalloc(const pgb_desc* desc, const float* theta, const float* X1, int32_t n1,
                                 const float* X2, int32_t n2, float* K, int64_t ldk, void* stream) {
-  if (!desc_ok(desc) || !theta || !X1 || !X2 || !K || n1 < 0 || n2 < 0 || ldk < n2) return PGB_EINVAL;
+  // the same descriptor check and error codes as pgb_gram
+  if (pgb::validate_desc(desc) != PGB_OK || !theta || !X1 || !X2 || !K || n1 < 0 || n2 < 0 || ldk < n2)
+    return PGB_EINVAL;
   if (n1 == 0 || n2 == 0) return PGB_OK;
   const pgb::Shape sh = pgb::shape_from_desc(desc);
   const size_t need = ((size_t)n1 + (size_t)n2) * (size_t)sh.Dp;

@@ -79,6 +79,9 @@ struct DagJob {
   const int* reuse;
   int reuse_mode;
   const int* active;     // when non-null and 0 the job is skipped (converged problem)
+  // test hook: (i << 16 | j) + 1 of one off-diagonal tile whose ready flag is
+  // never released, so the waits for it run out (0: none)
+  int withhold;
   // optional per-task timestamps (globaltimer ns): [task][8] = start, k-loop
   // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
   // C assembled (after the accumulator is applied)
@@ -91,6 +94,12 @@ struct DagJob {
   const void* tm_R;
   const void* tm_Linv;
 };
+
+// api.cu ----------------------------------------------------------------------
+// PGB_OK, or the error code every entry point taking a pgb_desc returns for
+// it (PGB_EINVAL for a malformed descriptor, PGB_EUNSUPPORTED for more than
+// MAX_D kernel features).
+int validate_desc(const pgb_desc* d);
 
 // Tensor map of a row-major fp32 matrix (rows x cols, row stride ld floats)
 // with 128-row x 32-column boxes and 128-byte swizzle, the layout the

@@ -62,7 +62,8 @@ __global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2
     P.da[i] = 0.0f;
   }
   if (m.y == 0) {
-    if (threadIdx.x < 8) P.status[threadIdx.x] = threadIdx.x == ST_NOTPD_COL ? INT_MAX : 0;
+    if (threadIdx.x < 8 && threadIdx.x != ST_WAIT_US)
+      P.status[threadIdx.x] = threadIdx.x == ST_NOTPD_COL ? INT_MAX : 0;
     if (threadIdx.x < 4) P.reuse[threadIdx.x] = 0;
     if (threadIdx.x == 0) *P.active = 1;
   }
@@ -183,7 +184,6 @@ __global__ void newton_finalize_kernel(const Prob* __restrict__ probs, int nprob
     if (!(err > P.tol)) status[ST_CONVERGED] = 1;
     if (err != err) atomicCAS(status + ST_CODE, 0, PGB_ENAN);
     const bool again = (err > P.tol) && (it < P.maxiter) && (status[ST_ABORT] == 0);
-    status[ST_SPARE0] = again ? 1 : 0;
     *P.active = again ? 1 : 0;
     if (again) atomicOr(any_active, 1);
   }

@@ -13,8 +13,11 @@ size, convergence flag); every round passes the objective the mask of the
 problems whose value is still needed (those in a line search), so a batched
 objective computes only those (``LaplaceBatch.set_enabled``).  The line search
 is a backtracking Armijo search (sufficient decrease c1 = 1e-4, halving);
-a non-finite value counts as no decrease, so steps that leave the domain
-(e.g. unordered cutpoints) are shortened.
+each trial step is first capped so that no coordinate moves by more than
+``max_step`` (the L-BFGS direction can be long where the curvature
+estimate is poor, and a log-parametrised coordinate moved by tens would
+overflow), and a non-finite value counts as no decrease, so steps that
+leave the domain are shortened.
 """
 
 from __future__ import annotations
@@ -35,7 +38,8 @@ class LockstepResult:
     history: list          # per evaluation round: mean f over problems
 
 
-def minimize_lockstep(fg, x0, maxiter=50, m=10, gtol=1e-5, ftol=1e-7, max_ls=12, c1=1e-4, callback=None):
+def minimize_lockstep(fg, x0, maxiter=50, m=10, gtol=1e-5, ftol=1e-7, max_ls=12, c1=1e-4, max_step=2.0,
+                      callback=None):
     """Minimise B independent smooth functions together.
 
     ``fg(X, mask)`` takes a (B, P) array and a (B,) boolean mask of the
@@ -44,7 +48,8 @@ def minimize_lockstep(fg, x0, maxiter=50, m=10, gtol=1e-5, ftol=1e-7, max_ls=12,
     at most ``gtol``, when a step lowers its value by at most ``ftol``
     relative (scipy's L-BFGS-B rule; the objective here is a float32
     computation, so the default is 1e-7), or when its line search fails.
-    Returns a :class:`LockstepResult`.
+    The first trial of each line search moves no coordinate by more than
+    ``max_step`` (None: no cap).  Returns a :class:`LockstepResult`.
     """
     x = np.array(x0, dtype=np.float64, copy=True)
     B, P = x.shape
@@ -99,8 +104,12 @@ def minimize_lockstep(fg, x0, maxiter=50, m=10, gtol=1e-5, ftol=1e-7, max_ls=12,
         bad_dir = ~(slope < 0)
         d[bad_dir] = -g[bad_dir] / np.maximum(gnorm[bad_dir, None], 1e-12)   # restart along -g
         slope = np.einsum("bp,bp->b", g, d)
-        # backtracking Armijo search, all problems in lockstep
+        # backtracking Armijo search, all problems in lockstep; the first
+        # trial moves no coordinate by more than max_step
         step = np.ones(B)
+        if max_step is not None:
+            dmax = np.abs(d).max(axis=1)
+            step = np.where(dmax > max_step, max_step / np.maximum(dmax, 1e-300), 1.0)
         searching = active.copy()
         f_new, g_new, x_new = f.copy(), g.copy(), x.copy()
         for _ in range(max_ls):
@@ -143,11 +152,17 @@ def minimize_lockstep(fg, x0, maxiter=50, m=10, gtol=1e-5, ftol=1e-7, max_ls=12,
 class LogParams:
     """Unconstrained coordinates of ordinal-probit (or Gaussian) hyperparameters.
 
-    u = (log l_1..l_nl, log s, log sigma_n, b_1 .. b_{J-1}) <-> theta = (l, s,
-    sigma_n, -inf, b_1 .. b_{J-1}, +inf): positives log-parametrised, the
-    interior cutpoints free.  ``grad_u = (x * dtheta for the logs, dtheta for
-    the cutpoints)`` by the chain rule.
+    u = (log l_1..l_nl, log s, log sigma_n, b_1, log(b_2 - b_1), ..,
+    log(b_{J-1} - b_{J-2})) <-> theta = (l, s, sigma_n, -inf, b_1 .. b_{J-1},
+    +inf): positives log-parametrised, the first interior cutpoint free and
+    each later one the previous plus a positive increment, so every u gives
+    cutpoints in increasing order (the reference's ``check_cutpoints``,
+    utilities.py:263-300, rejects any other).  Log coordinates are clipped
+    to [-80, 80] before the exponential (finite in float32).  The gradient in
+    u follows by the chain rule (``grad_u``).
     """
+
+    LOG_CLIP = 80.0
 
     def __init__(self, nl, J):
         self.nl = nl
@@ -155,20 +170,27 @@ class LogParams:
         self.P = nl + 2 + max(J - 1, 0)
 
     def to_theta(self, u):
-        u = np.atleast_2d(u)
+        u = np.atleast_2d(np.asarray(u, np.float64))
         nl, J = self.nl, self.J
-        pos = np.exp(u[:, :nl + 2])
+        pos = np.exp(np.clip(u[:, :nl + 2], -self.LOG_CLIP, self.LOG_CLIP))
         if J == 0:
             return pos
         inf = np.full((u.shape[0], 1), np.inf)
-        return np.concatenate([pos, -inf, u[:, nl + 2:], inf], axis=1)
+        if J < 2:
+            return np.concatenate([pos, -inf, inf], axis=1)
+        inc = np.exp(np.clip(u[:, nl + 3:], -self.LOG_CLIP, self.LOG_CLIP))
+        b = np.cumsum(np.concatenate([u[:, nl + 2:nl + 3], inc], axis=1), axis=1)
+        return np.concatenate([pos, -inf, b, inf], axis=1)
 
     def from_theta(self, theta):
-        theta = np.atleast_2d(theta)
+        theta = np.atleast_2d(np.asarray(theta, np.float64))
         nl, J = self.nl, self.J
         out = [np.log(theta[:, :nl + 2])]
-        if J:
-            out.append(theta[:, nl + 3:nl + 2 + J])
+        if J >= 2:
+            b = theta[:, nl + 3:nl + 2 + J]
+            if np.any(np.diff(b, axis=1) <= 0):
+                raise ValueError("interior cutpoints must be strictly increasing")
+            out += [b[:, :1], np.log(np.diff(b, axis=1))]
         return np.concatenate(out, axis=1)
 
     def grad_u(self, theta, grad_theta):
@@ -176,8 +198,13 @@ class LogParams:
         grad_theta = np.atleast_2d(grad_theta)
         nl, J = self.nl, self.J
         out = [theta[:, :nl + 2] * grad_theta[:, :nl + 2]]
-        if J:
-            out.append(grad_theta[:, nl + 3:nl + 2 + J])
+        if J >= 2:
+            gb = grad_theta[:, nl + 3:nl + 2 + J]
+            # b_k = b_1 + sum_{m < k} exp(v_m): d/db_1 = sum_k g_k,
+            # d/dv_m = exp(v_m) sum_{k > m} g_k
+            tail = np.cumsum(gb[:, ::-1], axis=1)[:, ::-1]
+            b = theta[:, nl + 3:nl + 2 + J]
+            out += [tail[:, :1], np.diff(b, axis=1) * tail[:, 1:]]
         return np.concatenate(out, axis=1)
 
 

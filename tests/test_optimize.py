@@ -71,10 +71,11 @@ def test_nonfinite_values_shorten_the_step():
 def test_logparams_roundtrip_and_chain_rule():
     lp = LogParams(nl=3, J=5)
     rng = np.random.default_rng(1)
-    u = np.concatenate([rng.normal(size=(4, 5)), np.sort(rng.normal(size=(4, 4)), axis=1)], axis=1)
+    u = rng.normal(size=(4, 9))          # any u: the cutpoints come out ordered
     th = lp.to_theta(u)
     assert th.shape == (4, 3 + 2 + 6)
     assert np.isneginf(th[:, 5]).all() and np.isposinf(th[:, -1]).all()
+    assert (np.diff(th[:, 6:10], axis=1) > 0).all()
     assert np.allclose(lp.from_theta(th), u)
     # d/du of h(theta(u)) for h(theta) = sum(w * finite theta) by central differences
     w = rng.normal(size=th.shape[1])
@@ -89,3 +90,41 @@ def test_logparams_roundtrip_and_chain_rule():
     eps = 1e-6
     fd = np.array([(h(u[:1] + eps * np.eye(9)[k]) - h(u[:1] - eps * np.eye(9)[k])) / (2 * eps) for k in range(9)])
     assert np.allclose(gu, fd, rtol=1e-6, atol=1e-8)
+
+
+def test_logparams_binary_and_extreme_coordinates():
+    lp = LogParams(nl=1, J=2)
+    th = lp.to_theta(np.array([[0.1, -0.2, 0.3, 0.7]]))
+    assert th.shape == (1, 1 + 2 + 3) and th[0, 4] == 0.7
+    with np.errstate(over="raise", invalid="raise"):
+        big = LogParams(nl=1, J=5).to_theta(np.array([[500.0, -500.0, 90.0, 1.0, 200.0, -300.0, 0.0]]))
+    assert np.isfinite(big[:, :3]).all() and np.isfinite(big[:, 4:8]).all()
+    assert np.isfinite(big.astype(np.float32)[:, :3]).all()
+    with pytest.raises(ValueError):
+        LogParams(nl=1, J=4).from_theta(np.array([[1.0, 1.0, 1.0, -np.inf, 0.5, 0.2, 0.9, np.inf]]))
+
+
+def test_trial_steps_are_capped():
+    """A long L-BFGS direction (a shallow slope beside a steep valley) moves
+    no coordinate by more than max_step from the point its line search
+    starts at, on any trial."""
+    log = []
+
+    def fg(X, mask=None):
+        log.append(("eval", X.copy()))
+        f = 1e-4 * X[:, 0] + 0.5 * X[:, 1] ** 2
+        return f, np.stack([np.full(X.shape[0], 1e-4), X[:, 1]], axis=1)
+
+    x0 = np.array([[0.0, 1e-3]])
+    minimize_lockstep(fg, x0, maxiter=6, max_step=0.5, ftol=0.0, gtol=0.0,
+                      callback=lambda x, f, g: log.append(("acc", x.copy())))
+    base, trials = x0, 0
+    for kind, x in log[1:]:
+        if kind == "acc":
+            base = x
+        else:
+            assert np.abs(x - base).max() <= 0.5 + 1e-12
+            trials += 1
+    assert trials >= 6
+    # without the cap the first direction (gamma = 1 / ||g||) would move ~1
+    assert np.abs(log[1][1] - x0).max() == pytest.approx(0.5)
