@@ -299,10 +299,12 @@ int upload_maps(Engine& e) {
   for (int p = 0; p < e.nprob; ++p) {
     const Prob& q = e.hp[p];
     unsigned char* m = h.data() + (size_t)p * MAPS_PER_PROB * 128;
-    bool ok = make_tile_map(m + MAP_L * 128, q.L, q.n_pad, q.ld, q.ld) &&
-              make_tile_map(m + MAP_LINV * 128, q.Linv, (long long)q.nt * T, T, T) &&
-              make_tile_map(m + MAP_RV * 128, q.Rv, T, q.ld, q.ld);
-    if (ok && q.Rz) ok = make_tile_map(m + MAP_RZ * 128, q.Rz, q.n_pad, q.ld, q.ld);
+    // the tensor cores read the TF32 hi/lo splits (2 ld columns per row)
+    const long long lds = 2 * q.ld;
+    bool ok = make_tile_map(m + MAP_L * 128, q.Ls, q.n_pad, lds, lds) &&
+              make_tile_map(m + MAP_LINV * 128, q.Linvs, (long long)q.nt * T, 2 * T, 2 * T) &&
+              make_tile_map(m + MAP_RV * 128, q.Rvs, T, lds, lds);
+    if (ok && q.Rz) ok = make_tile_map(m + MAP_RZ * 128, q.Rz, q.n_pad, lds, lds);
     if (!ok) return PGB_ECUDA;
   }
   return h2d(e.maps_all, h.data(), h.size(), e.cap_s);
@@ -357,6 +359,9 @@ size_t layout(Engine& e, uintptr_t base) {
     q.L = b.take<float>(npad * ld);
     q.Linv = b.take<float>((size_t)nt * T * T);
     q.Rv = b.take<float>((size_t)T * ld);
+    q.Ls = b.take<float>(npad * 2 * ld);
+    q.Linvs = b.take<float>((size_t)nt * T * 2 * T);
+    q.Rvs = b.take<float>((size_t)T * 2 * ld);
     float** vecs[] = {&q.a,    &q.f,    &q.d1, &q.W,    &q.sw, &q.r,  &q.t, &q.x, &q.logp, &q.d3,
                       &q.dsig, &q.svec, &q.rv, &q.zbar, &q.tz, &q.y2, &q.u, &q.c, &q.rowdot, &q.sw_prev, &q.da};
     for (float** v : vecs) *v = b.take<float>(npad);
@@ -386,6 +391,8 @@ size_t layout(Engine& e, uintptr_t base) {
       j.near = e.near[p];
       j.L = q.L;
       j.Linv = q.Linv;
+      j.Ls = q.Ls;
+      j.Linvs = q.Linvs;
       j.Xf = q.Xf;
       j.sw = q.sw;
       j.theta = q.theta;
@@ -404,6 +411,7 @@ size_t layout(Engine& e, uintptr_t base) {
     jb[JOB_VEC].nrt = 1;
     jb[JOB_VEC].nrhs = 1;
     jb[JOB_VEC].R = q.Rv;
+    jb[JOB_VEC].Rs = q.Rvs;
     jb[JOB_VEC].rhs_vec = q.t;
     jb[JOB_VEC].reuse_mode = 2;
     jb[JOB_VEC].active = q.active;
@@ -642,7 +650,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
 int ensure_grad_buffers(Engine& e) {
   if (e.grad_ready) return PGB_OK;
   size_t total = 0;
-  for (int p = 0; p < e.nprob; ++p) total += 2 * (((size_t)e.hp[p].n_pad * e.hp[p].ld * sizeof(float) + 255) & ~(size_t)255);
+  for (int p = 0; p < e.nprob; ++p) total += 3 * (((size_t)e.hp[p].n_pad * e.hp[p].ld * sizeof(float) + 255) & ~(size_t)255);
   PGB_TRY(ws_alloc(e.cap_s, &e.garena, total));
   CU_TRY(cudaMemsetAsync(e.garena, 0, total, e.cap_s));
   CU_TRY(cudaStreamSynchronize(e.cap_s));
@@ -650,9 +658,10 @@ int ensure_grad_buffers(Engine& e) {
   b.base = reinterpret_cast<uintptr_t>(e.garena);
   for (int p = 0; p < e.nprob; ++p) {
     const size_t mat = (size_t)e.hp[p].n_pad * e.hp[p].ld;
-    e.hp[p].Rz = b.take<float>(mat);
+    e.hp[p].Rz = b.take<float>(2 * mat);   // split only: L^-T is read by the tensor cores alone
     e.hp[p].Binv = b.take<float>(mat);
-    e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].R = e.hp[p].Rz;
+    e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].R = nullptr;
+    e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].Rs = e.hp[p].Rz;
   }
   PGB_TRY(upload_maps(e));
   PGB_TRY(engine_upload_tables(e));
@@ -927,7 +936,7 @@ void status_from_words(const int* h, pgb_status* out) {
 struct pgb_gp {
   Engine e;
   // predict workspace (grown on demand)
-  float* Rc = nullptr;
+  float* Rc = nullptr;     // split of the solved cross-kernel rows (mpad x 2 ld)
   float* rowsq = nullptr;
   float* Xq = nullptr;
   float* Xq_in = nullptr;
@@ -1208,7 +1217,9 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
     gp->ready_c = nullptr;
     gp->cap_c = 0;
     auto grab = [&e](void** p, size_t bytes) { return ws_alloc(e.cap_s, p, bytes); };
-    PGB_TRY(grab(reinterpret_cast<void**>(&gp->Rc), sizeof(float) * (size_t)mpad * q.ld));
+    // split only (2 ld columns): the solved rows are read back by the tensor
+    // cores alone (later right-hand-side tiles, the covariance product)
+    PGB_TRY(grab(reinterpret_cast<void**>(&gp->Rc), sizeof(float) * (size_t)mpad * 2 * q.ld));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->rowsq), sizeof(float) * (size_t)mpad * nt));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq), sizeof(float) * (size_t)mpad * sh.Dp));
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->Xq_in), sizeof(float) * (size_t)mpad * sh.D));
@@ -1216,7 +1227,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
     PGB_TRY(grab(reinterpret_cast<void**>(&gp->mv_ws), sizeof(float) * 2 * (size_t)mpad));
     if (!gp->map_c) PGB_TRY(grab(&gp->map_c, 128));
     alignas(64) unsigned char m[128];
-    if (!make_tile_map(m, gp->Rc, mpad, q.ld, q.ld)) return PGB_ECUDA;
+    if (!make_tile_map(m, gp->Rc, mpad, 2 * q.ld, 2 * q.ld)) return PGB_ECUDA;
     PGB_TRY(h2d(gp->map_c, m, sizeof(m), e.cap_s));
     gp->cap_c = mpad;
   }
@@ -1249,7 +1260,8 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
     DagJob jb = e.hjobs[JOB_CROSS];
     jb.nrt = mt;
     jb.nrhs = m;
-    jb.R = gp->Rc;
+    jb.R = nullptr;
+    jb.Rs = gp->Rc;
     jb.Xq = gp->Xq;
     jb.rowsq = gp->rowsq;
     jb.ready = gp->ready_c;
@@ -1442,6 +1454,7 @@ void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
                         {"logp", q.logp},   {"grad", q.grad},   {"err", q.err},     {"value", q.value},
                         {"reuse", q.reuse}, {"trace", gp->e.trace},
                         {"tasks_none", gp->e.tasks[JOB_NONE]},
+                        {"tasks_ident", gp->e.tasks[JOB_IDENT]},
                         {"ptrace", gp->e.hjobs[JOB_NONE].ptrace}};
   for (const Item& it : items)
     if (std::strcmp(it.n, name) == 0) return const_cast<void*>(it.p);

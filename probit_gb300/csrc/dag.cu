@@ -27,25 +27,28 @@ namespace pgb {
 
 constexpr int DAG_THREADS = 256;
 constexpr int SC_LD = T + 1;
-// tensor-core pipeline, unioned with the epilogue tiles sC, sL: NST stages
-// of (A, B) 128 x 32 fp32 chunks (16 KB each) that the tensor loads fill
-// and the split turns into their TF32 hi parts in place, and NLO slots of
-// the (A_lo, B_lo) parts.  A stage is reloaded once the MMAs of its chunk
-// completed, a lo slot rewritten once the MMAs of the chunk NLO before.
-constexpr int NST = 4;
-constexpr int NLO = 2;
+// tensor-core pipeline, unioned with the epilogue tiles sC, sL: NST stages,
+// each one 32-column chunk of the A and B operands as their TF32 hi and lo
+// parts (four 128 x 32 fp32 boxes, 16 KB each), loaded straight from the
+// split operand matrices (the epilogue that publishes a tile also writes its
+// split).  A stage is reloaded once the MMAs of its chunk completed.
+constexpr int NST = 3;
 constexpr int CHUNK_BYTES = T * 128;             // 128 rows x 32 fp32
-constexpr int STAGE_BYTES = 2 * CHUNK_BYTES;     // A(hi), B(hi)
-constexpr int LO_BYTES = 2 * CHUNK_BYTES;        // A_lo, B_lo
-constexpr int LO_OFF = NST * STAGE_BYTES;
-constexpr int UNION_BYTES = LO_OFF + NLO * LO_BYTES;   // >= 2 * T * SC_LD * 4
-constexpr int NBARS = 3 * NST + NLO + 1;         // full, empty, split [NST], lofree [NLO], acc
-// tensor memory: the 128 x 128 fp32 accumulator in columns 0..127, then NLO
-// slots of the A operand's (hi, lo) parts, 64 columns each
-constexpr uint32_t A_COL = 128;
-constexpr uint32_t TMEM_COLS = 256;
+constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;     // A hi, A lo, B hi, B lo
+constexpr int UNION_BYTES = NST * STAGE_BYTES;   // >= 2 * T * SC_LD * 4
+constexpr int CHUNKS_PER_KT = T / 32;            // chunks of one 128-wide k-tile
+constexpr int CHUNKS_PER_PART = 2;               // chunks summed in one partial accumulator
+constexpr int DRAIN_WARPS = DAG_THREADS / 32 - 2;   // warps 2..7 fold the partial sums
+constexpr int NBARS = 2 * NST + 4;               // full, empty [NST]; part full, part free [2]
+// tensor memory: the running 128 x 128 fp32 sum in columns 0..127 and two
+// partial accumulators (CHUNKS_PER_PART chunks each) in 128..255, 256..383
+constexpr uint32_t RUN_COL = 0;
+constexpr uint32_t PART_COL = 128;
+constexpr uint32_t TMEM_COLS = 512;
 constexpr size_t DAG_SMEM = UNION_BYTES + (2 * T * 17 + 2 * T) * 4 + 1024 + 64;
 static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
+static_assert(DAG_SMEM <= 232448, "dynamic shared memory above the 227 KB a block may use");
+static_assert(CHUNKS_PER_KT % CHUNKS_PER_PART == 0, "a k-tile is a whole number of partials");
 constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
 constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 
@@ -170,25 +173,44 @@ __device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, con
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// 32 x 32 Cholesky of the lower triangle of the block at A (row stride
-// SC_LD) by one warp: lane l holds row l in registers.  Column C: the pivot
-// from lane C by shuffle; every lane scales its entry by the pivot's
-// reciprocal square root and puts it in a 32-float line of shared memory at
-// position (l - C) mod 32, so that the later columns' multipliers sit at
-// fixed positions 1..31 and come back as eight 16-byte broadcast loads; then
-// every lane updates its later entries.  Entries above the diagonal are
+// Barrier over the first `count` threads of the block (a multiple of 32),
+// named barrier 1 (__syncthreads uses 0).
+__device__ __forceinline__ void bar_sync_first(int count) {
+  asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
+}
+
+// Cholesky of one 32-wide panel of the tile in sC (row stride SC_LD): the
+// rows jb..127 of columns jb..jb+31, whose trailing updates are applied.
+// Thread t < nr = 128 - jb holds row jb + t in registers.  Column C: the
+// warp of the diagonal block (threads 0..31) takes the pivot from lane C by
+// shuffle, scales its entries by the pivot's reciprocal square root and puts
+// them in a 32-float line of shared memory at position (lane - C) mod 32, so
+// the multipliers L[jb+C+m][C] sit at positions m = 1..31 and come back as
+// eight 16-byte broadcast loads, and the reciprocal square root beside it;
+// one barrier over the panel's warps; every row below the diagonal block
+// then scales its own entry, and every row updates its later entries with
+// the multipliers.  So the rows below are solved in the same column loop
+// instead of by a substitution after it.  Entries above the diagonal are
 // updated too (no per-entry predicate) and never written back.  The line is
-// double-buffered by column parity, so one __syncwarp per column orders the
-// store before the loads.  Every 4 columns the row is shifted left by 4
-// registers: the column loop stays a small loop (a fully unrolled version is
-// ~20 KB of straight-line code that runs at instruction-fetch latency inside
-// the factorisation kernel) while every register index is a compile-time
-// constant.  The final L is written back as each column completes;
-// srd[l] = 1 / L[l][l].  sbuf: 64 floats, 16-byte aligned.
-__device__ __forceinline__ void warp_potrf32(float* A, float* srd, float* sbuf, int lane, int col0, int* status) {
+// double-buffered by column parity: the barrier of column C orders its
+// store before the loads, and the loads of column C before the store of
+// column C + 2 (every warp passes barrier C + 1 after its loads of C).
+// Every 4 columns the row is shifted left by 4 registers, so the column loop
+// stays a small loop (a fully unrolled one is ~20 KB of straight-line code
+// that runs at instruction-fetch latency inside the factorisation kernel)
+// while every register index is a compile-time constant.  Each L entry is
+// written back to sC as its column completes.  sbuf: 96 floats, 16-byte
+// aligned (two lines, then 32 reciprocal square roots).
+__device__ __forceinline__ void panel_potrf(float* sC, int jb, float* sbuf, int col0, int* status) {
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int nr = T - jb;
+  if (tid >= nr) return;
+  const bool dwarp = tid < 32;
+  float* row = sC + (jb + tid) * SC_LD + jb;
+  float* srl = sbuf + 64;
   float d[32];
 #pragma unroll
-  for (int m = 0; m < 32; ++m) d[m] = A[lane * SC_LD + m];
+  for (int m = 0; m < 32; ++m) d[m] = row[m];
   int bad = -1;
 #pragma unroll 1
   for (int C0 = 0; C0 < 32; C0 += 4) {
@@ -196,13 +218,21 @@ __device__ __forceinline__ void warp_potrf32(float* A, float* srd, float* sbuf, 
     for (int k = 0; k < 4; ++k) {
       const int C = C0 + k;
       float* line = sbuf + 32 * (k & 1);
-      const float piv = __shfl_sync(FULL, d[k], C);
-      if (!(piv > 0.0f) && bad < 0) bad = C;
-      const float rl = rsqrtf(piv);
-      const float dc = (lane == C) ? piv * rl : d[k] * rl;
-      if (lane >= C) A[lane * SC_LD + C] = dc;
-      line[(lane - C) & 31] = dc;
-      __syncwarp();
+      float dc;
+      if (dwarp) {
+        const float piv = __shfl_sync(FULL, d[k], C);
+        if (!(piv > 0.0f) && bad < 0) bad = C;
+        const float rl = rsqrtf(piv);
+        dc = (lane == C) ? piv * rl : d[k] * rl;
+        if (lane >= C) row[C] = dc;
+        line[(lane - C) & 31] = dc;
+        if (lane == C) srl[C] = rl;
+        bar_sync_first(nr);
+      } else {
+        bar_sync_first(nr);
+        dc = d[k] * srl[C];
+        row[C] = dc;
+      }
 #pragma unroll
       for (int q = 0; q < 8; ++q) {
         const float4 v = reinterpret_cast<const float4*>(line)[q];
@@ -217,9 +247,7 @@ __device__ __forceinline__ void warp_potrf32(float* A, float* srd, float* sbuf, 
 #pragma unroll
     for (int m = 0; m < 28; ++m) d[m] = d[m + 4];
   }
-  __syncwarp();
-  srd[lane] = __frcp_rn(A[lane * SC_LD + lane]);
-  if (lane == 0 && bad >= 0) {
+  if (tid == 0 && bad >= 0) {
     atomicMin(status + ST_NOTPD_COL, col0 + bad);
     atomicCAS(status + ST_CODE, 0, PGB_ENOTPD);
   }
@@ -251,43 +279,51 @@ __device__ __forceinline__ void subst32_row(float* xs, const float* Lb, const fl
 }
 
 // In-place Cholesky of the lower triangle of the 128 x 128 tile in sC:
-// 32-wide panels; warp 0 factors the diagonal block, one thread per row
-// solves the panel below (L rows broadcast from shared memory, reciprocal
-// pivots in srd), 4 x 4 register blocks update the trailing lower triangle.
-// Panel p of the factor (columns 32p .. 32p+31) is final once its diagonal
-// block and the rows below are solved; it is then written to dst (row stride
-// ld; zeros above the diagonal) and `progress` is released to p + 1, so the
-// tiles below can start their substitution with it while the later panels
-// are factored.  The block's writes precede thread 0's release store through
-// the barrier, and the release orders them for whoever acquires the count.
-__device__ __forceinline__ void publish_panel(const float* sC, float* dst, long long ld, int* progress, int jb) {
+// 32-wide panels (panel_potrf: all rows of the panel in one column loop),
+// 4 x 4 register blocks update the trailing lower triangle.  Panel p of the
+// factor (columns 32p .. 32p+31) is final once its column loop is done; it
+// is then written to dst (row stride ld; zeros above the diagonal) and
+// `progress` is released to p + 1, so the tiles below can start their
+// substitution with it while the later panels are factored.  The block's
+// writes precede thread 0's release store through the barrier, and the
+// release orders them for whoever acquires the count.
+//
+// Panel jb of the tile goes to dst in fp32 (row stride ld) for the
+// substitutions and solves and, when dsts is given, as its TF32 hi/lo split
+// (the tile's hi columns in the split matrix, row stride lds) for the
+// tensor-core loads; then progress is released to jb / 32 + 1.
+__device__ __forceinline__ void publish_panel(const float* sC, float* dst, long long ld, float* dsts, long long lds,
+                                              int* progress, int jb) {
   for (int e = threadIdx.x; e < T * 32; e += DAG_THREADS) {
     const int r = e >> 5, c = jb + (e & 31);
-    dst[(size_t)r * ld + c] = c <= r ? sC[r * SC_LD + c] : 0.0f;
+    const float x = c <= r ? sC[r * SC_LD + c] : 0.0f;
+    dst[(size_t)r * ld + c] = x;
+    if (dsts) put_split(dsts + (size_t)r * lds + c, x);
   }
   __syncthreads();
   if (threadIdx.x == 0) st_release(progress, jb / 32 + 1);
 }
 
-__device__ void potrf_tile(float* sC, float* srd, int col0, int* status, float* dst, long long ld, int* progress,
-                           unsigned long long* pt = nullptr) {
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+__device__ void potrf_tile(float* sC, float* sbuf, int col0, int* status, float* dst, long long ld, float* dsts,
+                           long long lds, int* progress, unsigned long long* pt = nullptr) {
+  const int tid = threadIdx.x;
   for (int jb = 0; jb < T; jb += 32) {
     if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
-    if (warp == 0) warp_potrf32(sC + jb * SC_LD + jb, srd, srd + T, lane, col0 + jb, status);
+    panel_potrf(sC, jb, sbuf, col0 + jb, status);
     __syncthreads();
     if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
+    publish_panel(sC, dst, ld, dsts, lds, progress, jb);
+    if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
     const int rem = T - jb - 32;
-    if (rem <= 0) publish_panel(sC, dst, ld, progress, jb);
     if (rem > 0) {
-      if (tid < rem) subst32_row(sC + (jb + 32 + tid) * SC_LD + jb, sC + jb * SC_LD + jb, srd);
-      __syncthreads();
-      publish_panel(sC, dst, ld, progress, jb);
-      if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
+      // trailing update of the lower triangle of rows/columns jb+32.. by
+      // 4 x 4 register blocks, lower-triangle blocks only
       const int nb = rem / 4;
-      for (int blk = tid; blk < nb * nb; blk += DAG_THREADS) {
-        const int br = blk / nb, bc = blk % nb;
-        if (bc > br) continue;
+      for (int blk = tid; blk < nb * (nb + 1) / 2; blk += DAG_THREADS) {
+        int br = (int)((sqrtf(8.0f * blk + 1.0f) - 1.0f) * 0.5f);
+        while (br * (br + 1) / 2 > blk) --br;
+        while ((br + 1) * (br + 2) / 2 <= blk) ++br;
+        const int bc = blk - br * (br + 1) / 2;
         const int r0 = jb + 32 + br * 4, c0 = jb + 32 + bc * 4;
         float acc[4][4];
 #pragma unroll
@@ -387,21 +423,20 @@ __device__ __forceinline__ bool block_wait(const int* flag, int* status, int* s_
 
 // Per-block tensor-core state, uniform across the block.
 struct TcCtx {
-  uint32_t tmem;       // accumulator: 128 lanes x 128 fp32 columns
-  uint32_t g;          // chunks loaded so far by this block (stage g % NST, lo slot g % NLO)
-  uint32_t ntask;      // accumulator commits waited so far
+  uint32_t tmem;       // running sum in columns RUN_COL.., partial accumulators at PART_COL + 128 pb
+  uint32_t g;          // chunks loaded so far by this block (stage g % NST)
+  uint32_t kt;         // partials accumulated so far by this block (partial kt % 2)
   uint8_t* stages;     // 1024-aligned stage buffers (unioned with sC, sL)
   uint64_t* full;      // [NST] the stage's tensor loads landed
   uint64_t* empty;     // [NST] the MMAs that read the stage completed
-  uint64_t* split;     // [NST] the stage's chunk is split (one arrival per splitting warp)
-  uint64_t* lofree;    // [NLO] the MMAs that read the lo slot completed
-  uint64_t* acc;       // every MMA issued so far completed
+  uint64_t* pfull;     // [2] the MMAs summed in the partial completed
+  uint64_t* pfree;     // [2] the partial was added to the running sum (one arrival per drain warp)
 };
 
 // Operands of one accumulation acc += sum_{k0 <= k < k1} A_k B_k^T: A_k is
-// the 128 x 128 tile of the `amap` matrix at rows arow.., columns acol +
-// k*T.., B_k likewise.  Chunk c (32 columns) of the loop is k-tile
-// k0 + c / 4, columns (c % 4) * 32.
+// the 128 x 128 tile of the split matrix behind `amap` at rows arow..,
+// logical columns acol + k*T.., B_k likewise.  Chunk c (32 columns) of the
+// loop is k-tile k0 + c / 4, columns (c % 4) * 32.
 struct TcLoad {
   const void* amap;
   const void* bmap;
@@ -424,7 +459,7 @@ __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, 
   l.brow = brow;
   l.bcol = bcol;
   l.k0 = k0;
-  l.nchunks = (k1 - k0) * (T / 32);
+  l.nchunks = (k1 - k0) * CHUNKS_PER_KT;
   l.base = tc.g;
   l.issued = 0;
   l.ok = 1;
@@ -433,29 +468,32 @@ __device__ __forceinline__ TcLoad tc_load(const void* amap, int arow, int acol, 
   return l;
 }
 
-// Thread 0: issue the loads of chunk `c` into its stage, after the MMAs of
-// the stage's previous chunk completed and, at a k-tile boundary (every chunk
-// of the k-tile l.kfine), after the dependencies were published
-// (wait_tile(k-tile, chunk within it)).  A dependency wait that
-// gives up still issues the loads (the addresses are valid; the result is
-// discarded), so the stage accounting stays consistent.  False if a
-// pipeline wait timed out.
+// Thread 0 or 32: issue the loads of chunk `c` (A hi, A lo, B hi, B lo) into
+// its stage, after the MMAs of the stage's previous chunk completed and, at
+// a k-tile boundary (every chunk of the k-tile l.kfine), after the
+// dependencies were published (wait_tile(k-tile, chunk within it)).  A
+// dependency wait that gives up still issues the loads (the addresses are
+// valid; the result is discarded), so the stage accounting stays
+// consistent.  False if a pipeline wait timed out.
 template <class WaitTile>
 __device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, WaitTile& wait_tile) {
   const uint32_t g = l.base + (uint32_t)c;
   const uint32_t s = g % NST;
   if (g >= NST && !mbar_wait_bounded(tc.empty + s, ((g / NST) - 1u) & 1u, MMA_WAIT_NS)) return false;
-  const int kt = l.k0 + c / (T / 32), q = c % (T / 32);
+  const int kt = l.k0 + c / CHUNKS_PER_KT, q = c % CHUNKS_PER_KT;
   if (q == 0 || kt == l.kfine) {
     if (!wait_tile(kt, q)) l.ok = 0;
     fence_proxy_async_global();
-    if (l.kt && c == l.nchunks - (T / 32)) l.kt[0] = global_ns();
+    if (l.kt && c == l.nchunks - CHUNKS_PER_KT) l.kt[0] = global_ns();
   }
-  const int col = (l.k0 + c / (T / 32)) * T + (c % (T / 32)) * 32;
+  const int col = kt * T + q * 32;
+  const int ax = split_col(l.acol + col), bx = split_col(l.bcol + col);
   uint8_t* stage = tc.stages + s * STAGE_BYTES;
-  mbar_arrive_expect_tx(tc.full + s, 2 * CHUNK_BYTES);
-  tma_load_2d(stage, l.amap, l.acol + col, l.arow, tc.full + s);
-  tma_load_2d(stage + CHUNK_BYTES, l.bmap, l.bcol + col, l.brow, tc.full + s);
+  mbar_arrive_expect_tx(tc.full + s, 4 * CHUNK_BYTES);
+  tma_load_2d(stage, l.amap, ax, l.arow, tc.full + s);
+  tma_load_2d(stage + CHUNK_BYTES, l.amap, ax + T, l.arow, tc.full + s);
+  tma_load_2d(stage + 2 * CHUNK_BYTES, l.bmap, bx, l.brow, tc.full + s);
+  tma_load_2d(stage + 3 * CHUNK_BYTES, l.bmap, bx + T, l.brow, tc.full + s);
   l.issued = c + 1;
   return true;
 }
@@ -469,143 +507,88 @@ __device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& w
   return true;
 }
 
-// Split the fp32 A and B chunks the loads left in a stage into their TF32
-// hi and lo parts (round to nearest), by warps 2..7.  A goes to tensor
-// memory (the MMAs read it from there: `a_col` = hi in columns a_col ..
-// a_col + 31, lo in a_col + 32 .. +63, lane = row), so it costs no shared
-// memory traffic beyond one read; warp w may only write lanes 32 (w % 4) ..
-// +31, so warps 4, 5 take all 32 columns of their rows and warps 2, 6 and
-// 3, 7 half each.  B: hi in place, lo to the lo slot; a quarter of it on
-// each of the four SM sub-partitions (warp w runs on sub-partition w % 4):
-// warps 4 and 5 a quarter each, warps 2, 6, 3, 7 an eighth each, so the
-// shared-memory work of every sub-partition is the same.  The 128-byte
-// swizzle is the same for every part, so the split is element by element.
-constexpr int SPLIT_WARPS = DAG_THREADS / 32 - 2;
-__device__ __forceinline__ void split_a_cols(const uint8_t* stage, int r, int u0, int nu, float (&h)[32],
-                                             float (&o)[32]) {
-  // row r of the swizzled chunk: 16-byte unit u at position u ^ (r % 8)
-  const uint8_t* rowp = stage + r * 128;
+// Thread 0: the 12 MMAs of one 32-wide k-chunk into the partial accumulator
+// at tensor-memory column `part`, 4 k-steps x (hi lo, lo hi, hi hi), the
+// small terms first so they are not lost against the large one (a fourth
+// product lo lo changed no measured error).  Both operands come from the
+// stage in shared memory.
+__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, uint32_t part, bool first) {
+  const uint32_t a_hi = smem_u32(stage), a_lo = a_hi + CHUNK_BYTES;
+  const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
+  const uint32_t d = tc.tmem + part;
 #pragma unroll
-  for (int u = 0; u < 8; ++u) {
-    if (u < nu) {
-      const float4 x = *reinterpret_cast<const float4*>(rowp + (((u0 + u) ^ (r & 7)) << 4));
-      split_tf32(x.x, h[4 * u + 0], o[4 * u + 0]);
-      split_tf32(x.y, h[4 * u + 1], o[4 * u + 1]);
-      split_tf32(x.z, h[4 * u + 2], o[4 * u + 2]);
-      split_tf32(x.w, h[4 * u + 3], o[4 * u + 3]);
-    }
+  for (int ks = 0; ks < 4; ++ks) {
+    const uint32_t o = ks * 32;   // bytes into the swizzled rows
+    umma_tf32(d, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
+    umma_tf32(d, sdesc_sw128(a_lo + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+    umma_tf32(d, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
   }
 }
 
-__device__ __forceinline__ void convert_stage(const TcCtx& tc, uint8_t* stage, uint8_t* lo, uint32_t a_col) {
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int qd = warp & 3;
-  const int r = 32 * qd + lane;
-  const uint32_t lanes = (uint32_t)(32 * qd) << 16;
-  float h[32], o[32];
-  int b0, nb;   // this warp's float4 of B: b0 + lane + 32 q, q < nb
-  if (warp == 4 || warp == 5) {
-    split_a_cols(stage, r, 0, 8, h, o);
-    tmem_st_32x32(tc.tmem + lanes + a_col, h);
-    tmem_st_32x32(tc.tmem + lanes + a_col + 32, o);
-    b0 = (warp - 4) * 256;
-    nb = 8;
-  } else {
-    const int half = warp >= 6 ? 1 : 0;
-    split_a_cols(stage, r, 4 * half, 4, h, o);
-    float h16[16], o16[16];
+// Warps 2..7: add the partial accumulator at tensor-memory column `part`
+// to the running sum (or copy it there), each warp its 32-lane quarter of
+// the rows (warp w may only reach lanes 32 (w % 4) ..): warps 4 and 5 all
+// 128 columns of quarters 0 and 1, warps 2, 6 and 3, 7 half each of
+// quarters 2 and 3.  The addition is an ordinary fp32 add (round to
+// nearest); the tensor core's own accumulation rounds relative to the
+// accumulator's magnitude with a bias, which grows with the number of MMAs
+// summed into one accumulator (measured: a relative bias of the diagonal of
+// L rising to 2e-5 over 64 tile columns when a whole k-range accumulated in
+// place; -1.1e-6 of a 8192-long sum of positive products with one 128-wide
+// k-tile per partial), so each partial holds CHUNKS_PER_PART chunks.
+__device__ __forceinline__ void fold_partial(const TcCtx& tc, uint32_t part, bool copy) {
+  const int warp = threadIdx.x >> 5;
+  const uint32_t lanes = (uint32_t)(32 * (warp & 3)) << 16;
+  const int c0 = (warp == 4 || warp == 5) ? 0 : (warp >= 6 ? 64 : 0);
+  const int nc = (warp == 4 || warp == 5) ? 128 : 64;
+  for (int c = c0; c < c0 + nc; c += 32) {
+    float pv[32];
+    tmem_ld_32x32(tc.tmem + lanes + part + (uint32_t)c, pv);
+    if (!copy) {
+      float rv[32];
+      tmem_ld_32x32(tc.tmem + lanes + RUN_COL + (uint32_t)c, rv);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) {
-      h16[k] = h[k];
-      o16[k] = o[k];
+      for (int q = 0; q < 32; ++q) pv[q] += rv[q];
     }
-    tmem_st_32x32_x16(tc.tmem + lanes + a_col + 16 * half, h16);
-    tmem_st_32x32_x16(tc.tmem + lanes + a_col + 32 + 16 * half, o16);
-    b0 = 512 + (2 * (warp & 1) + half) * 128;
-    nb = 4;
-  }
-  float4* bh = reinterpret_cast<float4*>(stage + CHUNK_BYTES);
-  float4* bl = reinterpret_cast<float4*>(lo + CHUNK_BYTES);
-  float4 b[8];
-#pragma unroll
-  for (int q = 0; q < 8; ++q)
-    if (q < nb) b[q] = bh[b0 + lane + 32 * q];
-#pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    if (q < nb) {
-      float4 hh, oo;
-      split_tf32(b[q].x, hh.x, oo.x);
-      split_tf32(b[q].y, hh.y, oo.y);
-      split_tf32(b[q].z, hh.z, oo.z);
-      split_tf32(b[q].w, hh.w, oo.w);
-      bh[b0 + lane + 32 * q] = hh;
-      bl[b0 + lane + 32 * q] = oo;
-    }
+    tmem_st_32x32(tc.tmem + lanes + RUN_COL + (uint32_t)c, pv);
   }
   tmem_wait_st();
 }
 
-// Thread 0: the 12 MMAs of one 32-wide k-chunk, 4 k-steps x (hi lo, lo hi,
-// hi hi), the small terms first so they are not lost against the large one
-// (a fourth product lo lo changed no measured error).
-__device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stage, const uint8_t* lo, uint32_t a_col,
-                                            bool first) {
-  const uint32_t b_hi = smem_u32(stage) + CHUNK_BYTES, b_lo = smem_u32(lo) + CHUNK_BYTES;
-  const uint32_t a_hi = tc.tmem + a_col, a_lo = a_hi + 32;
-#pragma unroll
-  for (int ks = 0; ks < 4; ++ks) {
-    const uint32_t o = ks * 32;   // bytes into the swizzled B rows
-    const uint32_t ka = ks * 8;   // tensor-memory columns of A
-    umma_tf32_ts(tc.tmem, a_hi + ka, sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
-    umma_tf32_ts(tc.tmem, a_lo + ka, sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
-    umma_tf32_ts(tc.tmem, a_hi + ka, sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
-  }
-}
-
-// Wait (bounded) until every MMA this block issued has completed.
-__device__ bool tc_drain(TcCtx& tc, int* status) {
-  __syncthreads();
-  if (threadIdx.x == 0) umma_commit(tc.acc);
-  const bool ok = mbar_wait_bounded(tc.acc, tc.ntask & 1u, MMA_WAIT_NS);
-  tc.ntask++;
-  if (!ok && threadIdx.x == 0) {
-    atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
-    atomicExch(status + ST_ABORT, 1);
-  }
-  tc_fence_after();
-  __syncthreads();
-  return ok;
-}
-
-// acc (TMEM) += sum_k A_k B_k^T in 3xTF32 (acc starts from zero unless
-// `preloaded`).  Thread 0 must have called tc_start on `l`, and every thread
-// must have fenced its earlier generic writes to the stage buffers
-// (fence_proxy_async_smem) before the barrier that preceded it.  Three
-// roles: thread 32 issues the loads of each chunk as soon as the MMAs that
-// read its stage have completed (and its dependencies are published); warps
-// 2..7 split each chunk as soon as its loads land and signal the stage's
-// split barrier; thread 0 waits for that signal and issues the chunk's MMAs.
-// So loads, splits and MMAs of consecutive chunks overlap.  Every wait is bounded and every
-// loop runs to the end, so each warp takes the same number of steps; false
-// when a dependency wait gave up or a pipeline wait timed out (the problem
-// is then aborted and the accumulator is garbage).
+// The running sum (TMEM columns RUN_COL..) += sum_k A_k B_k^T in 3xTF32; it
+// starts from zero unless `preloaded` (e.g. with -C_init).  Thread 0 must
+// have called tc_start on `l`, and every thread must have fenced its earlier
+// generic writes to the stage buffers (fence_proxy_async_smem) before the
+// barrier that preceded it.  Three roles: thread 32 issues the loads of each
+// chunk as soon as the MMAs that read its stage have completed (and its
+// dependencies are published); thread 0 issues each chunk's MMAs as soon as
+// its loads land, into the partial accumulator of its group of
+// CHUNKS_PER_PART chunks (alternating between two, each reused once warps
+// 2..7 have folded it into the running sum); warps 2..7 fold each partial
+// as soon as its MMAs complete.  So loads, MMAs and folds overlap.  Every
+// wait is bounded and every loop runs to the end, so each warp takes the
+// same number of steps; false when a dependency wait gave up or a pipeline
+// wait timed out (the problem is then aborted and the sum is garbage).
 template <class WaitTile>
 __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, bool preloaded) {
   bool bad = false;
-  const int n = l.nchunks;
+  const int n = l.nchunks;   // a multiple of CHUNKS_PER_KT
+  const int nparts = n / CHUNKS_PER_PART;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
-    // the MMAs of each chunk once its split is signalled
     for (int c = 0; c < n; ++c) {
       const uint32_t g = l.base + (uint32_t)c;
       const uint32_t s = g % NST;
-      if (!mbar_wait_bounded(tc.split + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
-      if (l.kt && c >= n - (T / 32)) l.kt[1 + c - (n - (T / 32))] = global_ns();
+      const int q = c % CHUNKS_PER_PART;
+      const uint32_t u = tc.kt + (uint32_t)(c / CHUNKS_PER_PART), pb = u & 1u;
+      // partial u's buffer was last used by partial u - 2: wait for its fold
+      if (q == 0 && u >= 2 && !mbar_wait_bounded(tc.pfree + pb, ((u - 2u) >> 1) & 1u, MMA_WAIT_NS)) bad = true;
+      if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
+      if (l.kt && c >= n - CHUNKS_PER_KT) l.kt[1 + c - (n - CHUNKS_PER_KT)] = global_ns();
       tc_fence_after();
-      issue_chunk(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + (g % NLO) * LO_BYTES, A_COL + 64 * (g % NLO),
-                  c == 0 && !preloaded);
+      issue_chunk(tc, tc.stages + s * STAGE_BYTES, PART_COL + 128u * pb, q == 0);
       umma_commit(tc.empty + s);
-      umma_commit(tc.lofree + g % NLO);
+      if (q == CHUNKS_PER_PART - 1) umma_commit(tc.pfull + pb);
     }
   } else if (threadIdx.x == 32) {
     // the loads of the chunks after the first NST - 1 (issued by tc_start),
@@ -615,30 +598,29 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       if (!tc_issue(tc, l, c, wait_tile)) bad = true;
     if (!l.ok) bad = true;
   } else if (warp >= 2) {
-    // warps 2..7: split each chunk as soon as its loads land, ahead of the MMAs
-    for (int c = 0; c < n; ++c) {
-      const uint32_t g = l.base + (uint32_t)c;
-      const uint32_t s = g % NST;
-      if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
-      const uint32_t ls = g % NLO;
-      if (g >= NLO && !mbar_wait_bounded(tc.lofree + ls, ((g / NLO) - 1u) & 1u, MMA_WAIT_NS)) bad = true;
-      convert_stage(tc, tc.stages + s * STAGE_BYTES, tc.stages + LO_OFF + ls * LO_BYTES, A_COL + 64 * ls);
-      fence_proxy_async_smem();   // the split is read by the tensor cores
+    for (int t = 0; t < nparts; ++t) {
+      const uint32_t u = tc.kt + (uint32_t)t, pb = u & 1u;
+      if (!mbar_wait_bounded(tc.pfull + pb, (u >> 1) & 1u, MMA_WAIT_NS)) bad = true;
+      tc_fence_after();
+      fold_partial(tc, PART_COL + 128u * pb, !preloaded && t == 0);
       tc_fence_before();
       __syncwarp();
-      if (lane == 0) mbar_arrive(tc.split + s);
+      if (lane == 0) mbar_arrive(tc.pfree + pb);
     }
   }
   tc.g = l.base + (uint32_t)n;
+  tc.kt += (uint32_t)nparts;
   if (threadIdx.x == 0 && !l.ok) bad = true;
+  // every MMA has completed once the last partial was folded: the stage
+  // buffers are free and the running sum is final
   const bool any_bad = __syncthreads_or(bad) != 0;
   if (any_bad && threadIdx.x == 0) {
     atomicCAS(status + ST_CODE, 0, PGB_ETIMEOUT);
     atomicExch(status + ST_ABORT, 1);
   }
-  const bool drained = tc_drain(tc, status);
+  tc_fence_after();
   if (l.kt && threadIdx.x == 0) l.kt[5] = global_ns();
-  return drained && !any_bad;
+  return !any_bad;
 }
 
 // Store the TMEM accumulator, multiplied by `sign` (+1 or -1), into the
@@ -669,7 +651,11 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const long long ld = jb.ld;
   const bool is_rhs = i >= nt;
   const int ri = i - nt;
-  float* rowbase = is_rhs ? jb.R + (size_t)ri * T * ld : jb.L + (size_t)i * T * ld;
+  const long long lds = 2 * ld;   // row stride of the split matrices
+  // fp32 rows (L, and the right-hand-side rows that keep an fp32 copy) and
+  // split rows (every tile the tensor cores read later)
+  float* rowbase = is_rhs ? (jb.R ? jb.R + (size_t)ri * T * ld : nullptr) : jb.L + (size_t)i * T * ld;
+  float* rowbase_s = is_rhs ? jb.Rs + (size_t)ri * T * lds : jb.Ls + (size_t)i * T * lds;
   const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
   const bool withheld = jb.withhold == ((i << 16) | j) + 1;
   if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
@@ -719,13 +705,16 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   tmem_to_tile(tc, sC, -1.0f);
   if (tr) tr[6] = global_ns();
   __syncthreads();
-  float* dst = rowbase + (size_t)j * T;
+  float* dst = rowbase ? rowbase + (size_t)j * T : nullptr;
+  float* dsts = rowbase_s + (size_t)split_col(j * T);
   float* Linv_j = jb.Linv + (size_t)j * T * T;
+  float* Linvs_j = jb.Linvs + (size_t)j * T * (2 * T);
   if (tr) tr[4] = global_ns();
   if (!is_rhs && i == j) {
     // L_jj = chol(C), published (flag 1) before its inverse (flag 2), so the
     // sub-diagonal tile can start while the inverse is computed
-    potrf_tile(sC, sX, j * T, jb.status, dst, ld, jb.progress + j,
+    // (a diagonal tile of L is never a tensor-core operand: no split)
+    potrf_tile(sC, sX, j * T, jb.status, dst, ld, nullptr, lds, jb.progress + j,
                jb.ptrace ? jb.ptrace + (size_t)j * 16 : nullptr);
     if (jb.ptrace && threadIdx.x == 0) jb.ptrace[(size_t)j * 16 + 12] = global_ns();
     if (threadIdx.x == 0) {
@@ -745,7 +734,9 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     for (int cb = 0; cb < T; cb += 32) trsm_subst_block(sC, sL, sX, cb, cb + 32);
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      Linv_j[(size_t)r * T + c] = c <= r ? sC[c * SC_LD + r] : 0.0f;
+      const float x = c <= r ? sC[c * SC_LD + r] : 0.0f;
+      Linv_j[(size_t)r * T + c] = x;
+      put_split(Linvs_j + (size_t)r * (2 * T) + c, x);
     }
   } else if (!is_rhs && i <= j + jb.near) {
     // the tiles just below the diagonal feed the next columns' critical
@@ -773,7 +764,9 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       if (sub) {
         for (int e = threadIdx.x; e < T * 32; e += DAG_THREADS) {
           const int r = e >> 5, c = cb + (e & 31);
-          dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+          const float x = sC[r * SC_LD + c];
+          dst[(size_t)r * ld + c] = x;
+          put_split(dsts + (size_t)r * lds + c, x);
         }
         __syncthreads();
         if (threadIdx.x == 0) st_release(jb.progress + nt + j, cb / 32 + 1);
@@ -785,16 +778,19 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     if (!sub) {
       for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
         const int r = e >> 7, c = e & (T - 1);
-        dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+        const float x = sC[r * SC_LD + c];
+        dst[(size_t)r * ld + c] = x;
+        put_split(dsts + (size_t)r * lds + c, x);
       }
     }
   } else {
-    // X = C L_jj^-T = C Linv_jj^T on the tensor cores (C staged through dst)
+    // X = C L_jj^-T = C Linv_jj^T on the tensor cores (C staged through the
+    // tile's split, which the result overwrites)
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+      put_split(dsts + (size_t)r * lds + c, sC[r * SC_LD + c]);
     }
-    fence_proxy_async_global();   // dst is read back by the tensor loads
+    fence_proxy_async_global();   // the split is read back by the tensor loads
     fence_proxy_async_smem();     // sC is overwritten by them
     if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 2)) return;
     auto always = [](int, int) { return true; };
@@ -808,7 +804,9 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
-      dst[(size_t)r * ld + c] = sC[r * SC_LD + c];
+      const float x = sC[r * SC_LD + c];
+      if (dst) dst[(size_t)r * ld + c] = x;
+      put_split(dsts + (size_t)r * lds + c, x);
     }
   }
   if (is_rhs && jb.rhs_kind == RHS_CROSS && threadIdx.x < T) {
@@ -843,17 +841,16 @@ __device__ __forceinline__ TcCtx tc_setup(uint8_t* dsmem, uint64_t* bars, uint32
   tc.stages = dsmem + (aligned - base);
   tc.full = bars;
   tc.empty = bars + NST;
-  tc.split = bars + 2 * NST;
-  tc.lofree = bars + 3 * NST;
-  tc.acc = bars + 3 * NST + NLO;
+  tc.pfull = bars + 2 * NST;
+  tc.pfree = bars + 2 * NST + 2;
   tc.g = 0;
-  tc.ntask = 0;
+  tc.kt = 0;
   if (threadIdx.x < 32) {
     tmem_alloc(s_tmem, TMEM_COLS);
     tmem_relinquish();
   }
   if (threadIdx.x == 0) {
-    for (int k = 0; k < NBARS; ++k) mbar_init(bars + k, (k >= 2 * NST && k < 3 * NST) ? SPLIT_WARPS : 1);
+    for (int k = 0; k < NBARS; ++k) mbar_init(bars + k, k >= 2 * NST + 2 ? DRAIN_WARPS : 1);
     fence_mbar_init();
   }
   tc_fence_before();
@@ -1083,23 +1080,51 @@ void launch_syrk_zzt(const Prob* probs, const int4* tiles, int ntiles, int* coun
 
 }  // namespace pgb
 
+namespace pgb {
+// The split (TF32 hi/lo per 128-column tile) of a rows x cols fp32 matrix
+// (row stride ld; cols a multiple of 128) into dst (row stride 2 cols).
+__global__ void split_rows_kernel(const float* __restrict__ src, int rows, int cols, long long ld,
+                                  float* __restrict__ dst) {
+  const long long e = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= (long long)rows * cols) return;
+  const int r = (int)(e / cols), c = (int)(e % cols);
+  put_split(dst + (size_t)r * 2 * cols + split_col(c), src[(size_t)r * ld + c]);
+}
+}  // namespace pgb
+
 // Internal check entry (not part of the public C-ABI): one 128 x 128 tile
-// product through the tensor-core pipeline (A, B: 128 x K row-major device
-// arrays).
+// product C = A B^T through the tensor-core pipeline (A, B: 128 x K
+// row-major device arrays, split into TF32 hi/lo parts first, as the
+// factorisation's epilogues split the tiles they publish).
 extern "C" int pgbx_tc_tile_check(const float* A, const float* B, int K, float* C, int* status, void* stream) {
-  if (!A || !B || !C || !status || K <= 0 || K % pgb::T) return PGB_EINVAL;
-  pgb::dag_set_attributes();
-  alignas(64) unsigned char maps[2][128];
-  if (!pgb::make_tile_map(maps[0], A, pgb::T, K, K) || !pgb::make_tile_map(maps[1], B, pgb::T, K, K))
-    return PGB_ECUDA;
-  void* dmaps = nullptr;
-  if (cudaMalloc(&dmaps, sizeof(maps)) != cudaSuccess) return PGB_ENOMEM;
+  using namespace pgb;
+  if (!A || !B || !C || !status || K <= 0 || K % T) return PGB_EINVAL;
+  dag_set_attributes();
   cudaStream_t s = (cudaStream_t)stream;
-  if (cudaMemcpyAsync(dmaps, maps, sizeof(maps), cudaMemcpyHostToDevice, s) != cudaSuccess) return PGB_ECUDA;
-  pgb::tc_tile_check_kernel<<<1, pgb::DAG_THREADS, pgb::DAG_SMEM, s>>>(dmaps, static_cast<unsigned char*>(dmaps) + 128,
-                                                                       K, C, status);
-  const cudaError_t e = cudaGetLastError();
+  float* sp = nullptr;   // split A (T x 2K), then split B
+  void* dmaps = nullptr;
+  if (cudaMalloc(reinterpret_cast<void**>(&sp), sizeof(float) * 4 * (size_t)T * K) != cudaSuccess) return PGB_ENOMEM;
+  if (cudaMalloc(&dmaps, 256) != cudaSuccess) {
+    cudaFree(sp);
+    return PGB_ENOMEM;
+  }
+  alignas(64) unsigned char maps[2][128];
+  int rc = PGB_OK;
+  if (!make_tile_map(maps[0], sp, T, 2LL * K, 2LL * K) ||
+      !make_tile_map(maps[1], sp + 2 * (size_t)T * K, T, 2LL * K, 2LL * K))
+    rc = PGB_ECUDA;
+  if (rc == PGB_OK && cudaMemcpyAsync(dmaps, maps, sizeof(maps), cudaMemcpyHostToDevice, s) != cudaSuccess)
+    rc = PGB_ECUDA;
+  if (rc == PGB_OK) {
+    const int nb = ceil_div(T * K, 256);
+    split_rows_kernel<<<nb, 256, 0, s>>>(A, T, K, K, sp);
+    split_rows_kernel<<<nb, 256, 0, s>>>(B, T, K, K, sp + 2 * (size_t)T * K);
+    tc_tile_check_kernel<<<1, DAG_THREADS, DAG_SMEM, s>>>(dmaps, static_cast<unsigned char*>(dmaps) + 128, K, C,
+                                                          status);
+    if (cudaGetLastError() != cudaSuccess) rc = PGB_ECUDA;
+  }
   cudaStreamSynchronize(s);
   cudaFree(dmaps);
-  return e == cudaSuccess ? PGB_OK : PGB_ECUDA;
+  cudaFree(sp);
+  return rc;
 }

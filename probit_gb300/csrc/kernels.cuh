@@ -29,7 +29,12 @@ struct Prob {
   float* L;           // factor of B (n_pad x ld), lower tiles
   float* Linv;        // inverses of the diagonal tiles (nt x T x T)
   float* Rv;          // Newton RHS row tile (T x ld)
-  float* Rz;          // L^-T (n_pad x ld), gradient only
+  // splits (TF32 hi/lo parts side by side per 128-column tile, row stride
+  // 2 ld; see split_col in umma.cuh) of the tiles the tensor cores read
+  float* Ls;          // of L (n_pad x 2 ld)
+  float* Linvs;       // of Linv (nt T x 2 T)
+  float* Rvs;         // of Rv (T x 2 ld)
+  float* Rz;          // split of L^-T (n_pad x 2 ld), gradient only
   float* Binv;        // B^-1 (n_pad x ld), gradient only
   // vectors (n_pad each)
   float *a, *f, *d1, *W, *sw, *r, *t, *x, *logp, *d3, *dsig, *svec, *rv, *zbar, *tz, *y2, *u, *c, *rowdot, *sw_prev;
@@ -46,7 +51,7 @@ struct Prob {
   double* tpart;      // per-tile trace partials (lower tiles x (MAX_D + 1))
   double* lpart;      // per-block likelihood partials (ceil(n / VT) x (MAX_THETA + 2))
   int* tflags;        // 2 nt flags of the two wavefront solves
-  const void* tm_Rz;  // tensor map of Rz (128 x 32 fp32 boxes, 128-byte swizzle)
+  const void* tm_Rz;  // tensor map of the split Rz (128 x 32 fp32 boxes, 128-byte swizzle)
 };
 
 // One factorisation job of the tile-DAG kernel (dag.cu).
@@ -56,11 +61,14 @@ struct DagJob {
   long long ld;      // floats per row of L and R
   float* L;          // nt*T rows: lower tiles of the factor
   float* Linv;       // nt tiles of T x T: inverses of the diagonal tiles of L
+  float* Ls;         // split of L (row stride 2 ld)
+  float* Linvs;      // split of Linv (row stride 2 T)
   int near;          // tiles below each diagonal tile solved by substitution (1 .. kMaxNearDepth)
   int rhs_kind;      // RhsKind
   int nrt;           // RHS tile rows
   int nrhs;          // RHS rows in use
-  float* R;          // nrt*T rows: RHS rows, overwritten by the solution
+  float* R;          // nrt*T rows: RHS solution in fp32 (NULL: only the split is kept)
+  float* Rs;         // split of the RHS solution rows (row stride 2 ld)
   const float* rhs_vec;  // RHS_VEC: t (n)
   const float* Xq;       // RHS_CROSS: query features (nrhs x Dp)
   float* rowsq;          // RHS_CROSS: per row, per tile column sum of squares (nrhs x nt)
@@ -88,8 +96,8 @@ struct DagJob {
   unsigned long long* trace;
   unsigned long long* ptrace;   // optional: [2 nt][16] phase times of the diagonal factorisations, then of the
                                 // sub-diagonal substitutions; then [nt][2][8] last k-step times of (j, j), (j+1, j)
-  // tensor maps (128 x 32 fp32 boxes, 128-byte swizzle) of L, of R and of
-  // Linv (nt*T rows of T), for the tensor-core operand loads
+  // tensor maps (128 x 32 fp32 boxes, 128-byte swizzle) of the splits of L,
+  // of R and of Linv, for the tensor-core operand loads
   const void* tm_L;
   const void* tm_R;
   const void* tm_Linv;

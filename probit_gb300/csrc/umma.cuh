@@ -227,6 +227,22 @@ __device__ __forceinline__ void split_tf32(float x, float& hi, float& lo) {
   lo = round_tf32(x - hi);
 }
 
+// Split layout of an operand matrix: the TF32 hi and lo parts of every
+// 128-column tile side by side, hi in the tile's first 128 columns of the
+// split row and lo in the next 128, so a split matrix of a logical rows x ld
+// fp32 matrix has 2 ld columns.  Logical column `col` has its hi part at
+// split column split_col(col) and its lo part 128 columns further on; a
+// 32-column chunk of either part is one 128 x 32 tensor-map box.
+__host__ __device__ __forceinline__ int split_col(int col) { return ((col >> 7) << 8) + (col & 127); }
+
+// x as its hi/lo pair at p[0] (hi) and p[128] (lo).
+__device__ __forceinline__ void put_split(float* p, float x) {
+  float hi, lo;
+  split_tf32(x, hi, lo);
+  p[0] = hi;
+  p[128] = lo;
+}
+
 __device__ __forceinline__ uint32_t sw128_offset(int row, int unit) {
   return (uint32_t)(row * 128 + ((unit ^ (row & 7)) << 4));
 }
