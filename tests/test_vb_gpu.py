@@ -2,7 +2,10 @@
 pgb_vb_value_and_grad) against the float64 oracle restatement of VBGP
 (approximators.py:280-339, implicit/VB.py): the fixed point to 1e-3 of its
 largest entry, the objective to 1e-4 relative, the iteration count within 2
-of the oracle's, the gradient to 1e-3 of its largest entry, and predictions
+of the interval spanned by the oracle's float32 and float64 counts (the VB map
+contracts slowly, by ~0.8 a step on the N = 513 case, so near the 1e-4
+tolerance float32 rounding moves the count: the oracle takes 50 steps in
+float32 and 40 in float64 there), the gradient to 1e-3 of its largest entry, and predictions
 with the VB precision 1 / sigma^2 against the oracle's Approximator.predict."""
 
 import math
@@ -34,8 +37,9 @@ def test_vb_weight_and_objective(cuda_device, seed, N, D, J, kind):
     w = np.asarray(gp.weight(params), np.float64)
     it = gp.last_status()[1]
     w64, it64 = L.vb_weight(op, p.theta(), tol=TOL)
+    _, it32 = L.vb_weight(op, p.theta(), tol=TOL, dtype=np.float32)
     assert np.abs(w - w64).max() <= 1e-3 * np.abs(w64).max(), (np.abs(w - w64).max(), np.abs(w64).max())
-    assert abs(it - it64) <= 2, (it, it64)
+    assert min(it32, it64) - 2 <= it <= max(it32, it64) + 2, (it, it32, it64)
     v = gp.objective()(params)
     v64 = L.vb_objective(op, p.theta(), w64)
     assert abs(v - v64) <= 1e-4 * abs(v64), (v, v64)
