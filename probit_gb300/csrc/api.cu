@@ -1452,7 +1452,7 @@ void* pgbx_gp_buffer(pgb_gp* gp, const char* name) {
                         {"zbar", q.zbar},   {"u", q.u},         {"c", q.c},         {"rowdot", q.rowdot},
                         {"L", q.L},         {"Linv", q.Linv},   {"Rz", q.Rz},       {"Binv", q.Binv},
                         {"logp", q.logp},   {"grad", q.grad},   {"err", q.err},     {"value", q.value},
-                        {"reuse", q.reuse}, {"trace", gp->e.trace},
+                        {"reuse", q.reuse}, {"trace", gp->e.trace}, {"da", q.da},
                         {"tasks_none", gp->e.tasks[JOB_NONE]},
                         {"tasks_ident", gp->e.tasks[JOB_IDENT]},
                         {"ptrace", gp->e.hjobs[JOB_NONE].ptrace}};

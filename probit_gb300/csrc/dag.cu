@@ -793,6 +793,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     fence_proxy_async_global();   // the split is read back by the tensor loads
     fence_proxy_async_smem();     // sC is overwritten by them
     if (!block_wait(jb.ready + (size_t)j * nt + j, jb.status, s_ok + 2, 2)) return;
+    if (tr) tr[7] = global_ns();
     auto always = [](int, int) { return true; };
     TcLoad trsm_load = tc_load(rows_map, row0, j * T, jb.tm_Linv, j * T, 0, 0, 1, tc);
     if (threadIdx.x == 0) {
@@ -800,6 +801,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       tc_start(tc, trsm_load, always);
     }
     if (!tc_run(tc, trsm_load, jb.status, always, false)) return;
+    if (tr) tr[5] = global_ns();
     tmem_to_tile(tc, sC, 1.0f);
     __syncthreads();
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {

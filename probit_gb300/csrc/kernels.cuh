@@ -91,8 +91,9 @@ struct DagJob {
   // never released, so the waits for it run out (0: none)
   int withhold;
   // optional per-task timestamps (globaltimer ns): [task][8] = start, k-loop
-  // done, tile ready, flag released, epilogue start, L_jj published (diagonal),
-  // C assembled (after the accumulator is applied)
+  // done, tile ready, flag released, epilogue start, L_jj published (diagonal)
+  // or tensor-core solve done (other tiles), C assembled (after the
+  // accumulator is applied), solve operands staged (tensor-core solves)
   unsigned long long* trace;
   unsigned long long* ptrace;   // optional: [2 nt][16] phase times of the diagonal factorisations, then of the
                                 // sub-diagonal substitutions; then [nt][2][8] last k-step times of (j, j), (j+1, j)

@@ -64,20 +64,25 @@ class ShardedBatch:
 
     ``gps`` / ``params`` are the whole batch (the same on every rank);
     each rank builds a :class:`~probit_gb300.LaplaceBatch` of its share on its
-    current CUDA device.  ``value_and_grad()(params)`` returns, on every rank,
-    the values and gradients of all problems in batch order."""
+    current CUDA device (``batch_cls`` stands in for it where no GPU is
+    used).  ``value_and_grad()(params)`` returns, on every rank, the values
+    and gradients of all problems in batch order; with ``world == 1`` no
+    process group is needed."""
 
-    def __init__(self, gps, params, group=None, rank=None, world=None):
-        import torch.distributed as dist
+    def __init__(self, gps, params, group=None, rank=None, world=None, batch_cls=None):
+        if batch_cls is None:
+            from .batch import LaplaceBatch as batch_cls
+        if rank is None or world is None:
+            import torch.distributed as dist
 
-        from .batch import LaplaceBatch
-
+            rank = dist.get_rank(group) if rank is None else rank
+            world = dist.get_world_size(group) if world is None else world
         self.group = group
-        self.rank = dist.get_rank(group) if rank is None else rank
-        self.world = dist.get_world_size(group) if world is None else world
+        self.rank = rank
+        self.world = world
         self.n = len(gps)
         self.local = shard_indices([float(gp.N) ** 3 for gp in gps], self.rank, self.world)
-        self.batch = LaplaceBatch([gps[k] for k in self.local], [params[k] for k in self.local]) if self.local else None
+        self.batch = batch_cls([gps[k] for k in self.local], [params[k] for k in self.local]) if self.local else None
 
     def value_and_grad(self):
         local_vg = self.batch.value_and_grad() if self.batch is not None else None
@@ -88,7 +93,51 @@ class ShardedBatch:
                 res = list(zip(vals, grads))
             else:
                 res = []
-            allr = gather_results(self.local, res, self.n, self.group)
+            if self.world == 1:
+                allr = res
+            else:
+                allr = gather_results(self.local, res, self.n, self.group)
             return [r[0] for r in allr], [r[1] for r in allr]
 
         return vg
+
+
+def run_sharded_rounds(gps, params, rounds, warmup=1, group=None, rank=None, world=None, batch_cls=None,
+                       sync=None):
+    """Evaluate a batch sharded over the ranks ``rounds`` times and time it.
+
+    Each round is one ``ShardedBatch.value_and_grad()`` call: every rank
+    evaluates its LPT share (one batched launch sequence on its GPU) and the
+    per-problem results are gathered on every rank.  A barrier precedes the
+    timed rounds; ``sync`` (e.g. ``torch.cuda.synchronize``) is called on both
+    sides of them; the time is the maximum over ranks.  Returns a dict with
+    the rank's problem count, the problems per second of the whole job
+    (len(gps) * rounds / max time), every rank's local time and the last
+    round's results in batch order."""
+    import time
+
+    sb = ShardedBatch(gps, params, group=group, rank=rank, world=world, batch_cls=batch_cls)
+    vg = sb.value_and_grad()
+    for _ in range(warmup):
+        out = vg(params)
+    dist = None
+    if sb.world > 1:
+        import torch.distributed as dist
+
+        dist.barrier(group)
+    if sync:
+        sync()
+    t0 = time.perf_counter()
+    for _ in range(rounds):
+        out = vg(params)
+    if sync:
+        sync()
+    local_s = time.perf_counter() - t0
+    times = [local_s]
+    if dist is not None:
+        times = [None] * sb.world
+        dist.all_gather_object(times, local_s, group=group)
+    wall = max(times)
+    return {"ranks": sb.world, "rank": sb.rank, "local_problems": len(sb.local), "rounds": rounds,
+            "value": len(gps) * rounds / wall, "max_s": wall, "per_rank_s": times,
+            "values": out[0], "grads": out[1]}

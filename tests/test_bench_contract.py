@@ -65,3 +65,31 @@ def test_accuracy_check_closed_form():
             raise ValueError("no data")
 
     assert "error" in bench.accuracy_check(Broken(), 0.0)
+
+
+def test_summary_is_short_and_last():
+    """The GPU arm ends its line with `summary`, a few numbers per section, so
+    the tail of the output (what a reader of the run's record sees) holds
+    every section's figures."""
+    sys.path.insert(0, str(ROOT))
+    import bench
+
+    line = {
+        "accuracy": {"rel_err": 2.3e-5, "predict": {"mean_err_of_max": 1.3e-5, "var_err_of_s": 2.7e-6}},
+        "predict": {"ms": 26.7},
+        "c0": {"device_ms_per_step": 3.1, "e2e_ms_per_step": 4.2, "newton_iterations": 6,
+               "accuracy": {"rel_err_vs_float64": 1e-6}, "cpu_baseline": {"value": 1.5}},
+        "batched": {"value": 3200.0, "e2e": {"value": 3100.0}, "plain": {"value": 500.0}, "batched_over_plain": 6.4,
+                    "results_identical_to_plain": True, "cpu_baseline": {"value": 1.2}},
+        "hyperopt": {"value": 600.0, "evaluation_rounds": 300, "batched_over_plain": 9.6, "e2e_over_cpu": 380.0},
+        "served": {"workers": 12, "pool": 256,
+                   "offered_2000_per_s": {"p50_ms": 1.0, "p99_ms": 4.0, "small_p50_ms": 0.8, "small_p99_ms": 3.0,
+                                          "req_s": 1990.0, "requests": 120000, "errors": 0, "window_s": 60.0},
+                   "offered_150_per_s": {"p50_ms": 0.7, "p99_ms": 3.0, "small_p50_ms": 0.6, "small_p99_ms": 2.0,
+                                         "req_s": 149.0, "requests": 750, "errors": 0, "window_s": 5.0}},
+        "sharded_c2": {"ranks": 1, "value": 3100.0},
+    }
+    s = bench.summary_of(line)
+    assert set(s) == {"c1_rel_err", "c1_predict_err", "c1_predict_ms", "c0", "c2", "c3", "c4", "sharded_c2"}
+    assert s["c2"]["batched_over_plain"] == 6.4 and s["c2"]["identical"] is True
+    assert len(json.dumps(s)) < 1300

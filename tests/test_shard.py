@@ -112,3 +112,46 @@ def test_sharded_batch_order_over_gloo_world_2(tmp_path):
         assert np.array_equal(got[2], np.arange(len(Ns), dtype=float))
     l0, l1 = (set(np.load(f"{out}.{r}.local.npy").tolist()) for r in range(2))
     assert not (l0 & l1) and (l0 | l1) == set(range(len(Ns)))
+
+
+def _bench_worker(rank, world, port, out_path):
+    import torch.distributed as dist
+
+    dist.init_process_group("gloo", init_method=f"tcp://127.0.0.1:{port}", rank=rank, world_size=world)
+    try:
+        Ns = [40, 4000, 128, 900, 2048, 33, 513, 3000, 64, 1500]
+        res = shard.run_sharded_rounds([_FakeGP(n) for n in Ns], [float(k) for k in range(len(Ns))], rounds=3,
+                                       batch_cls=_FakeBatch)
+        np.save(f"{out_path}.{rank}.npy", np.array([res["values"], [g[1] for g in res["grads"]]]))
+        np.save(f"{out_path}.{rank}.meta.npy", np.array([res["ranks"], res["local_problems"], res["value"],
+                                                          res["max_s"], max(res["per_rank_s"])]))
+    finally:
+        dist.destroy_process_group()
+
+
+def test_bench_sharded_rounds_over_gloo_world_2(tmp_path):
+    """The bench's sharded path (shard.run_sharded_rounds): LPT shares over two
+    gloo ranks, results gathered in batch order on both, the job's rate taken
+    over the slower rank."""
+    import torch.multiprocessing as mp
+
+    out = str(tmp_path / "b")
+    mp.spawn(_bench_worker, args=(2, _free_port(), out), nprocs=2, join=True)
+    Ns = [40, 4000, 128, 900, 2048, 33, 513, 3000, 64, 1500]
+    metas = [np.load(f"{out}.{r}.meta.npy") for r in range(2)]
+    for r in range(2):
+        got = np.load(f"{out}.{r}.npy")
+        assert np.array_equal(got[0], np.array(Ns, float))
+        assert np.array_equal(got[1], np.arange(len(Ns), dtype=float))
+        assert metas[r][0] == 2 and metas[r][3] == metas[r][4]
+        assert metas[r][2] == pytest.approx(len(Ns) * 3 / metas[r][3])
+    assert metas[0][1] + metas[1][1] == len(Ns)
+    assert metas[0][3] == metas[1][3]
+
+
+def test_bench_sharded_rounds_single_rank():
+    Ns = [100, 2000, 300]
+    res = shard.run_sharded_rounds([_FakeGP(n) for n in Ns], [0.0, 1.0, 2.0], rounds=2, rank=0, world=1,
+                                   batch_cls=_FakeBatch)
+    assert res["ranks"] == 1 and res["local_problems"] == 3
+    assert res["values"] == [float(n) for n in Ns]
