@@ -46,7 +46,7 @@ constexpr uint32_t RUN_COL = 0;
 constexpr uint32_t PART_COL = 128;
 constexpr uint32_t TMEM_COLS = 512;
 constexpr size_t DAG_SMEM = UNION_BYTES + (2 * T * 17 + 2 * T) * 4 + 1024 + 64;
-static_assert(UNION_BYTES >= 2 * T * SC_LD * 4, "epilogue tiles must fit in the stage buffers");
+static_assert(UNION_BYTES >= (T * SC_LD + T * (T + 4)) * 4, "epilogue tiles must fit in the stage buffers");
 static_assert(DAG_SMEM <= 232448, "dynamic shared memory above the 227 KB a block may use");
 static_assert(CHUNKS_PER_KT % CHUNKS_PER_PART == 0, "a k-tile is a whole number of partials");
 constexpr uint32_t IDESC_128x128 = idesc_tf32(128, 128);
@@ -181,67 +181,89 @@ __device__ __forceinline__ void bar_sync_first(int count) {
 
 // Cholesky of one 32-wide panel of the tile in sC (row stride SC_LD): the
 // rows jb..127 of columns jb..jb+31, whose trailing updates are applied.
-// Thread t < nr = 128 - jb holds row jb + t in registers.  Column C: the
-// warp of the diagonal block (threads 0..31) takes the pivot from lane C by
-// shuffle, scales its entries by the pivot's reciprocal square root and puts
-// them in a 32-float line of shared memory at position (lane - C) mod 32, so
-// the multipliers L[jb+C+m][C] sit at positions m = 1..31 and come back as
-// eight 16-byte broadcast loads, and the reciprocal square root beside it;
-// one barrier over the panel's warps; every row below the diagonal block
-// then scales its own entry, and every row updates its later entries with
-// the multipliers.  So the rows below are solved in the same column loop
-// instead of by a substitution after it.  Entries above the diagonal are
-// updated too (no per-entry predicate) and never written back.  The line is
-// double-buffered by column parity: the barrier of column C orders its
-// store before the loads, and the loads of column C before the store of
-// column C + 2 (every warp passes barrier C + 1 after its loads of C).
-// Every 4 columns the row is shifted left by 4 registers, so the column loop
-// stays a small loop (a fully unrolled one is ~20 KB of straight-line code
-// that runs at instruction-fetch latency inside the factorisation kernel)
-// while every register index is a compile-time constant.  Each L entry is
-// written back to sC as its column completes.  sbuf: 96 floats, 16-byte
-// aligned (two lines, then 32 reciprocal square roots).
+// Thread t < nr = 128 - jb holds row jb + t in registers, and the columns go
+// four at a time.  Group C0..C0+3: the warp of the diagonal block (threads
+// 0..31) factors its 4 x 4 diagonal block by shuffles (pivot from lane C,
+// scale by the pivot's reciprocal square root, update the group's later
+// columns with the multiplier shuffled from its row's lane) and puts every
+// lane's four entries in four lines of shared memory (line c, entry lane:
+// L[jb+lane][C0+c]) and the four reciprocal square roots beside them; one
+// barrier over the panel's warps; every row below the diagonal block then
+// solves its four entries against the 4 x 4 block from the lines, and every
+// row updates its later columns by a rank-4 update with the multipliers
+// L[jb+C0+m][C0+c] = line c, entry C0+m (16-byte broadcast loads; entries
+// 32..63 of each line are 0, for the register slots past the panel).  So
+// one barrier serves four columns.  Entries above the diagonal are computed
+// too (no per-entry predicate) and never written back.  The lines are
+// double-buffered by group parity: the barrier of group g orders its stores
+// before the loads, and every warp passes barrier g + 1 only after its loads
+// of group g, before the stores of group g + 2.  Every group the row is
+// shifted left by 4 registers, so the loop stays small while every register
+// index is a compile-time constant.  sbuf: 576 floats, 16-byte aligned (two
+// buffers of four 64-float lines and four reciprocal square roots).
+constexpr int PBUF = 4 * 64 + 32;
 __device__ __forceinline__ void panel_potrf(float* sC, int jb, float* sbuf, int col0, int* status) {
   const int tid = threadIdx.x, lane = tid & 31;
   const int nr = T - jb;
   if (tid >= nr) return;
   const bool dwarp = tid < 32;
   float* row = sC + (jb + tid) * SC_LD + jb;
-  float* srl = sbuf + 64;
+  if (dwarp) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) sbuf[(k >> 2) * PBUF + (k & 3) * 64 + 32 + lane] = 0.0f;
+  }
   float d[32];
 #pragma unroll
   for (int m = 0; m < 32; ++m) d[m] = row[m];
   int bad = -1;
 #pragma unroll 1
   for (int C0 = 0; C0 < 32; C0 += 4) {
+    float* lines = sbuf + PBUF * ((C0 >> 2) & 1);
+    float* srl = lines + 4 * 64;
+    float l[4];
+    if (dwarp) {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) {
-      const int C = C0 + k;
-      float* line = sbuf + 32 * (k & 1);
-      float dc;
-      if (dwarp) {
-        const float piv = __shfl_sync(FULL, d[k], C);
+      for (int c = 0; c < 4; ++c) {
+        const int C = C0 + c;
+        const float piv = __shfl_sync(FULL, d[c], C);
         if (!(piv > 0.0f) && bad < 0) bad = C;
         const float rl = rsqrtf(piv);
-        dc = (lane == C) ? piv * rl : d[k] * rl;
-        if (lane >= C) row[C] = dc;
-        line[(lane - C) & 31] = dc;
-        if (lane == C) srl[C] = rl;
-        bar_sync_first(nr);
-      } else {
-        bar_sync_first(nr);
-        dc = d[k] * srl[C];
-        row[C] = dc;
+        l[c] = (lane == C) ? piv * rl : d[c] * rl;
+        if (lane == C) srl[c] = rl;
+#pragma unroll
+        for (int c2 = c + 1; c2 < 4; ++c2) d[c2] = fmaf(-l[c], __shfl_sync(FULL, l[c], C0 + c2), d[c2]);
+        lines[c * 64 + lane] = l[c];
       }
+      bar_sync_first(nr);
+    } else {
+      bar_sync_first(nr);
 #pragma unroll
-      for (int q = 0; q < 8; ++q) {
-        const float4 v = reinterpret_cast<const float4*>(line)[q];
-        const float lv[4] = {v.x, v.y, v.z, v.w};
+      for (int c = 0; c < 4; ++c) {
+        float v = d[c];
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const int m = 4 * q + e;
-          if (m >= 1 && k + m < 32) d[k + m] = fmaf(-dc, lv[e], d[k + m]);
-        }
+        for (int c2 = 0; c2 < c; ++c2) v = fmaf(-l[c2], lines[c2 * 64 + C0 + c], v);
+        l[c] = v * srl[c];
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 4; ++c)
+      if (!dwarp || lane >= C0 + c) row[C0 + c] = l[c];
+#pragma unroll
+    for (int q = 1; q < 8; ++q) {
+      const float4 v0 = *reinterpret_cast<const float4*>(lines + 0 * 64 + C0 + 4 * q);
+      const float4 v1 = *reinterpret_cast<const float4*>(lines + 1 * 64 + C0 + 4 * q);
+      const float4 v2 = *reinterpret_cast<const float4*>(lines + 2 * 64 + C0 + 4 * q);
+      const float4 v3 = *reinterpret_cast<const float4*>(lines + 3 * 64 + C0 + 4 * q);
+      const float a0[4] = {v0.x, v0.y, v0.z, v0.w}, a1[4] = {v1.x, v1.y, v1.z, v1.w};
+      const float a2[4] = {v2.x, v2.y, v2.z, v2.w}, a3[4] = {v3.x, v3.y, v3.z, v3.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        float x = d[4 * q + e];
+        x = fmaf(-l[0], a0[e], x);
+        x = fmaf(-l[1], a1[e], x);
+        x = fmaf(-l[2], a2[e], x);
+        x = fmaf(-l[3], a3[e], x);
+        d[4 * q + e] = x;
       }
     }
 #pragma unroll
@@ -253,27 +275,42 @@ __device__ __forceinline__ void panel_potrf(float* sC, int jb, float* sbuf, int 
   }
 }
 
-// Row substitution x[c] = (x[c] - sum_{m<c} x[m] L[c][m]) / L[c][c] for a
-// 32-wide block, L rows read from shared memory (row stride SC_LD), unrolled
-// by template recursion: it runs on up to 128 threads at once, which share
-// the instruction fetch, and its independent loads give the warps enough
-// instruction-level parallelism (a loop form measured 5-10x slower here).
+// Row stride of transposed L panels in shared memory (Lt[c * LT_LD + r] =
+// L[r][c]): a multiple of 4, so a column of L is read as 16-byte vectors.
+constexpr int LT_LD = T + 4;
+
+// Row substitution x L^T = c for a 32-wide block (x[c] = (c[c] - sum_{m<c}
+// x[m] L[c][m]) / L[c][c]), column by column: x[C] is final after the
+// updates of columns < C, then it updates every later entry with column C of
+// L (read from the transposed block, Ltb[C * LT_LD + m] = L[m][C], as 16-byte
+// broadcast loads).  The dependency chain is 32 steps long and the updates of
+// different entries are independent, where the dot-product order
+// (x[C] -= sum over m < C) chains all 496 fused multiply-adds of a row.
+// Unrolled by template recursion, so every register index is a constant.
 template <int C>
-__device__ __forceinline__ void subst32_col(float (&x)[32], const float* Lb, const float* rdiag) {
+__device__ __forceinline__ void subst32_col(float (&x)[32], const float* Ltb, const float* rdiag) {
   if constexpr (C < 32) {
-    float acc = x[C];
+    x[C] *= rdiag[C];
+    const float* col = Ltb + C * LT_LD;
 #pragma unroll
-    for (int m = 0; m < C; ++m) acc = fmaf(-x[m], Lb[C * SC_LD + m], acc);
-    x[C] = acc * rdiag[C];
-    subst32_col<C + 1>(x, Lb, rdiag);
+    for (int q = (C + 1) / 4; q < 8; ++q) {
+      const float4 v = *reinterpret_cast<const float4*>(col + 4 * q);
+      const float lv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        const int m = 4 * q + e;
+        if (m > C) x[m] = fmaf(-x[C], lv[e], x[m]);
+      }
+    }
+    subst32_col<C + 1>(x, Ltb, rdiag);
   }
 }
 
-__device__ __forceinline__ void subst32_row(float* xs, const float* Lb, const float* rdiag) {
+__device__ __forceinline__ void subst32_row(float* xs, const float* Ltb, const float* rdiag) {
   float x[32];
 #pragma unroll
   for (int m = 0; m < 32; ++m) x[m] = xs[m];
-  subst32_col<0>(x, Lb, rdiag);
+  subst32_col<0>(x, Ltb, rdiag);
 #pragma unroll
   for (int m = 0; m < 32; ++m) xs[m] = x[m];
 }
@@ -355,19 +392,20 @@ __device__ void potrf_tile(float* sC, float* sbuf, int col0, int* status, float*
 
 // X L^T = C in place for the first `rows` rows of sC (a multiple of 4), by
 // 32-column blocks: block cb needs panel cb of L (rows cb.., columns
-// cb .. cb+31) in sL; one thread per row solves the block of its row, then
-// 4 x 4 register blocks update the remaining columns.  Used on the critical
-// path (the tiles just below the diagonal), panel by panel as the diagonal
-// tile publishes them, and for the inverse of the diagonal tile.
-__device__ void trsm_subst_panel(float* sC, const float* sL, float* srd, int cb, int rows) {
+// cb .. cb+31), transposed in sLt (sLt[c * LT_LD + r] = L[r][c]); one thread
+// per row solves the block of its row, then 4 x 4 register blocks update the
+// remaining columns.  Used on the critical path (the tiles just below the
+// diagonal), panel by panel as the diagonal tile publishes them, and for the
+// inverse of the diagonal tile.
+__device__ void trsm_subst_panel(float* sC, const float* sLt, float* srd, int cb, int rows) {
   const int tid = threadIdx.x;
-  if (tid < 32) srd[cb + tid] = __frcp_rn(sL[(cb + tid) * SC_LD + cb + tid]);
+  if (tid < 32) srd[cb + tid] = __frcp_rn(sLt[(cb + tid) * LT_LD + cb + tid]);
   __syncthreads();
-  if (tid < rows) subst32_row(sC + tid * SC_LD + cb, sL + cb * SC_LD + cb, srd + cb);
+  if (tid < rows) subst32_row(sC + tid * SC_LD + cb, sLt + cb * LT_LD + cb, srd + cb);
   __syncthreads();
 }
 
-__device__ void trsm_trail_panel(float* sC, const float* sL, int cb, int rows) {
+__device__ void trsm_trail_panel(float* sC, const float* sLt, int cb, int rows) {
   const int tid = threadIdx.x;
   const int rem = T - cb - 32;
   if (rem > 0) {
@@ -381,12 +419,11 @@ __device__ void trsm_trail_panel(float* sC, const float* sL, int cb, int rows) {
         for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
 #pragma unroll 8
       for (int m = 0; m < 32; ++m) {
-        float a[4], b[4];
+        float a[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          a[q] = sC[(r0 + q) * SC_LD + cb + m];
-          b[q] = sL[(c0 + q) * SC_LD + cb + m];
-        }
+        for (int q = 0; q < 4; ++q) a[q] = sC[(r0 + q) * SC_LD + cb + m];
+        const float4 bv = *reinterpret_cast<const float4*>(sLt + (cb + m) * LT_LD + c0);
+        const float b[4] = {bv.x, bv.y, bv.z, bv.w};
 #pragma unroll
         for (int q = 0; q < 4; ++q)
 #pragma unroll
@@ -401,9 +438,9 @@ __device__ void trsm_trail_panel(float* sC, const float* sL, int cb, int rows) {
   }
 }
 
-__device__ void trsm_subst_block(float* sC, const float* sL, float* srd, int cb, int rows) {
-  trsm_subst_panel(sC, sL, srd, cb, rows);
-  trsm_trail_panel(sC, sL, cb, rows);
+__device__ void trsm_subst_block(float* sC, const float* sLt, float* srd, int cb, int rows) {
+  trsm_subst_panel(sC, sLt, srd, cb, rows);
+  trsm_trail_panel(sC, sLt, cb, rows);
 }
 
 // Thread 0 waits (an acquire load; the barrier then orders the rest of the
@@ -727,7 +764,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     for (int e = threadIdx.x; e < T * T; e += DAG_THREADS) {
       const int r = e >> 7, c = e & (T - 1);
       const float l = sC[r * SC_LD + c];
-      sL[r * SC_LD + c] = c <= r ? l : 0.0f;
+      sL[c * LT_LD + r] = c <= r ? l : 0.0f;   // transposed
       sC[r * SC_LD + c] = r == c ? 1.0f : 0.0f;
     }
     __syncthreads();
@@ -756,7 +793,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       if (sp) sp[cb / 8] = global_ns();
       for (int e = threadIdx.x; e < (T - cb) * 32; e += DAG_THREADS) {
         const int r = cb + (e >> 5), c = cb + (e & 31);
-        sL[r * SC_LD + c] = __ldcg(Ljj + (size_t)r * ld + c);
+        sL[c * LT_LD + r] = __ldcg(Ljj + (size_t)r * ld + c);   // transposed
       }
       __syncthreads();
       if (sp) sp[cb / 8 + 1] = global_ns();
