@@ -76,7 +76,12 @@ enum GraphOp {
 };
 bool is_vb(int op) { return op == OP_VB_WEIGHT || op == OP_VB_OBJECTIVE || op == OP_VB_VG; }
 bool needs_grad_buffers(int op) { return op == OP_VG || op == OP_VB_VG; }
-enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_COUNT = 4 };
+enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_VEC_IDENT = 4, JOB_COUNT = 5 };
+// Merged task lists: Newton step, factor only, factor with L^-T, and the
+// Newton step of an evidence + gradient evaluation (problems with a Gaussian
+// likelihood solve their L^-T rows with the factor of the first step, which
+// is final since W does not change).
+enum TaskList { TL_STEP = 0, TL_NONE = 1, TL_IDENT = 2, TL_VG_STEP = 3, TL_COUNT = 4 };
 enum Counter { C_DAG = 0, C_TRSV_T = 1, C_PREDICT = 2, C_TRSV_L = 3, C_SYRK = 4, C_COUNT = 8 };
 
 constexpr int kStatusWords = 8;
@@ -161,7 +166,7 @@ struct Engine {
   // block maps
   std::vector<int2> h_vmap, h_bmap, h_claims;
   std::vector<int4> h_syrk;
-  std::vector<int4> h_tasks[3];
+  std::vector<int4> h_tasks[TL_COUNT];
   int2* vmap = nullptr;
   int nvb = 0;
   int2* bmap = nullptr;
@@ -172,8 +177,10 @@ struct Engine {
   int nsyrk = 0;
   DagJob* jobs = nullptr;                  // [problem * JOB_COUNT + slot]
   std::vector<DagJob> hjobs;
-  int4* tasks[3] = {nullptr, nullptr, nullptr};
-  int ntasks[3] = {0, 0, 0};
+  int4* tasks[TL_COUNT] = {};
+  int ntasks[TL_COUNT] = {};
+  int* zvalid_all = nullptr;
+  int has_gauss = 0;                       // some problem has a Gaussian likelihood
   int2* claims = nullptr;
   int nclaims = 0;
   // graphs
@@ -218,9 +225,25 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
       for (int r = 0; r <= j; ++r) v.push_back(make_int4(job, nt + r, j, 0));
     } else if (kind == RHS_CROSS) {
       for (int r = 0; r < nrt; ++r) v.push_back(make_int4(job, nt + r, j, 0));
+    } else if (kind == RHS_VEC_IDENT) {
+      v.push_back(make_int4(job, nt, j, 0));
+      for (int r = 0; r <= j; ++r) v.push_back(make_int4(job, nt + 1 + r, j, 0));
     }
   }
   return v;
+}
+
+// The tasks of problem p (nt tile rows) in task list `list`; `gauss`: the
+// problem's likelihood is Gaussian (its evaluation Newton step solves L^-T).
+std::vector<int4> list_tasks(int p, int nt, int list, bool gauss) {
+  switch (list) {
+    case TL_STEP: return build_tasks(p * JOB_COUNT + JOB_VEC, nt, RHS_VEC, 1, true);
+    case TL_NONE: return build_tasks(p * JOB_COUNT + JOB_NONE, nt, RHS_NONE, 0, true);
+    case TL_IDENT: return build_tasks(p * JOB_COUNT + JOB_IDENT, nt, RHS_IDENT, nt, true);
+    default:
+      return gauss ? build_tasks(p * JOB_COUNT + JOB_VEC_IDENT, nt, RHS_VEC_IDENT, nt + 1, true)
+                   : build_tasks(p * JOB_COUNT + JOB_VEC, nt, RHS_VEC, 1, true);
+  }
 }
 
 // Lookahead stage of tile task (i, j) of a problem with nt tile rows
@@ -336,7 +359,8 @@ size_t layout(Engine& e, uintptr_t base) {
   e.bmap = b.take<int2>(e.h_bmap.size());
   e.claims = b.take<int2>(e.h_claims.size());
   e.syrk_tiles = b.take<int4>(e.h_syrk.size());
-  for (int k = 0; k < 3; ++k) e.tasks[k] = b.take<int4>(e.h_tasks[k].size());
+  for (int k = 0; k < TL_COUNT; ++k) e.tasks[k] = b.take<int4>(e.h_tasks[k].size());
+  e.zvalid_all = b.take<int>(np);
   for (MvGroup& g : e.mv) g.map = b.take<int2>(g.h.size());
   for (TraceGroup& g : e.tr) g.tiles = b.take<int4>(g.h.size());
   size_t ready_off = 0, tflags_off = 0;
@@ -376,6 +400,7 @@ size_t layout(Engine& e, uintptr_t base) {
     q.active = e.active_all + p;
     q.enabled = e.enabled_all + p;
     q.reuse = e.reuse_all + (size_t)p * 4;
+    q.zvalid = e.zvalid_all + p;
     q.tflags = e.tflags_all + tflags_off;
     tflags_off += 2 * (size_t)nt;
     q.Rz = nullptr;
@@ -398,14 +423,14 @@ size_t layout(Engine& e, uintptr_t base) {
       j.theta = q.theta;
       j.sh = s;
       j.ready = e.ready_all + ready_off;
-      j.progress = e.ready_all + ready_off + 2 * (size_t)nt * nt;
+      j.progress = e.ready_all + ready_off + (2 * (size_t)nt + 1) * nt;
       j.status = q.status;
       j.reuse = q.reuse + 2;
       j.reuse_mode = 0;
       j.tm_L = map_slot(e, p, MAP_L);
       j.tm_Linv = map_slot(e, p, MAP_LINV);
     }
-    ready_off += 2 * (size_t)nt * nt + 2 * nt;
+    ready_off += (2 * (size_t)nt + 1) * nt + 2 * nt;
     DagJob* jb = &e.hjobs[(size_t)p * JOB_COUNT];
     jb[JOB_VEC].rhs_kind = RHS_VEC;
     jb[JOB_VEC].nrt = 1;
@@ -426,6 +451,12 @@ size_t layout(Engine& e, uintptr_t base) {
     jb[JOB_IDENT].nrhs = (int)npad;
     jb[JOB_IDENT].tm_R = q.tm_Rz;
     jb[JOB_CROSS].rhs_kind = RHS_CROSS;
+    jb[JOB_IDENT].zvalid = q.zvalid;
+    jb[JOB_VEC_IDENT] = jb[JOB_VEC];
+    jb[JOB_VEC_IDENT].rhs_kind = RHS_VEC_IDENT;
+    jb[JOB_VEC_IDENT].nrt = 1 + nt;
+    jb[JOB_VEC_IDENT].tm_Z = q.tm_Rz;
+    jb[JOB_VEC_IDENT].Zs = q.Rz;
   }
   return b.off;
 }
@@ -455,11 +486,12 @@ int engine_upload_tables(Engine& e) {
 // problem's near band depth), problems by rank within a stage.  The task
 // counts do not depend on the depths.
 void build_task_lists(Engine& e) {
-  const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
-  for (int k = 0; k < 3; ++k) {
+  for (int k = 0; k < TL_COUNT; ++k) {
     std::vector<std::vector<int4>> per(e.nprob);
-    for (int p = 0; p < e.nprob; ++p)
-      per[p] = build_tasks(p * JOB_COUNT + k, e.nt[p], kinds[k], k == 0 ? 1 : e.nt[p], true);
+    for (int p = 0; p < e.nprob; ++p) {
+      const bool gauss = e.desc[p].likelihood == PGB_LIK_GAUSSIAN;
+      per[p] = list_tasks(p, e.nt[p], k, gauss);
+    }
     e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near, e.whole_max);
     e.ntasks[k] = (int)e.h_tasks[k].size();
   }
@@ -482,7 +514,7 @@ int engine_set_near(Engine& e, const int32_t* near) {
   build_task_lists(e);
   for (int p = 0; p < e.nprob; ++p)
     for (int k = 0; k < JOB_COUNT; ++k) e.hjobs[(size_t)p * JOB_COUNT + k].near = v[p];
-  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
+  for (int k = 0; k < TL_COUNT; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
   return engine_upload_tables(e);
 }
 
@@ -515,9 +547,12 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     e.x_total += (size_t)descs[p].n * descs[p].d;
     e.y_total += (size_t)descs[p].n;
     e.th_total += (size_t)e.th[p];
-    e.ready_words += 2 * (size_t)e.nt[p] * e.nt[p] + 2 * e.nt[p];
+    // tile flags of the L rows and of up to nt + 1 right-hand-side row
+    // tiles, then the panel counters
+    e.ready_words += (2 * (size_t)e.nt[p] + 1) * e.nt[p] + 2 * e.nt[p];
     e.tflags_words += 2 * (size_t)e.nt[p];
     e.dag_dm = std::max(e.dag_dm, dm_of(e.sh[p].Dp));
+    if (descs[p].likelihood == PGB_LIK_GAUSSIAN) e.has_gauss = 1;
     e.nt_max = std::max(e.nt_max, e.nt[p]);
   }
   CU_TRY(cudaGetDevice(&e.device));
@@ -621,7 +656,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   PGB_TRY(upload(e.bmap, e.h_bmap, e.cap_s));
   PGB_TRY(upload(e.claims, e.h_claims, e.cap_s));
   PGB_TRY(upload(e.syrk_tiles, e.h_syrk, e.cap_s));
-  for (int k = 0; k < 3; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
+  for (int k = 0; k < TL_COUNT; ++k) PGB_TRY(upload(e.tasks[k], e.h_tasks[k], e.cap_s));
   for (MvGroup& g : e.mv) PGB_TRY(upload(g.map, g.h, e.cap_s));
   for (TraceGroup& g : e.tr) PGB_TRY(upload(g.tiles, g.h, e.cap_s));
   {
@@ -630,7 +665,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     const char* tv = std::getenv("PGB_TRACE");
     if (tv && tv[0] == '1') {
       size_t mx = 0;
-      for (int k = 0; k < 3; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
+      for (int k = 0; k < TL_COUNT; ++k) mx = std::max(mx, (size_t)e.ntasks[k]);
       void* tp = nullptr;
       if (ws_alloc(e.cap_s, &tp, sizeof(unsigned long long) * (mx * 8 + (size_t)e.nt_max * 48)) == PGB_OK) {
         e.trace = static_cast<unsigned long long*>(tp);
@@ -662,6 +697,7 @@ int ensure_grad_buffers(Engine& e) {
     e.hp[p].Binv = b.take<float>(mat);
     e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].R = nullptr;
     e.hjobs[(size_t)p * JOB_COUNT + JOB_IDENT].Rs = e.hp[p].Rz;
+    e.hjobs[(size_t)p * JOB_COUNT + JOB_VEC_IDENT].Zs = e.hp[p].Rz;
   }
   PGB_TRY(upload_maps(e));
   PGB_TRY(engine_upload_tables(e));
@@ -678,14 +714,14 @@ void enq_matvec(Engine& e, MatvecOp op, cudaStream_t s) {
   for (MvGroup& g : e.mv) launch_gram_matvec(g.kind, g.DM, e.probs, g.map, (int)g.h.size(), op, s);
 }
 
-void enq_dag(Engine& e, int slot, cudaStream_t s) {
+void enq_dag(Engine& e, int list, cudaStream_t s) {
   cudaMemsetAsync(e.ready_all, 0, sizeof(int) * e.ready_words, s);
   cudaMemsetAsync(e.counters + C_DAG, 0, sizeof(int), s);
-  launch_dag_factor(e.jobs, e.tasks[slot], e.ntasks[slot], e.counters + C_DAG, e.dag_dm,
-                    dag_grid(e, e.ntasks[slot]), s);
+  launch_dag_factor(e.jobs, e.tasks[list], e.ntasks[list], e.counters + C_DAG, e.dag_dm,
+                    dag_grid(e, e.ntasks[list]), s);
 }
 
-void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond) {
+void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int list) {
   // f += K da: f follows a by the updates (f = 0, da = a at the start), so
   // the rounding of f shrinks with the step instead of staying at the float32
   // error of a full K a, which would otherwise set a floor under ||da||
@@ -695,7 +731,8 @@ void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, in
   // bitwise-unchanged W keeps the resident factor
   launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
   // new W: L L^T = B and w = L^-1 t in one factorisation (skipped on reuse)
-  enq_dag(e, JOB_VEC, s);
+  enq_dag(e, list, s);
+  if (list == TL_VG_STEP) launch_mark_z(e.probs, e.nprob, s);
   launch_reuse_mark_valid(e.probs, e.nprob, s);
   // reused W: w = L^-1 t by the forward wavefront solve; then x = L^-T w
   cudaMemsetAsync(e.tflags_all, 0, sizeof(int) * e.tflags_words, s);
@@ -746,7 +783,7 @@ void enq_step(Engine& e, int op, cudaStream_t s, cudaGraphConditionalHandle h, i
   if (is_vb(op))
     enq_vb_step(e, s, h, use_cond);
   else
-    enq_newton_step(e, s, h, use_cond);
+    enq_newton_step(e, s, h, use_cond, (op == OP_VG && e.has_gauss) ? TL_VG_STEP : TL_STEP);
 }
 
 void enq_prologue(Engine& e, int op, cudaStream_t s) {
@@ -755,7 +792,7 @@ void enq_prologue(Engine& e, int op, cudaStream_t s) {
   if (is_vb(op)) {
     // B = I + K / sigma^2 does not change along the VB iteration: factor once
     launch_vb_setup(e.probs, e.vmap, e.nvb, s);
-    enq_dag(e, JOB_NONE, s);
+    enq_dag(e, TL_NONE, s);
     launch_vb_mark(e.probs, e.nprob, s);
   }
 }
@@ -804,7 +841,7 @@ void enq_epilogue(Engine& e, int op, cudaStream_t s) {
     launch_trsv(e.probs, e.claims, e.nclaims, 0, e.counters + C_TRSV_L, 1, 1, trsv_grid(e), s);
     launch_trsv(e.probs, e.claims, e.nclaims, 1, e.counters + C_TRSV_T, 0, 1, trsv_grid(e), s);
     launch_vb_grad_vec(e.probs, e.vmap, e.nvb, s);
-    enq_dag(e, JOB_IDENT, s);   // L^-T on the resident factor
+    enq_dag(e, TL_IDENT, s);   // L^-T on the resident factor
     cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
     launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);   // B^-1
     for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), s);
@@ -815,7 +852,7 @@ void enq_epilogue(Engine& e, int op, cudaStream_t s) {
     launch_activate_enabled(e.probs, e.nprob, s);   // every enabled problem takes part from here on
     enq_precision(e, s);
     launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
-    enq_dag(e, op == OP_VG ? JOB_IDENT : JOB_NONE, s);
+    enq_dag(e, op == OP_VG ? TL_IDENT : TL_NONE, s);
     launch_reuse_mark_valid(e.probs, e.nprob, s);
     if (op >= OP_OBJECTIVE) launch_evidence(e.probs, e.vmap, e.nvb, e.nprob, s);
     if (op == OP_VG) enq_grad(e, s);
@@ -1177,7 +1214,7 @@ int pgb_factor(pgb_gp* gp, void* stream) {
   Engine& e = gp->e;
   CU_TRY(cudaMemsetAsync(e.hp[0].reuse + 2, 0, sizeof(int), s));   // always a full factorisation
   launch_activate_enabled(e.probs, e.nprob, s);
-  enq_dag(e, JOB_NONE, s);
+  enq_dag(e, TL_NONE, s);
   CU_TRY(cudaGetLastError());
   return PGB_OK;
 }
@@ -1248,7 +1285,7 @@ int predict_impl(pgb_gp* gp, const float* X, const float* theta, const float* a,
   if (!reuse_factor) {
     launch_reset_problems(e.probs, e.vmap, e.nvb, 0, s);
     launch_sqrt_w(sh.n, q.n_pad, W, q.sw, s);
-    enq_dag(e, JOB_NONE, s);
+    enq_dag(e, TL_NONE, s);
     gp->factor_valid = 0;   // factor of the caller's W, not of the resident posterior
   }
   CU_TRY(cudaMemcpyAsync(gp->Xq_in, Xs, sizeof(float) * (size_t)m * sh.D, cudaMemcpyDeviceToDevice, s));
@@ -1474,25 +1511,26 @@ int pgbx_batch_tasks(pgb_batch* b, int slot, const void** tasks, const void** tr
 
 // Internal diagnostic entry (host only, no GPU needed): the merged task list
 // the engine builds for `count` problems of nt[p] tile rows (kind 0 Newton
-// step, 1 factor only, 2 with L^-T) with near band depths near[p] (NULL:
+// step, 1 factor only, 2 with L^-T, 3 the Newton step of an evidence +
+// gradient evaluation with every problem Gaussian: the Newton row and the
+// L^-T rows) with near band depths near[p] (NULL:
 // the built-in rule) and problems of at most whole_max tile rows as one
 // task (job, -1, 0, 0), written to out[4 * task] as (job, i, j, 0); returns
 // the task count (call with out = NULL to size).
 int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t* near, int32_t whole_max,
                    int32_t* out) {
-  if (!nt || count < 1 || kind < 0 || kind > 2) return -1;
+  if (!nt || count < 1 || kind < 0 || kind >= TL_COUNT) return -1;
   std::vector<int> nearv(count);
   for (int p = 0; p < count; ++p) {
     nearv[p] = near ? near[p] : near_depth(nt[p]);
     if (nearv[p] < 1 || nearv[p] > kMaxNearDepth) return -1;
   }
-  const int kinds[3] = {RHS_VEC, RHS_NONE, RHS_IDENT};
   std::vector<std::vector<int4>> per(count);
   std::vector<int> ntv(nt, nt + count), order(count), rank(count);
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nt[a] > nt[b]; });
   for (int r = 0; r < count; ++r) rank[order[r]] = r;
-  for (int p = 0; p < count; ++p) per[p] = build_tasks(p * JOB_COUNT + kind, nt[p], kinds[kind], kind == 0 ? 1 : nt[p], true);
+  for (int p = 0; p < count; ++p) per[p] = list_tasks(p, nt[p], kind, true);
   std::vector<int4> v = merge_tasks(per, ntv, rank, nearv, whole_max);
   if (out)
     for (size_t t = 0; t < v.size(); ++t) {

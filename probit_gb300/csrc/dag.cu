@@ -61,7 +61,7 @@ constexpr uint64_t MMA_WAIT_NS = 2000000000ull;  // 2 s
 //   L tile (i, j):  w_r K(x_r, x_c) w_c (+ 1 on the diagonal; the upper half
 //                   of a diagonal tile is 0; padding rows/columns have w = 0)
 //   RHS_CROSS rows: K(x*_r, x_c) w_c for the query points (row weight 1)
-//   RHS_VEC row 0:  t;   RHS_IDENT: the identity block of row tile ri
+//   RHS_VEC row 0:  t;   RHS_IDENT: the identity block of row tile rrow
 // The entry loop is one uniform formula over the zero-padded features, so
 // its code stays small whatever the kernel family.
 constexpr int SX_STRIDE = 17;   // DM + 1 (<= 16 + 1), breaks bank conflicts
@@ -108,7 +108,7 @@ __device__ void stage_features(const DagJob& jb, int i, int j, float* sX) {
 // -C_init into the TMEM accumulator (all 8 warps; thread: row r, columns
 // cb .. cb + 63).
 template <int DM>
-__device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, const float* sX) {
+__device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, const float* sX, int rk, int rrow) {
   const float* sXr = sX;
   const float* sXc = sX + T * SX_STRIDE;
   const float* sWr = sXc + T * SX_STRIDE;
@@ -118,8 +118,7 @@ __device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, con
   const int cb = (w >> 2) * 64;
   const uint32_t taddr = tmem + ((uint32_t)((w & 3) * 32) << 16);
   const bool is_rhs = i >= jb.nt;
-  const int ri = i - jb.nt;
-  if (!is_rhs || jb.rhs_kind == RHS_CROSS) {
+  if (!is_rhs || rk == RHS_CROSS) {
     const int matern = jb.sh.kind == PGB_KERNEL_MATERN12;
     const float sv = __ldg(jb.theta + jb.sh.nl);
     const bool diag = !is_rhs && i == j;
@@ -158,10 +157,10 @@ __device__ void cinit_to_tmem(const DagJob& jb, int i, int j, uint32_t tmem, con
         const int c = cb + 32 * h + q;
         const int gj = j * T + c;
         float val;
-        if (jb.rhs_kind == RHS_VEC)
-          val = (ri == 0 && r == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
+        if (rk == RHS_VEC)
+          val = (rrow == 0 && r == 0 && gj < n) ? __ldcg(jb.rhs_vec + gj) : 0.0f;
         else
-          val = (ri == j && r == c) ? 1.0f : 0.0f;
+          val = (rrow == j && r == c) ? 1.0f : 0.0f;
         v[q] = -val;
       }
       tmem_st_32x32(taddr + (uint32_t)(cb + 32 * h), v);
@@ -688,18 +687,24 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const long long ld = jb.ld;
   const bool is_rhs = i >= nt;
   const int ri = i - nt;
+  // the kind of this right-hand-side row tile and its row tile in its own
+  // matrix (RHS_VEC_IDENT: tile 0 is the Newton row, tiles 1.. L^-T rows)
+  const bool zrow = is_rhs && jb.rhs_kind == RHS_VEC_IDENT && ri > 0;
+  const int rk = !is_rhs ? RHS_NONE : jb.rhs_kind == RHS_VEC_IDENT ? (zrow ? RHS_IDENT : RHS_VEC) : jb.rhs_kind;
+  const int rrow = zrow ? ri - 1 : ri;
   const long long lds = 2 * ld;   // row stride of the split matrices
   // fp32 rows (L, and the right-hand-side rows that keep an fp32 copy) and
   // split rows (every tile the tensor cores read later)
-  float* rowbase = is_rhs ? (jb.R ? jb.R + (size_t)ri * T * ld : nullptr) : jb.L + (size_t)i * T * ld;
-  float* rowbase_s = is_rhs ? jb.Rs + (size_t)ri * T * lds : jb.Ls + (size_t)i * T * lds;
-  const int k0 = (is_rhs && jb.rhs_kind == RHS_IDENT) ? ri : 0;
+  float* rowbase = is_rhs ? ((jb.R && !zrow) ? jb.R + (size_t)rrow * T * ld : nullptr) : jb.L + (size_t)i * T * ld;
+  float* rowbase_s = is_rhs ? (zrow ? jb.Zs : jb.Rs) + (size_t)rrow * T * lds : jb.Ls + (size_t)i * T * lds;
+  const int k0 = rk == RHS_IDENT ? rrow : 0;
   const bool withheld = jb.withhold == ((i << 16) | j) + 1;
-  if (!is_rhs && jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0) {
+  const bool reused = jb.reuse_mode == 1 && __ldcg(jb.reuse) != 0;
+  if (reused && (!is_rhs || (jb.zvalid && __ldcg(jb.zvalid) != 0))) {
     // the resident L tile (and, on the diagonal, its inverse) is already the
-    // factor: publish it and move on
+    // factor, or the identity rows were solved with it: publish and move on
     __syncthreads();
-    if (threadIdx.x == 0 && !withheld) st_release(jb.ready + (size_t)i * nt + j, i == j ? 2 : 1);
+    if (threadIdx.x == 0 && !withheld) st_release(jb.ready + (size_t)i * nt + j, (!is_rhs && i == j) ? 2 : 1);
     return;
   }
 
@@ -717,8 +722,8 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
            wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
   };
-  const void* rows_map = is_rhs ? jb.tm_R : jb.tm_L;
-  const int row0 = (is_rhs ? ri : i) * T;
+  const void* rows_map = is_rhs ? (zrow ? jb.tm_Z : jb.tm_R) : jb.tm_L;
+  const int row0 = (is_rhs ? rrow : i) * T;
   TcLoad acc_load = tc_load(rows_map, row0, 0, jb.tm_L, j * T, 0, k0, j, tc);
   acc_load.kfine = kfine;
   if (jb.ptrace && (threadIdx.x == 0 || threadIdx.x == 32) && !is_rhs && i <= j + 1) acc_load.kt = jb.ptrace + (size_t)32 * nt + (size_t)(2 * j + (i - j)) * 8;
@@ -728,9 +733,9 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
     tc_start(tc, acc_load, wait_tile);
   }
   float* sX = reinterpret_cast<float*>(tc.stages + UNION_BYTES);
-  if (!is_rhs || jb.rhs_kind == RHS_CROSS) stage_features<DM>(jb, i, j, sX);
+  if (!is_rhs || rk == RHS_CROSS) stage_features<DM>(jb, i, j, sX);
   __syncthreads();
-  cinit_to_tmem<DM>(jb, i, j, tc.tmem, sX);
+  cinit_to_tmem<DM>(jb, i, j, tc.tmem, sX, rk, rrow);
   __syncthreads();
   if (have_acc) {
     if (!tc_run(tc, acc_load, jb.status, wait_tile, true)) return;
@@ -848,7 +853,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
       put_split(dsts + (size_t)r * lds + c, x);
     }
   }
-  if (is_rhs && jb.rhs_kind == RHS_CROSS && threadIdx.x < T) {
+  if (rk == RHS_CROSS && threadIdx.x < T) {
     // predictive variance terms: squared norm of this tile's part of each row
     const int r = threadIdx.x;
     const int gi = ri * T + r;
@@ -941,7 +946,11 @@ __global__ void __launch_bounds__(DAG_THREADS, 1) dag_factor_kernel(const DagJob
     // for; stops at the first abort of the problem
     const int nt = jb.nt;
     for (int j = 0; j < nt; ++j) {
-      const int nr = jb.rhs_kind == RHS_VEC ? 1 : jb.rhs_kind == RHS_IDENT ? j + 1 : jb.rhs_kind == RHS_CROSS ? jb.nrt : 0;
+      const int nr = jb.rhs_kind == RHS_VEC         ? 1
+                     : jb.rhs_kind == RHS_IDENT     ? j + 1
+                     : jb.rhs_kind == RHS_VEC_IDENT ? j + 2
+                     : jb.rhs_kind == RHS_CROSS     ? jb.nrt
+                                                    : 0;
       for (int i = j; i < nt + nr; ++i) {
         __syncthreads();
         if (threadIdx.x == 0) s_task = ld_relaxed(jb.status + ST_ABORT);

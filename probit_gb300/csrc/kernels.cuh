@@ -10,7 +10,10 @@
 
 namespace pgb {
 
-enum RhsKind { RHS_NONE = 0, RHS_VEC = 1, RHS_IDENT = 2, RHS_CROSS = 3 };
+// RHS_VEC_IDENT: row tile 0 is the Newton right-hand side (RHS_VEC), row
+// tiles 1 .. nt the identity rows (RHS_IDENT) of L^-T, solved in the same
+// launch as the factor they use.
+enum RhsKind { RHS_NONE = 0, RHS_VEC = 1, RHS_IDENT = 2, RHS_CROSS = 3, RHS_VEC_IDENT = 4 };
 
 constexpr int VT = 256;   // points per block of the per-point kernels
 
@@ -47,6 +50,7 @@ struct Prob {
                       // (Newton loop: until it stops; later phases: = *enabled)
   const int* enabled; // 0: the problem is skipped by every kernel (outputs kept)
   int* reuse;         // [0] factor valid, [1] W differs, [2] reuse decision
+  int* zvalid;        // 1: the split L^-T rows (Rz) were solved with the resident factor
   double* part;       // per-block partial sums (ceil(n_pad / VT))
   double* tpart;      // per-tile trace partials (lower tiles x (MAX_D + 1))
   double* lpart;      // per-block likelihood partials (ceil(n / VT) x (MAX_THETA + 2))
@@ -69,6 +73,9 @@ struct DagJob {
   int nrhs;          // RHS rows in use
   float* R;          // nrt*T rows: RHS solution in fp32 (NULL: only the split is kept)
   float* Rs;         // split of the RHS solution rows (row stride 2 ld)
+  float* Zs;         // RHS_VEC_IDENT: split of the identity rows' solution (L^-T)
+  const void* tm_Z;  // RHS_VEC_IDENT: tensor map of Zs
+  const int* zvalid; // RHS_IDENT: when 1 (and *reuse), the identity rows are solved already
   const float* rhs_vec;  // RHS_VEC: t (n)
   const float* Xq;       // RHS_CROSS: query features (nrhs x Dp)
   float* rowsq;          // RHS_CROSS: per row, per tile column sum of squares (nrhs x nt)
@@ -192,6 +199,10 @@ void launch_predictive_dist(const Shape& sh, const float* theta, const float* me
 // factor reuse per active problem: differs |= any(sw != sw_prev); decide
 void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st);
+// After a Newton-step factorisation whose job solved the identity rows too
+// (Gaussian likelihood in an evidence + gradient evaluation): zvalid = 1
+// where the factor was computed in this step without error.
+void launch_mark_z(const Prob* probs, int nprob, cudaStream_t st);
 // enabled problems: status words, reuse flags, active = 1 and (zero_a)
 // a = 0; disabled problems: active = 0, nothing else touched
 void launch_reset_problems(const Prob* probs, const int2* vmap, int nblocks, int zero_a, cudaStream_t st);

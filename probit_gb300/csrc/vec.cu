@@ -66,6 +66,7 @@ __global__ void reset_problems_kernel(const Prob* __restrict__ probs, const int2
       P.status[threadIdx.x] = threadIdx.x == ST_NOTPD_COL ? INT_MAX : 0;
     if (threadIdx.x < 4) P.reuse[threadIdx.x] = 0;
     if (threadIdx.x == 0) *P.active = 1;
+    if (threadIdx.x == 0) *P.zvalid = 0;
   }
 }
 
@@ -804,6 +805,18 @@ __global__ void reuse_mark_valid_kernel(const Prob* __restrict__ probs, int npro
 
 void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st) {
   reuse_mark_valid_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
+}
+
+__global__ void mark_z_kernel(const Prob* __restrict__ probs, int nprob) {
+  const int p = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p >= nprob) return;
+  const Prob& P = probs[p];
+  if (*P.active == 0 || P.sh.lik != PGB_LIK_GAUSSIAN) return;
+  if (P.reuse[2] == 0) *P.zvalid = P.status[ST_CODE] == 0 ? 1 : 0;   // factored (with L^-T) in this step
+}
+
+void launch_mark_z(const Prob* probs, int nprob, cudaStream_t st) {
+  mark_z_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
 }
 
 }  // namespace pgb

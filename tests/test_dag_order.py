@@ -6,8 +6,12 @@ cannot deadlock as long as every dependency comes earlier in the list.  The
 list is built on the host (pgbx_dag_order returns it without a GPU), so this
 is checked here for single problems and for mixed-size batches, for the
 Newton-step (one right-hand-side row), factor-only and L^-T (identity
-right-hand side) task lists.
+right-hand side) task lists, and for the evaluation Newton step of Gaussian
+problems (the Newton row, then the L^-T rows, in one list).
 """
+
+JOB_COUNT = 5
+SLOT = {0: 0, 1: 1, 2: 2, 3: 4}   # task list -> job slot of its problems
 
 import ctypes as C
 
@@ -36,25 +40,28 @@ def _deps(i, j, nt, kind):
             d.append((j, j))
         return d
     r = i - nt
-    k0 = r if kind == 2 else 0   # identity rows start at their own column
+    if kind == 3:                 # row tile 0: the Newton row; then identity rows r - 1
+        k0 = 0 if r == 0 else r - 1
+    else:
+        k0 = r if kind == 2 else 0   # identity rows start at their own column
     return [(i, k) for k in range(k0, j)] + [(j, k) for k in range(k0, j)] + [(j, j)]
 
 
 @pytest.mark.parametrize("near", [None, 1, 2, 4, 16])
-@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
 @pytest.mark.parametrize("nts", [[1], [2], [5], [17], [3, 1, 7, 2, 7], [32, 1, 1, 4, 9, 2, 16]])
 def test_dag_order_topological(native_lib, nts, kind, near):
     tasks = _order(native_lib, nts, kind, near)
     pos = {}
     for t, (job, i, j, _) in enumerate(tasks):
-        p = job // 4
-        assert job % 4 == kind
+        p = job // JOB_COUNT
+        assert job % JOB_COUNT == SLOT[kind]
         key = (p, i, j)
         assert key not in pos, key
         pos[key] = t
     for p, nt in enumerate(nts):
-        nrt = 1 if kind == 0 else (0 if kind == 1 else nt)
-        expect = nt * (nt + 1) // 2 + (nt if kind == 0 else (nt * (nt + 1) // 2 if kind == 2 else 0))
+        tri = nt * (nt + 1) // 2
+        expect = tri + {0: nt, 1: 0, 2: tri, 3: nt + tri}[kind]
         assert sum(1 for k in pos if k[0] == p) == expect
         for (pp, i, j), t in pos.items():
             if pp != p:
@@ -89,20 +96,20 @@ def test_dag_order_near_depth(native_lib):
     assert native_lib.pgbx_dag_order(arr, 1, 1, (C.c_int32 * 1)(0), 0, None) == -1   # depth 0 is refused
 
 
-@pytest.mark.parametrize("kind", [0, 1, 2])
+@pytest.mark.parametrize("kind", [0, 1, 2, 3])
 def test_small_problems_run_whole(native_lib, kind):
     """Problems of at most whole_max tile rows are one task (i = -1) in the
     first stage; the others keep every tile task, in the same order."""
     nts = [5, 1, 2, 3, 2]
     tasks = _order(native_lib, nts, kind, whole_max=2)
-    whole = [int(job) // 4 for job, i, _, _ in tasks if i == -1]
+    whole = [int(job) // JOB_COUNT for job, i, _, _ in tasks if i == -1]
     assert sorted(whole) == [1, 2, 4]
     # first stage: the diagonal tile of column 0 of the large problems and the
     # whole problems, by size
-    first = [(int(job) // 4, int(i)) for job, i, _, _ in tasks[:5]]
+    first = [(int(job) // JOB_COUNT, int(i)) for job, i, _, _ in tasks[:5]]
     assert first == [(0, 0), (3, 0), (2, -1), (4, -1), (1, -1)]
-    rest = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in tasks if i != -1]
+    rest = [(int(job) // JOB_COUNT, int(i), int(j)) for job, i, j, _ in tasks if i != -1]
     assert {p for p, _, _ in rest} == {0, 3}
     full = _order(native_lib, nts, kind, whole_max=0)
-    kept = [(int(job) // 4, int(i), int(j)) for job, i, j, _ in full if int(job) // 4 in (0, 3)]
+    kept = [(int(job) // JOB_COUNT, int(i), int(j)) for job, i, j, _ in full if int(job) // JOB_COUNT in (0, 3)]
     assert rest == kept
