@@ -82,6 +82,7 @@ enum JobSlot { JOB_VEC = 0, JOB_NONE = 1, JOB_IDENT = 2, JOB_CROSS = 3, JOB_VEC_
 // likelihood solve their L^-T rows with the factor of the first step, which
 // is final since W does not change).
 enum TaskList { TL_STEP = 0, TL_NONE = 1, TL_IDENT = 2, TL_VG_STEP = 3, TL_COUNT = 4 };
+constexpr int kZLag = 4;
 enum Counter { C_DAG = 0, C_TRSV_T = 1, C_PREDICT = 2, C_TRSV_L = 3, C_SYRK = 4, C_COUNT = 8 };
 
 constexpr int kStatusWords = 8;
@@ -181,6 +182,7 @@ struct Engine {
   int ntasks[TL_COUNT] = {};
   int* zvalid_all = nullptr;
   int has_gauss = 0;                       // some problem has a Gaussian likelihood
+  int zlag = kZLag;                        // columns of delay of the identity rows solved beside a factor
   int2* claims = nullptr;
   int nclaims = 0;
   // graphs
@@ -227,7 +229,9 @@ std::vector<int4> build_tasks(int job, int nt, int kind, int nrt, bool with_L) {
       for (int r = 0; r < nrt; ++r) v.push_back(make_int4(job, nt + r, j, 0));
     } else if (kind == RHS_VEC_IDENT) {
       v.push_back(make_int4(job, nt, j, 0));
-      for (int r = 0; r <= j; ++r) v.push_back(make_int4(job, nt + 1 + r, j, 0));
+      // w = 1: an identity row solved beside the factorisation (handed out
+      // later, see merge_tasks)
+      for (int r = 0; r <= j; ++r) v.push_back(make_int4(job, nt + 1 + r, j, 1));
     }
   }
   return v;
@@ -268,8 +272,14 @@ int dag_stage(int i, int j, int nt, int near) {
 // then column, then row.
 // A problem of at most `whole_max` tile rows becomes one task (job, -1, 0, 0)
 // at stage 0: one block runs all its tiles in order (no waits on other blocks).
+// Identity rows solved beside a factorisation (task w = 1) go `zlag` columns
+// later than the other right-hand-side tiles of their column: they wait for
+// their row's previous tile and for the inverse of the diagonal tile, and a
+// block holding one would otherwise sit waiting while factorisation tiles
+// are handed out.  Their dependencies all sit in earlier stages still.
 std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const std::vector<int>& nt,
-                              const std::vector<int>& rank, const std::vector<int>& near, int whole_max) {
+                              const std::vector<int>& rank, const std::vector<int>& near, int whole_max,
+                              int zlag = 0) {
   struct Key {
     int stage, rank, j, i;
     int4 t;
@@ -279,7 +289,8 @@ std::vector<int4> merge_tasks(const std::vector<std::vector<int4>>& per, const s
     if (nt[p] <= whole_max && !per[p].empty())
       all.push_back(Key{0, rank[p], 0, -1, make_int4(per[p][0].x, -1, 0, 0)});
     else
-      for (const int4& t : per[p]) all.push_back(Key{dag_stage(t.y, t.z, nt[p], near[p]), rank[p], t.z, t.y, t});
+      for (const int4& t : per[p])
+        all.push_back(Key{dag_stage(t.y, t.z, nt[p], near[p]) + (t.w ? 2 * zlag : 0), rank[p], t.z, t.y, t});
   std::sort(all.begin(), all.end(), [](const Key& a, const Key& b) {
     if (a.stage != b.stage) return a.stage < b.stage;
     if (a.rank != b.rank) return a.rank < b.rank;
@@ -492,7 +503,7 @@ void build_task_lists(Engine& e) {
       const bool gauss = e.desc[p].likelihood == PGB_LIK_GAUSSIAN;
       per[p] = list_tasks(p, e.nt[p], k, gauss);
     }
-    e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near, e.whole_max);
+    e.h_tasks[k] = merge_tasks(per, e.nt, e.rank, e.near, e.whole_max, e.zlag);
     e.ntasks[k] = (int)e.h_tasks[k].size();
   }
 }
@@ -629,6 +640,9 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
     // block (0: every tile is its own task)
     const char* wv = std::getenv("PGB_WHOLE_TILES");
     if (wv && wv[0] >= '0' && wv[0] <= '9') e.whole_max = std::atoi(wv);
+    // PGB_ZLAG=k: identity rows solved beside a factorisation go k columns late
+    const char* zv = std::getenv("PGB_ZLAG");
+    if (zv && zv[0] >= '0' && zv[0] <= '9') e.zlag = std::atoi(zv);
   }
   build_task_lists(e);
   // merged solve claims: position by position, problems by rank
@@ -1531,7 +1545,7 @@ int pgbx_dag_order(const int32_t* nt, int32_t count, int32_t kind, const int32_t
   std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return nt[a] > nt[b]; });
   for (int r = 0; r < count; ++r) rank[order[r]] = r;
   for (int p = 0; p < count; ++p) per[p] = list_tasks(p, nt[p], kind, true);
-  std::vector<int4> v = merge_tasks(per, ntv, rank, nearv, whole_max);
+  std::vector<int4> v = merge_tasks(per, ntv, rank, nearv, whole_max, kZLag);
   if (out)
     for (size_t t = 0; t < v.size(); ++t) {
       out[4 * t] = v[t].x;

@@ -54,12 +54,15 @@ def handle_bytes(n, d, kind, grad=True, m=0):
     Fp = -(-F // 4) * 4
     mat = 4 * npad * npad
     vec = 4 * npad * (22 + Fp)
-    b = mat + 4 * nt * 128 * 128 + 4 * 128 * npad + vec + 8 * npad * 80 + 16 * nt * nt + 4096
+    # L in fp32 and as its TF32 hi/lo split, the same for the diagonal
+    # inverses and the Newton right-hand-side row tile, vectors, partial sums,
+    # tile flags
+    b = 3 * mat + 3 * 4 * nt * 128 * 128 + 3 * 4 * 128 * npad + vec + 8 * npad * 80         + 4 * ((2 * nt + 1) * nt + 2 * nt) + 16 * nt * nt + 4096
     if grad:
-        b += 2 * mat
+        b += 3 * mat          # split L^-T and B^-1
     if m > 0:
         mpad = -(-m // 128) * 128
-        b += 4 * mpad * (npad + nt + Fp + d + 2) + 4 * (nt + mpad // 128) * nt
+        b += 4 * mpad * (2 * npad + nt + Fp + d + 2) + 4 * (nt + mpad // 128) * nt
     return b
 
 
