@@ -187,7 +187,7 @@ struct Engine {
   int nclaims = 0;
   // graphs
   cudaGraphExec_t gexec[OP_COUNT] = {};
-  cudaStream_t cap_s = nullptr, cap_s2 = nullptr;
+  cudaStream_t cap_s = nullptr, cap_s2 = nullptr, cap_s3 = nullptr;   // capture streams (s3: nested bodies)
   int grad_ready = 0;
   int eager = 0;                           // PGB_EAGER=1: kernels launched directly, host-driven loop
   unsigned long long* trace = nullptr;     // PGB_TRACE=1: per-task timestamps of the DAG
@@ -483,6 +483,7 @@ void engine_free(Engine& e) {
     cudaStreamDestroy(e.cap_s);
   }
   if (e.cap_s2) cudaStreamDestroy(e.cap_s2);
+  if (e.cap_s3) cudaStreamDestroy(e.cap_s3);
   e.arena = e.garena = nullptr;
   e.trace = nullptr;
 }
@@ -657,6 +658,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
   // one arena
   CU_TRY(cudaStreamCreateWithFlags(&e.cap_s, cudaStreamNonBlocking));
   CU_TRY(cudaStreamCreateWithFlags(&e.cap_s2, cudaStreamNonBlocking));
+  CU_TRY(cudaStreamCreateWithFlags(&e.cap_s3, cudaStreamNonBlocking));
   const size_t bytes = layout(e, 0);
   PGB_TRY(ws_alloc(e.cap_s, &e.arena, bytes));
   layout(e, reinterpret_cast<uintptr_t>(e.arena));
@@ -735,6 +737,42 @@ void enq_dag(Engine& e, int list, cudaStream_t s) {
                     dag_grid(e, e.ntasks[list]), s);
 }
 
+// A conditional handle of the graph being captured on s, with the value it
+// takes at each launch of the graph.
+int cond_handle(cudaStream_t s, unsigned default_value, cudaGraphConditionalHandle* h) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg = nullptr;
+  CU_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, nullptr, nullptr, nullptr));
+  CU_TRY(cudaGraphConditionalHandleCreate(h, cg, default_value, cudaGraphCondAssignDefault));
+  return PGB_OK;
+}
+
+// Add a conditional node (WHILE or IF) on handle h at the current point of
+// the capture on s, whose body is captured on s2 by `body(s2)`.
+template <class Body>
+int capture_cond(cudaStream_t s, cudaStream_t s2, cudaGraphConditionalHandle h, cudaGraphConditionalNodeType type,
+                 Body body) {
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cg = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  CU_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams cp = {};
+  cp.type = cudaGraphNodeTypeConditional;
+  cp.conditional.handle = h;
+  cp.conditional.type = type;
+  cp.conditional.size = 1;
+  cudaGraphNode_t cnode;
+  CU_TRY(cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp));
+  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
+  CU_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
+  CU_TRY(cudaStreamBeginCaptureToGraph(s2, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
+  body(s2);
+  cudaGraph_t body_out = nullptr;
+  CU_TRY(cudaStreamEndCapture(s2, &body_out));
+  return PGB_OK;
+}
+
 void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, int use_cond, int list) {
   // f += K da: f follows a by the updates (f = 0, da = a at the start), so
   // the rounding of f shrinks with the step instead of staying at the float32
@@ -745,7 +783,18 @@ void enq_newton_step(Engine& e, cudaStream_t s, cudaGraphConditionalHandle h, in
   // bitwise-unchanged W keeps the resident factor
   launch_reuse_check(e.probs, e.vmap, e.nvb, e.nprob, s);
   // new W: L L^T = B and w = L^-1 t in one factorisation (skipped on reuse)
-  enq_dag(e, list, s);
+  if (use_cond) {
+    // only when some problem needs a new factor this step (after the first
+    // steps most have stopped or reuse theirs, and a launch that skips every
+    // task still walks the whole merged list)
+    cudaGraphConditionalHandle hf;
+    if (cond_handle(s, 0, &hf) == PGB_OK) {
+      launch_need_factor(e.probs, e.nprob, hf, s);
+      capture_cond(s, e.cap_s3, hf, cudaGraphCondTypeIf, [&](cudaStream_t bs) { enq_dag(e, list, bs); });
+    }
+  } else {
+    enq_dag(e, list, s);
+  }
   if (list == TL_VG_STEP) launch_mark_z(e.probs, e.nprob, s);
   launch_reuse_mark_valid(e.probs, e.nprob, s);
   // reused W: w = L^-1 t by the forward wavefront solve; then x = L^-T w
@@ -913,27 +962,9 @@ int run_eager(Engine& e, int op, cudaStream_t s) {
 // condition (the loop runs at least once).
 template <class Body>
 int capture_while(cudaStream_t s, cudaStream_t s2, Body body) {
-  cudaStreamCaptureStatus cs;
-  cudaGraph_t cg = nullptr;
-  const cudaGraphNode_t* deps = nullptr;
-  size_t ndeps = 0;
-  CU_TRY(cudaStreamGetCaptureInfo(s, &cs, nullptr, &cg, &deps, nullptr, &ndeps));
   cudaGraphConditionalHandle h;
-  CU_TRY(cudaGraphConditionalHandleCreate(&h, cg, 1, cudaGraphCondAssignDefault));
-  cudaGraphNodeParams cp = {};
-  cp.type = cudaGraphNodeTypeConditional;
-  cp.conditional.handle = h;
-  cp.conditional.type = cudaGraphCondTypeWhile;
-  cp.conditional.size = 1;
-  cudaGraphNode_t cnode;
-  CU_TRY(cudaGraphAddNode(&cnode, cg, deps, nullptr, ndeps, &cp));
-  cudaGraph_t bodyg = cp.conditional.phGraph_out[0];
-  CU_TRY(cudaStreamUpdateCaptureDependencies(s, &cnode, nullptr, 1, cudaStreamSetCaptureDependencies));
-  CU_TRY(cudaStreamBeginCaptureToGraph(s2, bodyg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed));
-  body(s2, h);
-  cudaGraph_t body_out = nullptr;
-  CU_TRY(cudaStreamEndCapture(s2, &body_out));
-  return PGB_OK;
+  PGB_TRY(cond_handle(s, 1, &h));
+  return capture_cond(s, s2, h, cudaGraphCondTypeWhile, [&](cudaStream_t bs) { body(bs, h); });
 }
 
 // Capture the graph of one operation.

@@ -199,6 +199,9 @@ void launch_predictive_dist(const Shape& sh, const float* theta, const float* me
 // factor reuse per active problem: differs |= any(sw != sw_prev); decide
 void launch_reuse_check(const Prob* probs, const int2* vmap, int nblocks, int nprob, cudaStream_t st);
 void launch_reuse_mark_valid(const Prob* probs, int nprob, cudaStream_t st);
+// Graph condition = some active problem factors in this Newton step (its
+// reuse decision is 0).
+void launch_need_factor(const Prob* probs, int nprob, cudaGraphConditionalHandle cond, cudaStream_t st);
 // After a Newton-step factorisation whose job solved the identity rows too
 // (Gaussian likelihood in an evidence + gradient evaluation): zvalid = 1
 // where the factor was computed in this step without error.

@@ -819,4 +819,18 @@ void launch_mark_z(const Prob* probs, int nprob, cudaStream_t st) {
   mark_z_kernel<<<ceil_div(nprob, 128), 128, 0, st>>>(probs, nprob);
 }
 
+__global__ void need_factor_kernel(const Prob* __restrict__ probs, int nprob, cudaGraphConditionalHandle cond) {
+  bool need = false;
+  for (int p = threadIdx.x; p < nprob; p += blockDim.x) {
+    const Prob& P = probs[p];
+    if (*P.active != 0 && P.reuse[2] == 0) need = true;
+  }
+  need = __syncthreads_or(need) != 0;
+  if (threadIdx.x == 0) cudaGraphSetConditional(cond, need ? 1u : 0u);
+}
+
+void launch_need_factor(const Prob* probs, int nprob, cudaGraphConditionalHandle cond, cudaStream_t st) {
+  need_factor_kernel<<<1, 256, 0, st>>>(probs, nprob, cond);
+}
+
 }  // namespace pgb
