@@ -72,9 +72,12 @@ def parse():
     ap.add_argument("--hyperopt", type=int, default=256,
                     help="problems of the lockstep L-BFGS hyperparameter workload (0: skip)")
     ap.add_argument("--hyperopt-steps", type=int, default=50)
-    ap.add_argument("--serve-seconds", type=float, default=3.0,
+    ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="arrival window of the serving workload at 2000 req/s (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=12)
+    ap.add_argument("--serve-max-large", type=int, default=1,
+                    help="large (n > 2048) requests served at once (the rest of the GPU serves small ones)")
+    ap.add_argument("--serve-large-blocks", type=int, default=64, help="SM share of each large request's launches")
     ap.add_argument("--no-c0", action="store_true", help="skip the config-0 section")
     return ap.parse_args()
 
@@ -547,12 +550,14 @@ def run_serving(args, dev):
     from probit_gb300 import serving as S
     from probit_gb300 import workloads as Wk
 
-    out = {"workers": args.serve_workers, "pool": 256}
+    out = {"workers": args.serve_workers, "pool": 256, "max_large": args.serve_max_large,
+           "large_blocks": args.serve_large_blocks}
     for tag, rate, dur, seed in (("offered_2000_per_s", 2000.0, args.serve_seconds, 4),
                                  ("offered_150_per_s", 150.0, max(5.0, args.serve_seconds), 5)):
         probs, reqs = Wk.serving_c4(rate=rate, duration=dur, pool=256, seed=seed, device=dev)
         gc.collect()   # the previous run's objects are not collected during this one
-        srv = S.Server(workers=args.serve_workers)
+        srv = S.Server(workers=args.serve_workers, max_large=args.serve_max_large,
+                       large_blocks=args.serve_large_blocks, warm_large=True)
         try:
             t0 = time.perf_counter()
             srv.replay([S.Request(0.0, "fit", k, p) for k, p in enumerate(probs)], realtime=False)

@@ -14,8 +14,11 @@ one GPU:
   CUDA stream, so the kernels of different requests overlap on the device
   (the tile-DAG launches of small problems use a few SMs each); requests of
   small problems (n <= ``small_n``) go to higher-priority streams and are
-  taken first, some workers take only them, and large problems' launches are
-  capped at ``large_blocks`` persistent blocks so small ones run beside them;
+  taken first, some workers take only them, at most ``max_large`` large
+  problems run at a time and their launches are capped at ``large_blocks``
+  persistent blocks, so the SMs left over always serve small requests (a
+  large request's latency then absorbs the overload, a small one's does
+  not);
 * a model is used by one request at a time (a handle is not thread-safe);
   other requests for it wait in the queue.
 
@@ -146,7 +149,7 @@ class Server:
     """Continuous-batching request server on the current CUDA device."""
 
     def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True,
-                 warm_rows=4096):
+                 warm_rows=4096, max_large=1, warm_large=False):
         import torch
 
         self.torch = torch
@@ -157,12 +160,18 @@ class Server:
         self.used = 0
         self.small_n = small_n
         self.large_blocks = large_blocks   # SM share of the launches of a problem with n > small_n
+        self.max_large = max_large         # large requests running at once (0: no limit)
+        self.large_running = 0
         # after the first fit of a small model, its evidence + gradient handle is
         # created and its graph captured (one evaluation at the fitted
         # hyperparameters) and its predict workspace sized for `warm_rows`
         # test points (one prediction) before the model is released, so no
         # request pays a first-use graph build or workspace allocation
         self.warm_small = warm_small
+        # the same warm-up for large models (their first evidence + gradient
+        # request otherwise grows the memory pool and captures a graph while
+        # other requests run)
+        self.warm_large = warm_large
         self.warm_rows = int(warm_rows)
         self.warm_errors = []          # warm-ups that failed (the first request then builds instead)
         self.busy_workers = 0
@@ -187,8 +196,11 @@ class Server:
                 role = "small_first"
             else:
                 role = "any"
-            stream = torch.cuda.Stream(device=self.device, priority=lo if role == "any" else hi)
-            t = threading.Thread(target=self._worker, args=(stream, role), daemon=True)
+            # small requests on a high-priority stream, large ones on a low-priority
+            # one: blocks of small requests' launches are scheduled first
+            streams = (torch.cuda.Stream(device=self.device, priority=hi),
+                       torch.cuda.Stream(device=self.device, priority=lo))
+            t = threading.Thread(target=self._worker, args=(streams, role), daemon=True)
             self.workers.append(t)
             t.start()
 
@@ -282,16 +294,18 @@ class Server:
         do not fit in memory yet) are stepped over and put back."""
         skipped = []
         found = None
+        large_ok = not self.max_large or self.large_running < self.max_large
         for _ in range(scan):
             heaps = self.heaps
+            big = heaps[1] if large_ok else []
             if role == "small":
                 h = heaps[0]
             elif role == "small_first":
-                h = heaps[0] if heaps[0] else heaps[1]
-            elif heaps[0] and heaps[1]:
-                h = heaps[0] if heaps[0][0] < heaps[1][0] else heaps[1]
+                h = heaps[0] if heaps[0] else big
+            elif heaps[0] and big:
+                h = heaps[0] if heaps[0][0] < big[0] else big
             else:
-                h = heaps[0] if heaps[0] else heaps[1]
+                h = heaps[0] if heaps[0] else big
             if not h:
                 break
             item = heapq.heappop(h)
@@ -315,6 +329,8 @@ class Server:
             m = _Model(req.model, req.problem)
             self.models[req.model] = m
         m.busy = True
+        if req.n > self.small_n:
+            self.large_running += 1
         fit, vg, cap = self._plan(req, m)
         grow = m.footprint(fit, vg, cap) - m.bytes
         self.used += grow
@@ -322,7 +338,7 @@ class Server:
         return req, m
 
     # -- execution ----------------------------------------------------------------
-    def _worker(self, stream, role):
+    def _worker(self, streams, role):
         torch = self.torch
         torch.cuda.set_device(self.device)
         while True:
@@ -336,6 +352,7 @@ class Server:
                         break
                     self.lock.wait(timeout=0.002)
             req, m = got
+            stream = streams[0] if req.n <= self.small_n else streams[1]
             req.start = self.now()
             try:
                 with torch.cuda.stream(stream):
@@ -344,8 +361,12 @@ class Server:
             except Exception as exc:   # reported per request
                 req.error = repr(exc)
             req.done = self.now()
-            warm = (self.warm_small and req.kind == "fit" and req.error is None and m.hvg is None
-                    and m.problem.n <= self.small_n)
+            if req.n > self.small_n:
+                with self.lock:
+                    self.large_running -= 1
+                    self.lock.notify_all()
+            warm = (req.kind == "fit" and req.error is None and m.hvg is None
+                    and (self.warm_large if m.problem.n > self.small_n else self.warm_small))
             with self.lock:
                 if warm:   # account the handles first; skip the warm-up if they do not fit
                     cap = max(m.cap_m, -(-self.warm_rows // 128) * 128)
