@@ -42,9 +42,9 @@ ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
 METRIC = "Laplace evidence+grad solves/s"
-# dram__bytes_read.sum + dram__bytes_write.sum of one N = 8192 factorisation
-# launch (ncu capture summarised in profiles/dag_factor_kernel_gaussian_N8192.md)
-FACTOR_TRAFFIC_N8192 = 85.472512e6 + 116.641792e6
+# dram__bytes_read.sum + dram__bytes_write.sum of one N = 8192 factor-only
+# launch (one-pass ncu capture, profiles/launches_gaussian_N8192_evidence_grad.md)
+FACTOR_TRAFFIC_N8192 = 3.08e9 + 0.44347e9
 # nominal dense TF32 tensor rate of a GB300 (TFLOP/s); a 3xTF32 product issues
 # three TF32 MMAs per algorithmic one
 TF32_NOMINAL_TFLOPS = 1100.0
