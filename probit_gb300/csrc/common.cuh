@@ -16,6 +16,9 @@
 namespace pgb {
 
 constexpr int T = 128;           // tile edge of every blocked matrix
+// k-columns of one tensor-core pipeline chunk: one tensor-map box of 128
+// rows, stored with a 64-byte swizzle (16 fp32 a row) or a 128-byte one (32)
+constexpr int CHUNK_COLS = 32;
 constexpr int MAX_D = 16;        // input dimensions handled by the kernels
 constexpr int MAX_THETA = 64;    // entries of one hyperparameter block
 

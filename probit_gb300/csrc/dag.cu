@@ -28,16 +28,19 @@ namespace pgb {
 constexpr int DAG_THREADS = 256;
 constexpr int SC_LD = T + 1;
 // tensor-core pipeline, unioned with the epilogue tiles sC, sL: NST stages,
-// each one 32-column chunk of the A and B operands as their TF32 hi and lo
-// parts (four 128 x 32 fp32 boxes, 16 KB each), loaded straight from the
+// each one CHUNK_COLS-column chunk of the A and B operands as their TF32 hi
+// and lo parts (four 128 x CHUNK_COLS fp32 boxes), loaded straight from the
 // split operand matrices (the epilogue that publishes a tile also writes its
 // split).  A stage is reloaded once the MMAs of its chunk completed.
-constexpr int NST = 3;
-constexpr int CHUNK_BYTES = T * 128;             // 128 rows x 32 fp32
+// (16-column chunks, six 32 KB stages with five in flight, measured 8-10%
+// slower than 32-column ones in three 64 KB stages.)
+constexpr int CHUNK_BYTES = T * CHUNK_COLS * 4;  // 128 rows x CHUNK_COLS fp32
 constexpr int STAGE_BYTES = 4 * CHUNK_BYTES;     // A hi, A lo, B hi, B lo
+constexpr int NST = 196608 / STAGE_BYTES;        // 192 KB of stages
 constexpr int UNION_BYTES = NST * STAGE_BYTES;   // >= 2 * T * SC_LD * 4
-constexpr int CHUNKS_PER_KT = T / 32;            // chunks of one 128-wide k-tile
-constexpr int CHUNKS_PER_PART = 2;               // chunks summed in one partial accumulator
+constexpr int CHUNKS_PER_KT = T / CHUNK_COLS;    // chunks of one 128-wide k-tile
+constexpr int CHUNKS_PER_PART = 64 / CHUNK_COLS; // chunks summed in one partial accumulator (64 k-columns)
+constexpr int KSTEPS = CHUNK_COLS / 8;           // MMA k-steps (8 TF32 each) of a chunk
 constexpr int DRAIN_WARPS = DAG_THREADS / 32 - 2;   // warps 2..7 fold the partial sums
 constexpr int NBARS = 2 * NST + 4;               // full, empty [NST]; part full, part free [2]
 // tensor memory: the running 128 x 128 fp32 sum in columns 0..127 and two
@@ -471,8 +474,9 @@ struct TcCtx {
 
 // Operands of one accumulation acc += sum_{k0 <= k < k1} A_k B_k^T: A_k is
 // the 128 x 128 tile of the split matrix behind `amap` at rows arow..,
-// logical columns acol + k*T.., B_k likewise.  Chunk c (32 columns) of the
-// loop is k-tile k0 + c / 4, columns (c % 4) * 32.
+// logical columns acol + k*T.., B_k likewise.  Chunk c (CHUNK_COLS columns)
+// of the loop is k-tile k0 + c / CHUNKS_PER_KT, columns
+// (c % CHUNKS_PER_KT) * CHUNK_COLS.
 struct TcLoad {
   const void* amap;
   const void* bmap;
@@ -522,7 +526,7 @@ __device__ __forceinline__ bool tc_issue(const TcCtx& tc, TcLoad& l, int c, Wait
     fence_proxy_async_global();
     if (l.kt && c == l.nchunks - CHUNKS_PER_KT) l.kt[0] = global_ns();
   }
-  const int col = kt * T + q * 32;
+  const int col = kt * T + q * CHUNK_COLS;
   const int ax = split_col(l.acol + col), bx = split_col(l.bcol + col);
   uint8_t* stage = tc.stages + s * STAGE_BYTES;
   mbar_arrive_expect_tx(tc.full + s, 4 * CHUNK_BYTES);
@@ -543,8 +547,12 @@ __device__ __forceinline__ bool tc_start(const TcCtx& tc, TcLoad& l, WaitTile& w
   return true;
 }
 
-// Thread 0: the 12 MMAs of one 32-wide k-chunk into the partial accumulator
-// at tensor-memory column `part`, 4 k-steps x (hi lo, lo hi, hi hi), the
+__device__ __forceinline__ uint64_t sdesc_op(uint32_t saddr) {
+  return CHUNK_COLS == 32 ? sdesc_sw128(saddr) : sdesc_sw64(saddr);
+}
+
+// Thread 0: the MMAs of one k-chunk into the partial accumulator at
+// tensor-memory column `part`, KSTEPS k-steps x (hi lo, lo hi, hi hi), the
 // small terms first so they are not lost against the large one (a fourth
 // product lo lo changed no measured error).  Both operands come from the
 // stage in shared memory.
@@ -553,11 +561,11 @@ __device__ __forceinline__ void issue_chunk(const TcCtx& tc, const uint8_t* stag
   const uint32_t b_hi = a_hi + 2 * CHUNK_BYTES, b_lo = a_hi + 3 * CHUNK_BYTES;
   const uint32_t d = tc.tmem + part;
 #pragma unroll
-  for (int ks = 0; ks < 4; ++ks) {
+  for (int ks = 0; ks < KSTEPS; ++ks) {
     const uint32_t o = ks * 32;   // bytes into the swizzled rows
-    umma_tf32(d, sdesc_sw128(a_hi + o), sdesc_sw128(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
-    umma_tf32(d, sdesc_sw128(a_lo + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
-    umma_tf32(d, sdesc_sw128(a_hi + o), sdesc_sw128(b_hi + o), IDESC_128x128, 1u);
+    umma_tf32(d, sdesc_op(a_hi + o), sdesc_op(b_lo + o), IDESC_128x128, (first && ks == 0) ? 0u : 1u);
+    umma_tf32(d, sdesc_op(a_lo + o), sdesc_op(b_hi + o), IDESC_128x128, 1u);
+    umma_tf32(d, sdesc_op(a_hi + o), sdesc_op(b_hi + o), IDESC_128x128, 1u);
   }
 }
 
@@ -620,7 +628,7 @@ __device__ bool tc_run(TcCtx& tc, TcLoad& l, int* status, WaitTile& wait_tile, b
       // partial u's buffer was last used by partial u - 2: wait for its fold
       if (q == 0 && u >= 2 && !mbar_wait_bounded(tc.pfree + pb, ((u - 2u) >> 1) & 1u, MMA_WAIT_NS)) bad = true;
       if (!mbar_wait_bounded(tc.full + s, (g / NST) & 1u, MMA_WAIT_NS)) bad = true;
-      if (l.kt && c >= n - CHUNKS_PER_KT) l.kt[1 + c - (n - CHUNKS_PER_KT)] = global_ns();
+      if (l.kt && c >= n - 4) l.kt[1 + c - (n - 4)] = global_ns();
       tc_fence_after();
       issue_chunk(tc, tc.stages + s * STAGE_BYTES, PART_COL + 128u * pb, q == 0);
       umma_commit(tc.empty + s);
@@ -718,7 +726,7 @@ __device__ void dag_task(const DagJob& jb, int i, int j, TcCtx& tc, int* s_ok, i
   const int kfine = (!is_rhs && i == j && j > 0) ? j - 1 : -1;
   const int* xprog = jb.progress + nt;
   auto wait_tile = [=](int k, int q) {
-    if (k == kfine) return wait_flag_geq(xprog + k, q + 1, status);
+    if (k == kfine) return wait_flag_geq(xprog + k, (q * CHUNK_COLS) / 32 + 1, status);
     return wait_flag_geq(ready + (size_t)i * nt + k, 1, status) &&
            wait_flag_geq(ready + (size_t)j * nt + k, 1, status);
   };

@@ -118,8 +118,9 @@ struct DagJob {
 int validate_desc(const pgb_desc* d);
 
 // Tensor map of a row-major fp32 matrix (rows x cols, row stride ld floats)
-// with 128-row x 32-column boxes and 128-byte swizzle, the layout the
-// tensor-core operand loads expect.  Host code; false if the driver refuses.
+// with 128-row x CHUNK_COLS-column boxes and the swizzle of that row width,
+// the layout the tensor-core operand loads expect.  Host code; false if the
+// driver refuses.
 bool make_tile_map(void* map128, const float* base, long long rows, long long cols, long long ld);
 
 // gram.cu ---------------------------------------------------------------------

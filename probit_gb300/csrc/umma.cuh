@@ -66,6 +66,18 @@ __device__ __forceinline__ uint64_t sdesc_sw128(uint32_t saddr) {
   return d;
 }
 
+// The same for a K-major SW64 operand (64-byte rows, 8-row groups 512 B
+// apart; the chunk base 512-byte aligned).
+__device__ __forceinline__ uint64_t sdesc_sw64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr >> 4) & 0x3FFFu);
+  d |= (uint64_t)1u << 16;                  // LBO (unused for swizzled K-major)
+  d |= (uint64_t)(512u >> 4) << 32;         // SBO
+  d |= (uint64_t)1u << 46;                  // descriptor version
+  d |= (uint64_t)4u << 61;                  // layout: SWIZZLE_64B
+  return d;
+}
+
 // ---------------------------------------------------------------- MMA
 __device__ __forceinline__ void umma_tf32(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
                                           uint32_t accumulate) {
