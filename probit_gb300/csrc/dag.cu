@@ -343,52 +343,65 @@ __device__ __forceinline__ void publish_panel(const float* sC, float* dst, long 
   if (threadIdx.x == 0) st_release(progress, jb / 32 + 1);
 }
 
+// Trailing update of the lower triangle of sC by panel jp (columns jp ..
+// jp+31 of L, already in sC): C[r][c] -= sum_m L[r][jp+m] L[c][jp+m] for the
+// 4 x 4 register blocks with columns c0 in [c_lo, c_hi) and rows r0 >= c0
+// (rows up to 127), by `nthr` threads numbered from 0 by `t`.
+__device__ __forceinline__ void trail_update(float* sC, int jp, int c_lo, int c_hi, int t, int nthr) {
+  const int nbc = (c_hi - c_lo) / 4;                 // column blocks
+  const int nbr = (T - c_lo) / 4;                    // row blocks from c_lo
+  for (int blk = t; blk < nbr * nbc; blk += nthr) {
+    const int br = blk / nbc, bc = blk % nbc;
+    const int r0 = c_lo + br * 4, c0 = c_lo + bc * 4;
+    if (c0 > r0) continue;
+    float acc[4][4];
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
+#pragma unroll 8
+    for (int m = 0; m < 32; ++m) {
+      float a[4], b[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        a[q] = sC[(r0 + q) * SC_LD + jp + m];
+        b[q] = sC[(c0 + q) * SC_LD + jp + m];
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+#pragma unroll
+        for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
+    }
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
+  }
+}
+
+// Panel by panel; the trailing update of panel p - 1 is split: its part on
+// panel p's columns goes first (all threads), the rest (columns beyond
+// panel p) runs on the warps the column loop of panel p leaves idle
+// (threads 128 - jb .. 255), at the same time.  Both parts only read
+// columns of panel p - 1 and write disjoint entries.
 __device__ void potrf_tile(float* sC, float* sbuf, int col0, int* status, float* dst, long long ld, float* dsts,
                            long long lds, int* progress, unsigned long long* pt = nullptr) {
   const int tid = threadIdx.x;
   for (int jb = 0; jb < T; jb += 32) {
     if (pt && tid == 0) pt[(jb / 32) * 3 + 0] = global_ns();
-    panel_potrf(sC, jb, sbuf, col0 + jb, status);
+    if (jb > 0) {
+      trail_update(sC, jb - 32, jb, jb + 32, tid, DAG_THREADS);
+      __syncthreads();
+    }
+    const int nr = T - jb;
+    if (tid < nr)
+      panel_potrf(sC, jb, sbuf, col0 + jb, status);
+    else if (jb > 0 && jb + 32 < T)
+      trail_update(sC, jb - 32, jb + 32, T, tid - nr, DAG_THREADS - nr);
     __syncthreads();
     if (pt && tid == 0) pt[(jb / 32) * 3 + 1] = global_ns();
     publish_panel(sC, dst, ld, dsts, lds, progress, jb);
     if (pt && tid == 0) pt[(jb / 32) * 3 + 2] = global_ns();
-    const int rem = T - jb - 32;
-    if (rem > 0) {
-      // trailing update of the lower triangle of rows/columns jb+32.. by
-      // 4 x 4 register blocks, lower-triangle blocks only
-      const int nb = rem / 4;
-      for (int blk = tid; blk < nb * (nb + 1) / 2; blk += DAG_THREADS) {
-        int br = (int)((sqrtf(8.0f * blk + 1.0f) - 1.0f) * 0.5f);
-        while (br * (br + 1) / 2 > blk) --br;
-        while ((br + 1) * (br + 2) / 2 <= blk) ++br;
-        const int bc = blk - br * (br + 1) / 2;
-        const int r0 = jb + 32 + br * 4, c0 = jb + 32 + bc * 4;
-        float acc[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int p = 0; p < 4; ++p) acc[q][p] = 0.0f;
-#pragma unroll 8
-        for (int m = 0; m < 32; ++m) {
-          float a[4], b[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            a[q] = sC[(r0 + q) * SC_LD + jb + m];
-            b[q] = sC[(c0 + q) * SC_LD + jb + m];
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int p = 0; p < 4; ++p) acc[q][p] = fmaf(a[q], b[p], acc[q][p]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int p = 0; p < 4; ++p) sC[(r0 + q) * SC_LD + c0 + p] -= acc[q][p];
-      }
-      __syncthreads();
-    }
   }
 }
 
