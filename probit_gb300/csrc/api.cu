@@ -724,10 +724,16 @@ int ensure_grad_buffers(Engine& e) {
 int block_cap(const Engine& e) { return e.max_blocks > 0 ? std::min(e.max_blocks, e.num_sms) : e.num_sms; }
 int dag_grid(const Engine& e, int ntasks) { return std::max(1, std::min(block_cap(e), ntasks)); }
 int trsv_grid(const Engine& e) { return std::max(1, std::min(e.nclaims, 4 * block_cap(e))); }
+// Grid of the kernels with one block per map item (Gram and B^-1 matvecs,
+// gradient trace): the whole map, or, on a handle capped to a share of the
+// SMs, twice the cap (the blocks stride over the map), so that these wide
+// launches leave the other SMs free as the persistent ones do.
+int wide_grid(const Engine& e, int nitems) { return e.max_blocks > 0 ? std::min(nitems, 2 * e.max_blocks) : nitems; }
 
 // ---------------------------------------------------------------- enqueue helpers
 void enq_matvec(Engine& e, MatvecOp op, cudaStream_t s) {
-  for (MvGroup& g : e.mv) launch_gram_matvec(g.kind, g.DM, e.probs, g.map, (int)g.h.size(), op, s);
+  for (MvGroup& g : e.mv)
+    launch_gram_matvec(g.kind, g.DM, e.probs, g.map, (int)g.h.size(), wide_grid(e, (int)g.h.size()), op, s);
 }
 
 void enq_dag(Engine& e, int list, cudaStream_t s) {
@@ -822,9 +828,9 @@ void enq_grad(Engine& e, cudaStream_t s) {
   enq_matvec(e, MatvecOp{F_RV, F_NONE, F_ZBAR, 0, 1}, s);
   // u = (I + K W)^-1 zbar = W^-1/2 B^-1 W^1/2 zbar
   launch_scale_tz(e.probs, e.vmap, e.nvb, s);
-  launch_binv_matvec(e.probs, e.bmap, e.nbb, s);
+  launch_binv_matvec(e.probs, e.bmap, e.nbb, wide_grid(e, e.nbb), s);
   launch_grad_vec3(e.probs, e.vmap, e.nvb, s);
-  for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), s);
+  for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), wide_grid(e, (int)g.h.size()), s);
   launch_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
 }
 
@@ -907,7 +913,7 @@ void enq_epilogue(Engine& e, int op, cudaStream_t s) {
     enq_dag(e, TL_IDENT, s);   // L^-T on the resident factor
     cudaMemsetAsync(e.counters + C_SYRK, 0, sizeof(int), s);
     launch_syrk_zzt(e.probs, e.syrk_tiles, e.nsyrk, e.counters + C_SYRK, dag_grid(e, e.nsyrk), s);   // B^-1
-    for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), s);
+    for (TraceGroup& g : e.tr) launch_grad_trace(g.DM, g.periodic, e.probs, g.tiles, (int)g.h.size(), wide_grid(e, (int)g.h.size()), s);
     launch_vb_grad_lik_final(e.probs, e.vmap, e.nvb, e.nprob, s);
     return;
   }

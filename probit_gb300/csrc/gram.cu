@@ -207,15 +207,22 @@ __device__ __forceinline__ float* prob_field(const Prob& P, int f) {
   }
 }
 
+// One map item (problem, row block) per block; a grid smaller than the map
+// (a handle whose launches are capped to a share of the SMs) strides over it.
 template <int MATERN, int DM, bool HAS_M>
 __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(const Prob* __restrict__ probs,
-                                                                 const int2* __restrict__ mvmap, MatvecOp op) {
-  const int2 m = mvmap[blockIdx.x];
-  const Prob& P = probs[m.x];
-  if (op.only_active && *P.active == 0) return;
-  const int n = P.sh.n;
-  mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
-                           prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>(), op.accumulate != 0);
+                                                                 const int2* __restrict__ mvmap, int nitems,
+                                                                 MatvecOp op) {
+  for (int b = blockIdx.x; b < nitems; b += gridDim.x) {
+    const int2 m = mvmap[b];
+    const Prob& P = probs[m.x];
+    if (op.only_active && *P.active == 0) continue;
+    const int n = P.sh.n;
+    mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
+                             prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>(),
+                             op.accumulate != 0);
+    __syncthreads();   // the next item's staging overwrites the shared rows
+  }
 }
 
 template <int MATERN, int DM>
@@ -228,30 +235,32 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_raw_kernel(Shape sh, c
 }
 
 template <int MATERN, int DM>
-static void mv_launch(const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
+static void mv_launch(const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op, cudaStream_t st) {
   if (op.use_binv)
-    gram_matvec_kernel<MATERN, DM, true><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
+    gram_matvec_kernel<MATERN, DM, true><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
   else
-    gram_matvec_kernel<MATERN, DM, false><<<nblocks, MV_THREADS, 0, st>>>(probs, mvmap, op);
+    gram_matvec_kernel<MATERN, DM, false><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
 }
 
 template <int MATERN>
-static void mv_launch_d(int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op, cudaStream_t st) {
+static void mv_launch_d(int DM, const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op,
+                        cudaStream_t st) {
   if (DM <= 4)
-    mv_launch<MATERN, 4>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 4>(probs, mvmap, nitems, grid, op, st);
   else if (DM <= 8)
-    mv_launch<MATERN, 8>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 8>(probs, mvmap, nitems, grid, op, st);
   else
-    mv_launch<MATERN, 16>(probs, mvmap, nblocks, op, st);
+    mv_launch<MATERN, 16>(probs, mvmap, nitems, grid, op, st);
 }
 
-void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
+void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op,
                         cudaStream_t st) {
-  if (nblocks <= 0) return;
+  if (nitems <= 0) return;
+  grid = grid > 0 && grid < nitems ? grid : nitems;
   if (kind == PGB_KERNEL_MATERN12)
-    mv_launch_d<1>(DM, probs, mvmap, nblocks, op, st);
+    mv_launch_d<1>(DM, probs, mvmap, nitems, grid, op, st);
   else
-    mv_launch_d<0>(DM, probs, mvmap, nblocks, op, st);
+    mv_launch_d<0>(DM, probs, mvmap, nitems, grid, op, st);
 }
 
 template <int MATERN>
@@ -278,11 +287,9 @@ void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr
 }
 
 // ---------------------------------------------------------------- B^-1 matvec
-// y2[r] = sum_c B^-1[r, c] tz[c]: one warp per row, 8 rows per block
-// (bmap: block -> (problem, row block)).
-__global__ void __launch_bounds__(256) binv_matvec_kernel(const Prob* __restrict__ probs,
-                                                          const int2* __restrict__ bmap) {
-  const int2 m = bmap[blockIdx.x];
+// One map item of binv_matvec_kernel (no shared memory, no barrier: a warp
+// whose row is past n returns on its own).
+__device__ __forceinline__ void binv_matvec_item(const Prob* __restrict__ probs, int2 m) {
   const Prob& P = probs[m.x];
   if (*P.active == 0) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -308,8 +315,18 @@ __global__ void __launch_bounds__(256) binv_matvec_kernel(const Prob* __restrict
   if (lane == 0) P.y2[r] = s;
 }
 
-void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaStream_t st) {
-  if (nblocks > 0) binv_matvec_kernel<<<nblocks, 256, 0, st>>>(probs, bmap);
+// y2[r] = sum_c B^-1[r, c] tz[c]: one warp per row, 8 rows per map item
+// (bmap: item -> (problem, row block)); a grid smaller than the map strides
+// over it.
+__global__ void __launch_bounds__(256) binv_matvec_kernel(const Prob* __restrict__ probs,
+                                                          const int2* __restrict__ bmap, int nitems) {
+  for (int b = blockIdx.x; b < nitems; b += gridDim.x) binv_matvec_item(probs, bmap[b]);
+}
+
+void launch_binv_matvec(const Prob* probs, const int2* bmap, int nitems, int grid, cudaStream_t st) {
+  if (nitems <= 0) return;
+  grid = grid > 0 && grid < nitems ? grid : nitems;
+  binv_matvec_kernel<<<grid, 256, 0, st>>>(probs, bmap, nitems);
 }
 
 // ---------------------------------------------------------------- gradient trace
@@ -323,10 +340,8 @@ void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaSt
 // tiles: (problem, I, J, ordinal of the tile within its problem); each block
 // writes its partial sums (double) to tpart[ordinal * (nl + 1) + k].
 template <int DM, bool PER>
-__global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict__ probs,
-                                                         const int4* __restrict__ tiles) {
+__device__ __forceinline__ void grad_trace_tile(const Prob* __restrict__ probs, const int4 tl) {
   constexpr int ND = PER ? DM / 2 : DM;   // input dimensions covered
-  const int4 tl = tiles[blockIdx.x];
   const Prob& P = probs[tl.x];
   if (*P.active == 0) return;
   const int I = tl.y, J = tl.z, ord = tl.w;
@@ -422,22 +437,35 @@ __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict_
   }
 }
 
-void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st) {
+// One tile per block; a grid smaller than the tile list (a handle whose
+// launches are capped to a share of the SMs) strides over it.
+template <int DM, bool PER>
+__global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict__ probs,
+                                                         const int4* __restrict__ tiles, int ntiles) {
+  for (int b = blockIdx.x; b < ntiles; b += gridDim.x) {
+    grad_trace_tile<DM, PER>(probs, tiles[b]);
+    __syncthreads();   // the next tile's staging overwrites the shared rows and sums
+  }
+}
+
+void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, int grid,
+                       cudaStream_t st) {
   if (ntiles <= 0) return;
+  grid = grid > 0 && grid < ntiles ? grid : ntiles;
   if (periodic) {
     if (DM <= 4)
-      grad_trace_kernel<4, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<4, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
     else if (DM <= 8)
-      grad_trace_kernel<8, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<8, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
     else
-      grad_trace_kernel<16, true><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<16, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
   } else {
     if (DM <= 4)
-      grad_trace_kernel<4, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<4, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
     else if (DM <= 8)
-      grad_trace_kernel<8, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<8, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
     else
-      grad_trace_kernel<16, false><<<ntiles, 256, 0, st>>>(probs, tiles);
+      grad_trace_kernel<16, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
   }
 }
 

@@ -147,16 +147,17 @@ struct MatvecOp {
 };
 // y (+)= row_scale * ((K [o B^-1]) v) for every problem of one (kind, DM)
 // group; mvmap: block -> (problem, row block of 128 / DM rows).
-void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nblocks, MatvecOp op,
+void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op,
                         cudaStream_t st);
 // Stand-alone Gram matvec over explicit pointers (predict mean).
 void launch_gram_matvec_raw(const Shape& sh, const float* theta, const float* Xr, int nr, const float* Xc, int nc,
                             const float* v, float* y, cudaStream_t st);
 // y2 = B^-1 tz, 8 rows per block: bmap block -> (problem, row block)
-void launch_binv_matvec(const Prob* probs, const int2* bmap, int nblocks, cudaStream_t st);
+void launch_binv_matvec(const Prob* probs, const int2* bmap, int nitems, int grid, cudaStream_t st);
 // trace partials over the lower tiles (problem, I, J, ordinal) of one
 // (DM, periodic) group
-void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, cudaStream_t st);
+void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, int grid,
+                       cudaStream_t st);
 
 // vec.cu ----------------------------------------------------------------------
 void launch_lik_eval(const Shape& sh, const float* theta, const float* f, const void* y, int n, float* logp,

@@ -18,7 +18,10 @@ one GPU:
   problems run at a time and their launches are capped at ``large_blocks``
   persistent blocks, so the SMs left over always serve small requests (a
   large request's latency then absorbs the overload, a small one's does
-  not);
+  not); small problems' launches can be capped too (``small_blocks``), so
+  that several small requests share the remaining SMs at once instead of
+  queueing behind one another's persistent blocks (a persistent block holds
+  its SM until its launch ends);
 * a model is used by one request at a time (a handle is not thread-safe);
   other requests for it wait in the queue.
 
@@ -149,8 +152,18 @@ class Server:
     """Continuous-batching request server on the current CUDA device."""
 
     def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True,
-                 warm_rows=4096, max_large=1, warm_large=False):
+                 warm_rows=4096, max_large=1, warm_large=False, small_blocks=0, switch_interval=2e-4):
+        import sys
+
         import torch
+
+        # the worker threads, the submitting thread and the caller share one
+        # interpreter lock; CPython hands it over every 5 ms by default, which
+        # puts multiples of 5 ms into the latency of a request whose thread
+        # waits for it.  A serving process sets a shorter interval (process
+        # wide; None leaves it as it is).
+        if switch_interval is not None:
+            sys.setswitchinterval(switch_interval)
 
         self.torch = torch
         self.lib = N.load()
@@ -160,6 +173,7 @@ class Server:
         self.used = 0
         self.small_n = small_n
         self.large_blocks = large_blocks   # SM share of the launches of a problem with n > small_n
+        self.small_blocks = small_blocks   # the same for n <= small_n (0: one block per SM)
         self.max_large = max_large         # large requests running at once (0: no limit)
         self.large_running = 0
         # after the first fit of a small model, its evidence + gradient handle is
@@ -408,8 +422,9 @@ class Server:
     def _create(self, p):
         h = C.c_void_p()
         N.check(self.lib.pgb_gp_create(p.desc(), C.byref(h)), "pgb_gp_create")
-        if p.n > self.small_n and self.large_blocks:
-            N.check(self.lib.pgb_gp_set_max_blocks(h, self.large_blocks), "pgb_gp_set_max_blocks")
+        cap = self.large_blocks if p.n > self.small_n else self.small_blocks
+        if cap:
+            N.check(self.lib.pgb_gp_set_max_blocks(h, cap), "pgb_gp_set_max_blocks")
         return h
 
     def _warm_vg(self, m, stream):

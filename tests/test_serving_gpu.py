@@ -18,8 +18,8 @@ def _fits(problems):
     return [S.Request(0.0, "fit", k, p) for k, p in enumerate(problems)]
 
 
-def _run(problems, requests, workers, sequential):
-    srv = S.Server(workers=workers, mem_budget=8 << 30)
+def _run(problems, requests, workers, sequential, **server_kw):
+    srv = S.Server(workers=workers, mem_budget=8 << 30, **server_kw)
     try:
         srv.replay(_fits(problems), realtime=False)
         if sequential:
@@ -50,6 +50,22 @@ def test_same_alone_and_in_the_mix(trace):
         for x, y in zip(a.result, m.result):
             assert np.array_equal(np.asarray(x), np.asarray(y)), (a.kind, a.model)
     assert kinds == {"fit", "vg", "predict"}
+
+
+@pytest.mark.gpu
+def test_block_caps_keep_results(trace):
+    """Capping a model's launches to a few blocks (the persistent ones, and
+    the matvec / gradient-trace grids, whose blocks then stride over their
+    maps) changes no bit of any result."""
+    problems, requests = trace
+    free = _run(problems, _clone(requests), workers=4, sequential=False)
+    capped = _run(problems, _clone(requests), workers=4, sequential=False, small_n=300, large_blocks=2,
+                  small_blocks=3, max_large=2)
+    assert any(p.n > 300 for p in problems) and any(p.n <= 300 for p in problems)
+    for a, m in zip(free, capped):
+        assert a.error is None and m.error is None, (a.error, m.error)
+        for x, y in zip(a.result, m.result):
+            assert np.array_equal(np.asarray(x), np.asarray(y)), (a.kind, a.model)
 
 
 @pytest.mark.gpu
