@@ -38,6 +38,12 @@ from pathlib import Path
 
 import numpy as np
 
+# Hardware work queues of the CUDA context (read when it is created): the
+# serving section drives 24 streams at once; with the default 8 queues a
+# small request's kernel can wait behind a large request's launch that only
+# shares its queue.
+os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
+
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
@@ -75,9 +81,11 @@ def parse():
     ap.add_argument("--serve-seconds", type=float, default=10.0,
                     help="arrival window of the serving workload at 2000 req/s (0: skip)")
     ap.add_argument("--serve-workers", type=int, default=12)
-    ap.add_argument("--serve-max-large", type=int, default=1,
+    ap.add_argument("--serve-max-large", type=int, default=5,
                     help="large (n > 2048) requests served at once (the rest of the GPU serves small ones)")
-    ap.add_argument("--serve-large-blocks", type=int, default=64, help="SM share of each large request's launches")
+    ap.add_argument("--serve-large-blocks", type=int, default=24, help="SM share of each large request's launches")
+    ap.add_argument("--serve-small-blocks", type=int, default=32,
+                    help="SM share of each small request's launches (0: one block per SM)")
     ap.add_argument("--no-c0", action="store_true", help="skip the config-0 section")
     return ap.parse_args()
 
@@ -557,13 +565,13 @@ def run_serving(args, dev):
     from probit_gb300 import workloads as Wk
 
     out = {"workers": args.serve_workers, "pool": 256, "max_large": args.serve_max_large,
-           "large_blocks": args.serve_large_blocks}
+           "large_blocks": args.serve_large_blocks, "small_blocks": args.serve_small_blocks}
     for tag, rate, dur, seed in (("offered_2000_per_s", 2000.0, args.serve_seconds, 4),
                                  ("offered_150_per_s", 150.0, max(5.0, args.serve_seconds), 5)):
         probs, reqs = Wk.serving_c4(rate=rate, duration=dur, pool=256, seed=seed, device=dev)
         gc.collect()   # the previous run's objects are not collected during this one
         srv = S.Server(workers=args.serve_workers, max_large=args.serve_max_large,
-                       large_blocks=args.serve_large_blocks, warm_large=True)
+                       large_blocks=args.serve_large_blocks, small_blocks=args.serve_small_blocks, warm_large=True)
         try:
             t0 = time.perf_counter()
             srv.replay([S.Request(0.0, "fit", k, p) for k, p in enumerate(probs)], realtime=False)

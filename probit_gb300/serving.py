@@ -18,10 +18,12 @@ one GPU:
   problems run at a time and their launches are capped at ``large_blocks``
   persistent blocks, so the SMs left over always serve small requests (a
   large request's latency then absorbs the overload, a small one's does
-  not); small problems' launches can be capped too (``small_blocks``), so
+  not); small problems' launches are capped too (``small_blocks``), so
   that several small requests share the remaining SMs at once instead of
   queueing behind one another's persistent blocks (a persistent block holds
-  its SM until its launch ends);
+  its SM until its launch ends); the streams need as many hardware work
+  queues (``CUDA_DEVICE_MAX_CONNECTIONS``, set before CUDA is initialised),
+  or requests on streams that share a queue wait for each other;
 * a model is used by one request at a time (a handle is not thread-safe);
   other requests for it wait in the queue.
 
@@ -151,11 +153,29 @@ class _Model:
 class Server:
     """Continuous-batching request server on the current CUDA device."""
 
-    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=64, small_only=4, warm_small=True,
-                 warm_rows=4096, max_large=1, warm_large=False, small_blocks=0, switch_interval=2e-4):
+    def __init__(self, workers=12, mem_budget=None, small_n=2048, large_blocks=24, small_only=4, warm_small=True,
+                 warm_rows=4096, max_large=5, warm_large=False, small_blocks=32, switch_interval=2e-4):
+        import os
         import sys
+        import warnings
 
         import torch
+
+        # Every worker drives two streams.  The CUDA context multiplexes streams
+        # onto a fixed number of hardware work queues (CUDA_DEVICE_MAX_CONNECTIONS,
+        # 8 unless set, read when the context is created); streams that share a
+        # queue are ordered, so a small request's kernel could wait behind a
+        # large request's launch.  Before the context exists the server asks
+        # for enough queues; after, it can only warn.
+        want = min(32, 2 * workers)
+        have = os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")
+        if not torch.cuda.is_initialized():
+            if have is None:
+                os.environ["CUDA_DEVICE_MAX_CONNECTIONS"] = str(max(want, 8))
+        elif int(have or 8) < want:
+            warnings.warn(f"CUDA_DEVICE_MAX_CONNECTIONS={have or 8} < {want} streams: requests on streams that "
+                          "share a hardware queue are serialised; set it before CUDA is initialised",
+                          RuntimeWarning, stacklevel=2)
 
         # the worker threads, the submitting thread and the caller share one
         # interpreter lock; CPython hands it over every 5 ms by default, which
