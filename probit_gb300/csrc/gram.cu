@@ -207,21 +207,30 @@ __device__ __forceinline__ float* prob_field(const Prob& P, int f) {
   }
 }
 
-// One map item (problem, row block) per block; a grid smaller than the map
-// (a handle whose launches are capped to a share of the SMs) strides over it.
 template <int MATERN, int DM, bool HAS_M>
+__device__ __forceinline__ void gram_matvec_item(const Prob* __restrict__ probs, int2 m, const MatvecOp& op) {
+  const Prob& P = probs[m.x];
+  if (op.only_active && *P.active == 0) return;
+  const int n = P.sh.n;
+  mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
+                           prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>(), op.accumulate != 0);
+}
+
+// One map item (problem, row block) per block.  STRIDE: the grid is smaller
+// than the map (a handle whose launches are capped to a share of the SMs)
+// and the blocks stride over it; a separate instantiation, so the one-item
+// kernel keeps its own register allocation.
+template <int MATERN, int DM, bool HAS_M, bool STRIDE>
 __global__ void __launch_bounds__(MV_THREADS) gram_matvec_kernel(const Prob* __restrict__ probs,
                                                                  const int2* __restrict__ mvmap, int nitems,
                                                                  MatvecOp op) {
-  for (int b = blockIdx.x; b < nitems; b += gridDim.x) {
-    const int2 m = mvmap[b];
-    const Prob& P = probs[m.x];
-    if (op.only_active && *P.active == 0) continue;
-    const int n = P.sh.n;
-    mv_core<MATERN, DM, HAS_M>(P.sh, P.theta, P.Xf, n, P.Xf, n, P.Binv, P.ld, prob_field(P, op.v),
-                             prob_field(P, op.row_scale), prob_field(P, op.y), m.y * mv_rows<DM>(),
-                             op.accumulate != 0);
-    __syncthreads();   // the next item's staging overwrites the shared rows
+  if constexpr (!STRIDE) {
+    gram_matvec_item<MATERN, DM, HAS_M>(probs, mvmap[blockIdx.x], op);
+  } else {
+    for (int b = blockIdx.x; b < nitems; b += gridDim.x) {
+      gram_matvec_item<MATERN, DM, HAS_M>(probs, mvmap[b], op);
+      __syncthreads();   // the next item's staging overwrites the shared rows
+    }
   }
 }
 
@@ -236,10 +245,18 @@ __global__ void __launch_bounds__(MV_THREADS) gram_matvec_raw_kernel(Shape sh, c
 
 template <int MATERN, int DM>
 static void mv_launch(const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op, cudaStream_t st) {
-  if (op.use_binv)
-    gram_matvec_kernel<MATERN, DM, true><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
-  else
-    gram_matvec_kernel<MATERN, DM, false><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
+  const bool stride = grid < nitems;
+  if (op.use_binv) {
+    if (stride)
+      gram_matvec_kernel<MATERN, DM, true, true><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
+    else
+      gram_matvec_kernel<MATERN, DM, true, false><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
+  } else {
+    if (stride)
+      gram_matvec_kernel<MATERN, DM, false, true><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
+    else
+      gram_matvec_kernel<MATERN, DM, false, false><<<grid, MV_THREADS, 0, st>>>(probs, mvmap, nitems, op);
+  }
 }
 
 template <int MATERN>
@@ -437,15 +454,28 @@ __device__ __forceinline__ void grad_trace_tile(const Prob* __restrict__ probs, 
   }
 }
 
-// One tile per block; a grid smaller than the tile list (a handle whose
-// launches are capped to a share of the SMs) strides over it.
-template <int DM, bool PER>
+// One tile per block.  STRIDE: the grid is smaller than the tile list (a
+// handle whose launches are capped to a share of the SMs) and the blocks
+// stride over it (a separate instantiation, as for the Gram matvec).
+template <int DM, bool PER, bool STRIDE>
 __global__ void __launch_bounds__(256) grad_trace_kernel(const Prob* __restrict__ probs,
                                                          const int4* __restrict__ tiles, int ntiles) {
-  for (int b = blockIdx.x; b < ntiles; b += gridDim.x) {
-    grad_trace_tile<DM, PER>(probs, tiles[b]);
-    __syncthreads();   // the next tile's staging overwrites the shared rows and sums
+  if constexpr (!STRIDE) {
+    grad_trace_tile<DM, PER>(probs, tiles[blockIdx.x]);
+  } else {
+    for (int b = blockIdx.x; b < ntiles; b += gridDim.x) {
+      grad_trace_tile<DM, PER>(probs, tiles[b]);
+      __syncthreads();   // the next tile's staging overwrites the shared rows and sums
+    }
   }
+}
+
+template <int DM, bool PER>
+static void trace_launch(const Prob* probs, const int4* tiles, int ntiles, int grid, cudaStream_t st) {
+  if (grid < ntiles)
+    grad_trace_kernel<DM, PER, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+  else
+    grad_trace_kernel<DM, PER, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
 }
 
 void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tiles, int ntiles, int grid,
@@ -454,18 +484,18 @@ void launch_grad_trace(int DM, int periodic, const Prob* probs, const int4* tile
   grid = grid > 0 && grid < ntiles ? grid : ntiles;
   if (periodic) {
     if (DM <= 4)
-      grad_trace_kernel<4, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<4, true>(probs, tiles, ntiles, grid, st);
     else if (DM <= 8)
-      grad_trace_kernel<8, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<8, true>(probs, tiles, ntiles, grid, st);
     else
-      grad_trace_kernel<16, true><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<16, true>(probs, tiles, ntiles, grid, st);
   } else {
     if (DM <= 4)
-      grad_trace_kernel<4, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<4, false>(probs, tiles, ntiles, grid, st);
     else if (DM <= 8)
-      grad_trace_kernel<8, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<8, false>(probs, tiles, ntiles, grid, st);
     else
-      grad_trace_kernel<16, false><<<grid, 256, 0, st>>>(probs, tiles, ntiles);
+      trace_launch<16, false>(probs, tiles, ntiles, grid, st);
   }
 }
 
