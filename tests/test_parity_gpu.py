@@ -4,7 +4,8 @@ Bars (the parity contract): negative log evidence within 1e-4 relative of the
 float32 oracle; weight, precision and predictive mean within 1e-4 of the
 largest entry; predictive variance within 1e-4 of the signal variance;
 gradient within 1e-3 of its largest entry; Newton iterations within 1.  Each
-output's error against the float64 oracle is checked to the same bars.
+output's error against the float64 oracle is checked to the same bars, and
+entry by entry (test_elementwise_relative).
 """
 
 import sys
@@ -69,6 +70,33 @@ def test_laplace_parity(name, cuda_device):
     mean2, var2 = gp.predict(g["Xtest"], params, np.array(a), np.array(W))
     assert np.abs(mean2 - mean).max() <= 1e-6 * np.abs(mean).max()
     assert np.abs(var2 - var).max() <= 1e-5 * s
+
+
+def rel_elem(x, ref, floor=0.0):
+    """Largest element-wise relative error, each entry's denominator at least
+    `floor` times the largest reference entry (for outputs that cross 0)."""
+    x, ref = np.asarray(x, np.float64), np.asarray(ref, np.float64)
+    den = np.maximum(np.abs(ref), floor * np.abs(ref).max() + 1e-30)
+    return float((np.abs(x - ref) / den).max())
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", list(CASES))
+def test_elementwise_relative(name, cuda_device):
+    """Entry by entry against the float64 oracle: the precision W (positive)
+    within 1e-4 relative of every entry; the weights a and the predictive mean
+    (which cross zero) within 1e-3 relative with denominators of at least 1%
+    of the largest entry; the predictive variance within 1e-3 relative."""
+    g = np.load(GOLD / f"{name}.npz")
+    p, theta, tol = make(name)
+    gp = pg.LaplaceGP((g["X"], g["y"]), p.prior(), LIK[CASES[name][1]], tolerance=tol)
+    params = p.params()
+    a, W = gp.approximate_posterior(params)
+    mean, var = gp.predict(g["Xtest"], params, a, W)
+    assert rel_elem(W, g["W_f64"]) < 1e-4, rel_elem(W, g["W_f64"])
+    assert rel_elem(a, g["a_f64"], 1e-2) < 1e-3, rel_elem(a, g["a_f64"], 1e-2)
+    assert rel_elem(mean, g["mean_f64"], 1e-2) < 1e-3, rel_elem(mean, g["mean_f64"], 1e-2)
+    assert rel_elem(var, g["var_f64"]) < 1e-3, rel_elem(var, g["var_f64"])
 
 
 @pytest.mark.gpu
