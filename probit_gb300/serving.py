@@ -74,6 +74,25 @@ def handle_bytes(n, d, kind, grad=True, m=0):
     return b
 
 
+def work_queue_setting(workers, current, cuda_initialized):
+    """(value to set CUDA_DEVICE_MAX_CONNECTIONS to or None, warning or None)
+    for a server of `workers` workers, two streams each (at most 32 hardware
+    queues exist).  `current` is the variable's value (None: unset, which
+    means 8).  Before the CUDA context exists an unset variable is set;
+    afterwards a count below the streams only draws a warning."""
+    want = max(8, min(32, 2 * workers))
+    try:
+        have = int(current) if current is not None else None
+    except ValueError:
+        have = None
+    if not cuda_initialized:
+        return (str(want) if current is None else None), None
+    if (have if have is not None else 8) < want:
+        return None, (f"CUDA_DEVICE_MAX_CONNECTIONS={current or 8} < {want} streams: requests on streams that "
+                      "share a hardware queue are serialised; set it before CUDA is initialised")
+    return None, None
+
+
 @dataclass
 class Problem:
     """The data and hyperparameters of one served GP (host arrays)."""
@@ -167,15 +186,12 @@ class Server:
         # queue are ordered, so a small request's kernel could wait behind a
         # large request's launch.  Before the context exists the server asks
         # for enough queues; after, it can only warn.
-        want = min(32, 2 * workers)
-        have = os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS")
-        if not torch.cuda.is_initialized():
-            if have is None:
-                os.environ["CUDA_DEVICE_MAX_CONNECTIONS"] = str(max(want, 8))
-        elif int(have or 8) < want:
-            warnings.warn(f"CUDA_DEVICE_MAX_CONNECTIONS={have or 8} < {want} streams: requests on streams that "
-                          "share a hardware queue are serialised; set it before CUDA is initialised",
-                          RuntimeWarning, stacklevel=2)
+        setting, warning = work_queue_setting(workers, os.environ.get("CUDA_DEVICE_MAX_CONNECTIONS"),
+                                              torch.cuda.is_initialized())
+        if setting is not None:
+            os.environ["CUDA_DEVICE_MAX_CONNECTIONS"] = setting
+        if warning is not None:
+            warnings.warn(warning, RuntimeWarning, stacklevel=2)
 
         # the worker threads, the submitting thread and the caller share one
         # interpreter lock; CPython hands it over every 5 ms by default, which

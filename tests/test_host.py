@@ -303,3 +303,19 @@ def test_dlpack_arrays_of_other_frameworks_are_imported_without_copy():
             return (1, 0)
 
     assert from_dlpack_or_none(Broken()) is None
+
+
+def test_serving_work_queue_setting():
+    """The server asks for one hardware work queue per stream (two per
+    worker, 8..32) before the CUDA context exists, leaves an explicit setting
+    alone, and after the context exists only warns when too few were set."""
+    from probit_gb300.serving import work_queue_setting
+
+    assert work_queue_setting(12, None, False) == ("24", None)
+    assert work_queue_setting(40, None, False) == ("32", None)
+    assert work_queue_setting(2, None, False) == ("8", None)
+    assert work_queue_setting(12, "16", False) == (None, None)       # the user's choice stands
+    assert work_queue_setting(12, "32", True) == (None, None)
+    for current in (None, "8", "bogus"):
+        setting, warning = work_queue_setting(12, current, True)
+        assert setting is None and "share a hardware queue" in warning
