@@ -597,7 +597,7 @@ int engine_init(Engine& e, const pgb_desc* descs, int count) {
         e.mv.push_back(g);
       }
       MvGroup& g = e.mv[gi[key]];
-      const int rows = 128 / DM;
+      const int rows = mv_block_rows(DM);
       for (int blk = 0; blk < ceil_div(descs[p].n, rows); ++blk) g.h.push_back(make_int2(p, blk));
     }
   }

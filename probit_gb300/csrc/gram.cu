@@ -105,15 +105,13 @@ void launch_gram_full(const Shape& sh, const float* theta, const float* X1f, int
 
 // ---------------------------------------------------------------- Gram matvec
 // y[r] = row_scale[r] * sum_c K(xr_r, xc_c) * (M ? M[r, c] : 1) * v[c]
-// One block owns 128 / DM rows and sweeps all columns; the per-row sums are
+// One block owns mv_block_rows(DM) rows and sweeps all columns; the per-row sums are
 // reduced in a fixed order, so results are bitwise reproducible.  The kernel
 // family is a template parameter and every per-entry quantity lives in
 // registers or shared memory.
 constexpr int MV_THREADS = 256;
-// rows per block: 32 for D <= 4, 16 for D <= 8, 8 for D <= 16 (constant
-// unrolled work per column)
 template <int DM>
-constexpr int mv_rows() { return 128 / DM; }
+constexpr int mv_rows() { return mv_block_rows(DM); }
 
 template <int MATERN, int DM>
 __device__ __forceinline__ float kval(const float* xi, const float* xj, float s) {
@@ -142,7 +140,18 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
 #pragma unroll
   for (int r = 0; r < MV_ROWS; ++r) acc[r] = 0.0f;
   const int rmax = min(MV_ROWS, nr - r0);
+  // HAS_M: the column's entries of M (one per row, from HBM) are loaded one
+  // column step ahead, so their latency overlaps the kernel evaluations of
+  // the current step instead of stalling each row's product
+  float mr[HAS_M ? MV_ROWS : 1], mn[HAS_M ? MV_ROWS : 1];
+  auto load_m = [&](float (&dst)[HAS_M ? MV_ROWS : 1], int c) {
+#pragma unroll
+    for (int r = 0; r < (HAS_M ? MV_ROWS : 1); ++r)
+      dst[r] = (HAS_M && r < rmax && c < nc) ? __ldg(M + (size_t)(r0 + r) * ldm + c) : 0.0f;
+  };
+  if constexpr (HAS_M) load_m(mr, threadIdx.x);
   for (int c = threadIdx.x; c < nc; c += MV_THREADS) {
+    if constexpr (HAS_M) load_m(mn, c + MV_THREADS);
     float xc[DM];
 #pragma unroll
     for (int f = 0; f < DM; ++f) xc[f] = f < Dp ? __ldg(Xc + (size_t)c * Dp + f) : 0.0f;
@@ -151,7 +160,7 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
 #pragma unroll
       for (int r = 0; r < MV_ROWS; ++r) {
         float k = kval<MATERN, DM>(sx[r], xc, sv);
-        if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
+        if constexpr (HAS_M) k *= mr[r];
         acc[r] = fmaf(k, vc, acc[r]);
       }
     } else {
@@ -159,10 +168,14 @@ __device__ __forceinline__ void mv_core(const Shape& sh, const float* __restrict
       for (int r = 0; r < MV_ROWS; ++r) {
         if (r < rmax) {
           float k = kval<MATERN, DM>(sx[r], xc, sv);
-          if (HAS_M) k *= __ldg(M + (size_t)(r0 + r) * ldm + c);
+          if constexpr (HAS_M) k *= mr[r];
           acc[r] = fmaf(k, vc, acc[r]);
         }
       }
+    }
+    if constexpr (HAS_M) {
+#pragma unroll
+      for (int r = 0; r < MV_ROWS; ++r) mr[r] = mn[r];
     }
   }
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;

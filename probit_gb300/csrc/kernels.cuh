@@ -145,8 +145,13 @@ struct MatvecOp {
   int only_active;  // skip problems whose Newton loop has stopped
   int accumulate;   // y += result instead of y = result
 };
+// Rows of one Gram-matvec map item (one block): 16 for up to 8 features,
+// 8 for 16.  A row's sum does not depend on it (every block sweeps all
+// columns in the same order); it sets the grid (n / rows blocks) and the
+// feature reloads (each block reads every column's features once).
+constexpr int mv_block_rows(int DM) { return DM <= 8 ? 16 : 8; }
 // y (+)= row_scale * ((K [o B^-1]) v) for every problem of one (kind, DM)
-// group; mvmap: block -> (problem, row block of 128 / DM rows).
+// group; mvmap: block -> (problem, row block of mv_block_rows(DM) rows).
 void launch_gram_matvec(int kind, int DM, const Prob* probs, const int2* mvmap, int nitems, int grid, MatvecOp op,
                         cudaStream_t st);
 // Stand-alone Gram matvec over explicit pointers (predict mean).
