@@ -386,20 +386,25 @@ __device__ __forceinline__ void grad_trace_tile(const Prob* __restrict__ probs, 
   const float* __restrict__ sw = P.sw;
   const float* __restrict__ cvec = P.c;
   const float* __restrict__ avec = P.a;
-  __shared__ float sxc[T][DM];
-  __shared__ float ssw[T], sc[T], sa[T];
+  // features and per-point vectors of the tile's columns (J) and rows (I)
+  __shared__ float sxc[T][DM], sxr[T][DM];
+  __shared__ float ssw[T], sc[T], sa[T], sswr[T], scr[T], sar[T];
   __shared__ float sinvl[MAX_D];
   __shared__ double sred[8][MAX_D + 1];
   for (int e = threadIdx.x; e < T * DM; e += 256) {
     const int c = e / DM, f = e % DM;
-    const int gc = J * T + c;
+    const int gc = J * T + c, gr = I * T + c;
     sxc[c][f] = (gc < n && f < sh.Dp) ? Xf[(size_t)gc * sh.Dp + f] : 0.0f;
+    sxr[c][f] = (gr < n && f < sh.Dp) ? Xf[(size_t)gr * sh.Dp + f] : 0.0f;
   }
   for (int c = threadIdx.x; c < T; c += 256) {
-    const int gc = J * T + c;
+    const int gc = J * T + c, gr = I * T + c;
     ssw[c] = gc < n ? sw[gc] : 0.0f;
     sc[c] = gc < n ? cvec[gc] : 0.0f;
     sa[c] = gc < n ? avec[gc] : 0.0f;
+    sswr[c] = gr < n ? sw[gr] : 0.0f;
+    scr[c] = gr < n ? cvec[gr] : 0.0f;
+    sar[c] = gr < n ? avec[gr] : 0.0f;
   }
   if (threadIdx.x < MAX_D) sinvl[threadIdx.x] = threadIdx.x < sh.nl ? 1.0f / __ldg(P.theta + threadIdx.x) : 0.0f;
   __syncthreads();
@@ -410,14 +415,23 @@ __device__ __forceinline__ void grad_trace_tile(const Prob* __restrict__ probs, 
   const int c = threadIdx.x & (T - 1);
   const int rh = threadIdx.x >> 7;  // 0 or 1
   const int gc = J * T + c;
+  // this thread's entries of B^-1 are loaded two of its rows ahead, so their
+  // latency overlaps the kernel evaluations of the rows before them
+  auto load_b = [&](int r) {
+    const int gr = I * T + r;
+    return (r < T && gr < n && gc < n && gc <= gr) ? __ldcg(Binv + (size_t)gr * ld + gc) : 0.0f;
+  };
+  float b0 = load_b(rh), b1 = load_b(rh + 2);
   for (int r = rh; r < T; r += 2) {
     const int gr = I * T + r;
+    const float bij = b0;
+    b0 = b1;
+    b1 = load_b(r + 4);
     if (gr >= n || gc >= n || gc > gr) continue;
     float xr[DM];
 #pragma unroll
-    for (int f = 0; f < DM; ++f) xr[f] = f < sh.Dp ? __ldg(Xf + (size_t)gr * sh.Dp + f) : 0.0f;
-    const float swr = __ldg(sw + gr), cr = __ldg(cvec + gr), ar = __ldg(avec + gr);
-    const float bij = __ldcg(Binv + (size_t)gr * ld + gc);
+    for (int f = 0; f < DM; ++f) xr[f] = sxr[r][f];
+    const float swr = sswr[r], cr = scr[r], ar = sar[r];
     float m;
     if (gr == gc)
       m = 0.5f * swr * bij * swr + cr * ar;
