@@ -72,6 +72,33 @@ def test_gaussian_evidence_is_exact_marginal_likelihood():
 
 
 @pytest.mark.parametrize("kind", L.KERNELS)
+def test_gaussian_prediction_is_exact_gp_posterior(kind):
+    """With a Gaussian likelihood the Laplace approximation is exact: the
+    weight is (K + s^2 I)^-1 y, W = 1/s^2, and predict / predict_covariance
+    are the GP posterior mean, variance and covariance (computed here with a
+    Cholesky solve, independently of the oracle's own formulas)."""
+    prob, theta = _small(kind, "gaussian", N=60)
+    ell, s, sig, _ = prob.split(theta)
+    rng = np.random.default_rng(3)
+    Xs = rng.uniform(-2.5, 2.5, size=(25, prob.X.shape[1]))
+    a, _ = L.newton_weight(prob, theta, tol=1e-12)
+    W, _ = L.precision(prob, theta, a)
+    Kxx = L.gram(kind, prob.X, prob.X, ell, s, prob.period) + sig ** 2 * np.eye(60)
+    Kxs = L.gram(kind, prob.X, Xs, ell, s, prob.period)
+    Kss = L.gram(kind, Xs, Xs, ell, s, prob.period)
+    c = np.linalg.cholesky(Kxx)
+    alpha = np.linalg.solve(c.T, np.linalg.solve(c, prob.y))
+    V = np.linalg.solve(c, Kxs)
+    assert np.abs(a - alpha).max() <= 1e-9 * np.abs(alpha).max()
+    assert np.allclose(W, 1.0 / sig ** 2, rtol=1e-12)
+    mean, var = L.predict(prob, theta, Xs, a, W)
+    assert np.abs(mean - Kxs.T @ alpha).max() <= 1e-9 * np.abs(mean).max()
+    assert np.abs(var - (np.diag(Kss) - (V * V).sum(0))).max() <= 1e-9 * s
+    cov = L.predict_covariance(prob, theta, Xs, a, W)
+    assert np.abs(cov - (Kss - V.T @ V)).max() <= 1e-9 * s
+
+
+@pytest.mark.parametrize("kind", L.KERNELS)
 @pytest.mark.parametrize("lik", ["gaussian", "probit", "probit_stable"])
 def test_bform_equals_reference_form(kind, lik):
     prob, theta = _small(kind, lik, N=60, seed=3)
