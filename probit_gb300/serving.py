@@ -196,8 +196,9 @@ class Server:
         # the worker threads, the submitting thread and the caller share one
         # interpreter lock; CPython hands it over every 5 ms by default, which
         # puts multiples of 5 ms into the latency of a request whose thread
-        # waits for it.  A serving process sets a shorter interval (process
-        # wide; None leaves it as it is).
+        # waits for it.  The server sets a shorter interval while it runs
+        # (process wide; close() restores the previous one; None leaves it).
+        self._old_switch = sys.getswitchinterval()
         if switch_interval is not None:
             sys.setswitchinterval(switch_interval)
 
@@ -279,6 +280,8 @@ class Server:
         return bool(self.heaps[0] or self.heaps[1])
 
     def close(self):
+        import sys
+
         with self.lock:
             self.stop = True
             self.lock.notify_all()
@@ -286,6 +289,7 @@ class Server:
             t.join()
         for m in list(self.models.values()):
             self._destroy(m)
+        sys.setswitchinterval(self._old_switch)
 
     # -- admission --------------------------------------------------------------
     def _plan(self, req, m):
